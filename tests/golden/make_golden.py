@@ -1,0 +1,253 @@
+"""Generate the golden vectors in tests/golden/ from the GPUGO reference source.
+
+Run in a container that has the reference checked out (it is read, never
+modified or copied):
+
+    python tests/golden/make_golden.py /path/to/GPUGO
+
+The reference is Numba-CUDA code, and Numba is not installed here.  This script
+executes the reference's own device functions as plain Python by providing a
+stand-in ``numba`` module:
+
+* ``cuda.jit`` returns the function unchanged;
+* ``cuda.libdevice.dadd_rd/ru, dmul_rd/ru, ddiv_rd/ru, drcp_rd/ru`` round the
+  exact rational result (``fractions.Fraction``) in the requested direction;
+* ``cuda.libdevice.pow(x, 2)`` is ``x*x`` and ``pow(x, 0.5)`` is ``sqrt(x)``,
+  both correctly rounded;
+* ``cuda.libdevice.sin/cos/exp`` (closed libdevice code that is not in the
+  reference) are the oracle's own functions, the same ones the CUDA product
+  implements, so value and sample bounds are comparable bit for bit.
+
+The scripts import their folder's old interval module (``import IARastrigin as
+ia``); the stand-in maps that import to the reference's updated library
+``Updated Interval Arithmetic Operations/IA.py``, whose directed-rounding
+semantics the product follows.  Its ``times`` assumes a non-negative scalar
+(IA.py:312) while the Ackley code list passes -0.02 and -20, so the Ackley and
+Griewank vectors are generated with a sign-aware ``times``.
+
+Only the imports and function definitions of each script are executed; its
+top-level statements (the whole 50-variable B&B run) are skipped.
+"""
+from __future__ import annotations
+
+import ast
+import math
+import os
+import sys
+import types
+from fractions import Fraction
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+import oracle  # noqa: E402  (the oracle's transcendentals stand in for libdevice)
+
+DBL_MAX = Fraction(sys.float_info.max)
+
+
+def _round(q: Fraction, up: bool) -> float:
+    if abs(q) > DBL_MAX:
+        if q > 0:
+            return math.inf if up else sys.float_info.max
+        return -sys.float_info.max if up else -math.inf
+    f = float(q)
+    if Fraction(f) == q:
+        return f
+    if up:
+        return f if Fraction(f) > q else float(np.nextafter(f, np.inf))
+    return f if Fraction(f) < q else float(np.nextafter(f, -np.inf))
+
+
+def _nonfinite(*xs):
+    return any(not math.isfinite(float(x)) for x in xs)
+
+
+def _dadd(a, b, up):
+    a = float(a); b = float(b)
+    if _nonfinite(a, b):
+        return np.float64(a + b)
+    q = Fraction(a) + Fraction(b)
+    if q == 0:
+        if a == 0 and b == 0:
+            na, nb = math.copysign(1, a) < 0, math.copysign(1, b) < 0
+            neg = (na and nb) if up else (na or nb)
+            return np.float64(-0.0 if neg else 0.0)
+        return np.float64(0.0 if up else -0.0)
+    return np.float64(_round(q, up))
+
+
+def _dmul(a, b, up):
+    a = float(a); b = float(b)
+    if _nonfinite(a, b) or a == 0 or b == 0:
+        return np.float64(a * b)
+    return np.float64(_round(Fraction(a) * Fraction(b), up))
+
+
+def _ddiv(a, b, up):
+    a = float(a); b = float(b)
+    if _nonfinite(a, b) or a == 0 or b == 0:
+        with np.errstate(all="ignore"):
+            return np.float64(np.float64(a) / np.float64(b))
+    return np.float64(_round(Fraction(a) / Fraction(b), up))
+
+
+def _pow(x, p):
+    x = np.float64(x)
+    if p == 2:
+        return np.float64(x * x)
+    if p == 0.5:
+        return np.float64(np.sqrt(x))
+    raise ValueError(f"pow exponent {p} not used by the four families")
+
+
+def _point(fn):
+    def f(x):
+        return np.float64(oracle.point_fn(fn, np.array([float(x)]))[0])
+    return f
+
+
+def make_numba_stub():
+    numba = types.ModuleType("numba")
+    cuda = types.SimpleNamespace()
+
+    def jit(*args, **kwargs):
+        if args and callable(args[0]):
+            return args[0]
+        return lambda f: f
+
+    lib = types.SimpleNamespace(
+        dadd_rd=lambda a, b: _dadd(a, b, False), dadd_ru=lambda a, b: _dadd(a, b, True),
+        dmul_rd=lambda a, b: _dmul(a, b, False), dmul_ru=lambda a, b: _dmul(a, b, True),
+        ddiv_rd=lambda a, b: _ddiv(a, b, False), ddiv_ru=lambda a, b: _ddiv(a, b, True),
+        drcp_rd=lambda b: _ddiv(1.0, b, False), drcp_ru=lambda b: _ddiv(1.0, b, True),
+        pow=_pow, sin=_point("sin"), cos=_point("cos"), exp=_point("exp"))
+    cuda.jit = jit
+    cuda.libdevice = lib
+    numba.cuda = cuda
+    return numba
+
+
+def load_updated_ia(ref_root: str, sign_aware_times: bool):
+    path = os.path.join(ref_root, "Updated Interval Arithmetic Operations", "IA.py")
+    mod = types.ModuleType("IA_updated")
+    mod.__file__ = path
+    exec(compile(open(path).read(), path, "exec"), mod.__dict__)
+    if sign_aware_times:
+        dmul_rd, dmul_ru = mod.cuda.libdevice.dmul_rd, mod.cuda.libdevice.dmul_ru
+
+        def times(lower, upper, val):
+            if val < 0:
+                return dmul_rd(upper, val), dmul_ru(lower, val)
+            return dmul_rd(lower, val), dmul_ru(upper, val)
+        mod.times = times
+    return mod
+
+
+def load_script(ref_root: str, rel: str, ia_name: str, ia_mod):
+    """Execute the function definitions of one reference script."""
+    path = os.path.join(ref_root, rel)
+    src = open(path).read()
+    tree = ast.parse(src)
+    keep = [node for node in tree.body
+            if isinstance(node, (ast.Import, ast.ImportFrom, ast.FunctionDef))]
+    sys.modules[ia_name] = ia_mod
+    ns: dict = {"__name__": "ref_" + ia_name}
+    exec(compile(ast.Module(body=keep, type_ignores=[]), path, "exec"), ns)
+    return ns
+
+
+FAMILIES = {
+    # name: (script, ia module name, prefix, domain, family id, coef builder, sign-aware times)
+    "rastrigin": ("GPUGO_1.1/7-Rastrigin/rastrigin50.py", "IARastrigin", "rastrigin", (-5.5, 6.0), 1,
+                  lambda n: np.concatenate([np.ones(n), np.full(n, 10.0), np.ones(n)]), False),
+    "rosenbrock": ("GPUGO_1.1/11-Rosenbrock/rosenbrock50.py", "IARosenbrock", "rosenbrock", (-30.0, 30.0), 2,
+                   lambda n: np.concatenate([np.full(n - 1, 100.0), np.ones(n - 1)]), False),
+    "ackley": ("GPUGO_1.1/1-Ackley/ackley50.py", "IAAckley", "ackley", (-35.0, 40.0), 3,
+               lambda n: np.concatenate([[20.0, 0.02], np.ones(n)]), True),
+    "griewank": ("GPUGO_1.1/5-Griewank/griewank50.py", "IAGriewank", "griewank", (-100.0, 110.0), 4,
+                 lambda n: np.array([4000.0]), True),
+}
+N = 50
+WID, GROUP, SAMPLES = 4, 10, 10
+
+
+def parents_for(name, dom, complete, rng):
+    """Parent boxes: the domain, one of its children, and a small box around the minimiser."""
+    lo, hi = dom
+    root = np.tile([lo, hi], N).astype(np.float64)
+    c1 = complete(root, int(rng.integers(0, WID ** GROUP)), 1)
+    xstar = 1.0 if name == "rosenbrock" else 0.0
+    tiny = np.empty(2 * N)
+    for i in range(N):
+        w = float(rng.uniform(0.5, 2.0)) * 1e-3
+        off = float(rng.uniform(-0.4, 0.4)) * w
+        tiny[2 * i] = xstar - w + off
+        tiny[2 * i + 1] = xstar + w + off
+    return [(root, 1), (c1, 11), (tiny, 41)]
+
+
+def main(ref_root: str):
+    oracle.build()
+    sys.modules["numba"] = make_numba_stub()
+    rng = np.random.default_rng(0x6770756F)
+    out = {}
+    for name, (rel, ia_name, pre, dom, fam, coef, sign_times) in FAMILIES.items():
+        ia_mod = load_updated_ia(ref_root, sign_times)
+        ns = load_script(ref_root, rel, ia_name, ia_mod)
+        value = ns[pre + "Value_IA"]
+        sample = ns[pre + "Sample_IA"]
+        deriv = ns[pre + "Derivative_IA"]
+        complete = ns["completeRegion"]
+        select = ns["selectVarInSubRegion"]
+        parents = parents_for(name, dom, complete, rng)
+        pidx, cycs, codes, lbs, flags, samps, dflags = [], [], [], [], [], [], []
+        for k, (pbox, cyc) in enumerate(parents):
+            pos = [int(p) for p in rng.integers(0, WID ** GROUP, 40)] + [0, WID ** GROUP - 1]
+            for p in pos:
+                lb, _ = value(pbox, p, 1e300, 0, cyc)
+                lb = float(lb)
+                # ruleOut value test against a UB just below the LB: must flag 1
+                _, f_lo = value(pbox, p, lb - abs(lb) * 1e-9 - 1e-300, 0, cyc)
+                lbs.append(lb)
+                flags.append(int(f_lo))
+                samps.append(float(sample(pbox, p, SAMPLES, cyc)))
+                # the Ackley gradient code list is not reproduced (see the oracle header)
+                dflags.append(int(deriv(pbox, p, 0, cyc)) if name != "ackley" else -1)
+                pidx.append(k); cycs.append(cyc); codes.append(p)
+        out[name + "_family"] = np.array([fam])
+        out[name + "_coef"] = coef(N)
+        out[name + "_domain"] = np.tile(np.array(dom, dtype=np.float64), N)
+        out[name + "_parents"] = np.stack([pb for pb, _ in parents])
+        out[name + "_parent_idx"] = np.array(pidx, dtype=np.int64)
+        out[name + "_cyc"] = np.array(cycs, dtype=np.int64)
+        out[name + "_code"] = np.array(codes, dtype=np.int64)
+        out[name + "_lb"] = np.array(lbs)
+        out[name + "_flag_below"] = np.array(flags, dtype=np.int64)
+        out[name + "_samp"] = np.array(samps)
+        out[name + "_dflag"] = np.array(dflags, dtype=np.int64)
+        print(name, "cases", len(codes), flush=True)
+        if name == "rastrigin":
+            # box decoder: completeRegion and selectVarInSubRegion on the parents above
+            dec_par, dec_cyc, dec_code, dec_box, dec_sel = [], [], [], [], []
+            for t in range(60):
+                pbox = parents[t % 3][0]
+                cyc = int(rng.choice([1, 11, 21, 31, 41]))
+                p = int(rng.integers(0, WID ** GROUP))
+                box = complete(pbox, p, cyc)
+                sel = np.array([select(pbox, i, p, cyc) for i in range(1, N + 1)], dtype=np.float64).ravel()
+                dec_par.append(t % 3); dec_cyc.append(cyc); dec_code.append(p)
+                dec_box.append(np.asarray(box, dtype=np.float64)); dec_sel.append(sel)
+            out["decoder_parent_idx"] = np.array(dec_par)
+            out["decoder_cyc"] = np.array(dec_cyc)
+            out["decoder_code"] = np.array(dec_code)
+            out["decoder_complete"] = np.stack(dec_box)
+            out["decoder_select"] = np.stack(dec_sel)
+    dst = os.path.join(HERE, "reference_vectors.npz")
+    np.savez_compressed(dst, **out)
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
