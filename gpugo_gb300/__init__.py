@@ -1,0 +1,227 @@
+"""gpugo_gb300 -- interval branch-and-bound global optimisation on GB300.
+
+The per-problem call of the reference (one GPUGO script: objective, box domain
+and stopping rule in; enclosure of the global minimum and surviving boxes out,
+GPUGO_1.1/1-Ackley/ackley50.py:950-1396) is :func:`solve`.  :func:`eval_children`
+is one sampling + ruleOutGPU pass (ackley50.py:602-766) over chosen children,
+and :class:`Engine` runs many solves in one persistent kernel (batching and
+serving).  All compute runs in libgpugo.so (hand-written CUDA for sm_103a);
+Python only marshals arguments.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import CERTIFIED, FINISHED, ITER_LIMIT, GpugoError
+from .problems import (CHAINED, COSQUAD, EXPSQRT, PRODCOS, STOP_GAP, STOP_WIDTH, Problem, config1, config2,
+                       config3, config4, config5, instance)
+
+__all__ = ["solve", "eval_children", "Engine", "SolveResult", "Problem", "GpugoError", "instance", "config1",
+           "config2", "config3", "config4", "config5", "COSQUAD", "CHAINED", "EXPSQRT", "PRODCOS",
+           "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info"]
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _spec(p: Problem):
+    dom = np.ascontiguousarray(p.domain, dtype=np.float64)
+    coef = np.ascontiguousarray(p.coef, dtype=np.float64)
+    s = _lib.Spec(int(p.family), int(p.n), int(p.wid), int(p.group), int(p.samples), int(p.stop_mode),
+                  float(p.width_tol), float(p.gap_tol), float(p.ub_init),
+                  dom.ctypes.data_as(_dp), coef.ctypes.data_as(_dp), coef.size, int(p.max_iter or 0),
+                  int(p.pool_cap or 0), int(p.parent_cap or 0))
+    return s, (dom, coef)
+
+
+@dataclass
+class SolveResult:
+    """Outcome of one solve: the reference prints ``[lb, ub]``, the output
+    regions, the elapsed time and the iteration count (ackley50.py:1384-1395)."""
+    lb: float
+    ub: float
+    status: int
+    iterations: int
+    boxes_bounded: int
+    samples_evaluated: int
+    pool_size: int
+    n_boxes: int
+    boxes: np.ndarray            # [k, n, 2]
+    box_lbs: np.ndarray
+    xhat: np.ndarray | None      # sample point whose upper bound is ub
+    device_ms: float = 0.0
+    trace: dict = field(default_factory=dict)
+
+    @property
+    def certified(self) -> bool:
+        return self.status == CERTIFIED
+
+    @property
+    def gap(self) -> float:
+        return self.ub - self.lb
+
+
+def _alloc_out(p: Problem, cap: int, trace_cap: int):
+    boxes = np.zeros((max(cap, 1), 2 * p.n))
+    lbs = np.zeros(max(cap, 1))
+    xhat = np.zeros(p.n)
+    tr = arrs = None
+    if trace_cap > 0:
+        arrs = (np.zeros(trace_cap), np.zeros(trace_cap, np.int64), np.zeros(trace_cap, np.int64),
+                np.zeros(trace_cap, np.int64))
+        i64 = ctypes.POINTER(ctypes.c_int64)
+        tr = _lib.Trace(trace_cap, arrs[0].ctypes.data_as(_dp), arrs[1].ctypes.data_as(i64),
+                        arrs[2].ctypes.data_as(i64), arrs[3].ctypes.data_as(i64))
+    return boxes, lbs, xhat, tr, arrs
+
+
+def _result(p: Problem, r, boxes, lbs, xhat, arrs) -> SolveResult:
+    k = int(r.n_out)
+    trace = {}
+    if arrs is not None:
+        m = min(int(r.iterations), arrs[0].size)
+        trace = {"ub": arrs[0][:m].copy(), "n_surv": arrs[1][:m].copy(), "pool": arrs[2][:m].copy(),
+                 "sel": arrs[3][:m].copy()}
+    return SolveResult(float(r.lb), float(r.ub), int(r.status), int(r.iterations), int(r.boxes_bounded),
+                       int(r.samples_evaluated), int(r.pool_size), int(r.n_boxes),
+                       boxes[:k].reshape(k, p.n, 2).copy(), lbs[:k].copy(),
+                       xhat.copy() if r.has_xhat else None, float(r.device_ms), trace)
+
+
+def solve(p: Problem, box_cap: int = 1024, trace_cap: int = 0) -> SolveResult:
+    """Solve one problem on the GPU (libgpugo.so ``gpugo_solve``)."""
+    L = _lib.load()
+    s, keep = _spec(p)
+    boxes, lbs, xhat, tr, arrs = _alloc_out(p, box_cap, trace_cap)
+    r = _lib.Result()
+    rc = L.gpugo_solve(ctypes.byref(s), ctypes.byref(r), boxes.ctypes.data_as(_dp), lbs.ctypes.data_as(_dp),
+                       box_cap, xhat.ctypes.data_as(_dp), ctypes.byref(tr) if tr is not None else None)
+    _lib.check(rc, "gpugo_solve")
+    return _result(p, r, boxes, lbs, xhat, arrs)
+
+
+def eval_children(p: Problem, parent_box: np.ndarray, cyc: int, codes: np.ndarray, ub: float):
+    """Per child: lower bound, smallest sampled upper bound, ruleOutGPU flag."""
+    L = _lib.load()
+    s, keep = _spec(p)
+    pb = np.ascontiguousarray(parent_box, dtype=np.float64).ravel()
+    codes = np.ascontiguousarray(codes, dtype=np.uint64).ravel()
+    m = codes.size
+    lb = np.empty(m)
+    samp = np.empty(m)
+    flag = np.empty(m, dtype=np.int32)
+    rc = L.gpugo_eval_children(ctypes.byref(s), pb.ctypes.data_as(_dp), int(cyc),
+                               codes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), m, float(ub),
+                               lb.ctypes.data_as(_dp), samp.ctypes.data_as(_dp),
+                               flag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    _lib.check(rc, "gpugo_eval_children")
+    return lb, samp, flag
+
+
+def device_info() -> tuple[int, int]:
+    L = _lib.load()
+    sm = ctypes.c_int32()
+    nsm = ctypes.c_int32()
+    _lib.check(L.gpugo_device_info(ctypes.byref(sm), ctypes.byref(nsm)), "gpugo_device_info")
+    return sm.value, nsm.value
+
+
+def instance_bytes(p: Problem) -> int:
+    L = _lib.load()
+    s, keep = _spec(p)
+    out = ctypes.c_int64()
+    _lib.check(L.gpugo_instance_bytes(ctypes.byref(s), ctypes.byref(out)), "gpugo_instance_bytes")
+    return out.value
+
+
+class Engine:
+    """Many solves resident on one GPU, advanced together by one persistent kernel.
+
+    ``submit`` admits a problem when a slot and enough pool memory are free
+    (``None`` otherwise), ``run`` advances every resident solve, ``poll`` returns
+    the finished ones and frees their memory.
+    """
+
+    def __init__(self, max_slots: int = 1024, arena_bytes: int = 8 << 30, wait_timeout_s: float = 60.0,
+                 blocks_per_sm: int = 0):
+        self._L = _lib.load()
+        cfg = _lib.EngineCfg(int(max_slots), 256, int(arena_bytes), float(wait_timeout_s), int(blocks_per_sm), 0)
+        h = ctypes.c_void_p()
+        _lib.check(self._L.gpugo_engine_create(ctypes.byref(cfg), ctypes.byref(h)), "gpugo_engine_create")
+        self._h = h
+        self._pending: dict[int, tuple] = {}
+        self.max_slots = max_slots
+
+    def close(self):
+        if self._h:
+            self._L.gpugo_engine_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, p: Problem, box_cap: int = 16, trace_cap: int = 0) -> int | None:
+        s, keep = _spec(p)
+        boxes, lbs, xhat, tr, arrs = _alloc_out(p, box_cap, trace_cap)
+        t = ctypes.c_int64()
+        rc = self._L.gpugo_submit(self._h, ctypes.byref(s), boxes.ctypes.data_as(_dp), lbs.ctypes.data_as(_dp),
+                                  box_cap, xhat.ctypes.data_as(_dp), ctypes.byref(tr) if tr is not None else None,
+                                  ctypes.byref(t))
+        if rc == _lib.ERR_BUSY:
+            return None
+        _lib.check(rc, "gpugo_submit")
+        self._pending[t.value] = (p, boxes, lbs, xhat, arrs, tr, keep)
+        return t.value
+
+    def run(self, max_iters: int = 0) -> int:
+        active = ctypes.c_int32()
+        _lib.check(self._L.gpugo_run(self._h, int(max_iters), ctypes.byref(active)), "gpugo_run")
+        return active.value
+
+    def poll(self, max_done: int = 4096) -> list[tuple[int, SolveResult]]:
+        arr = (_lib.Done * max_done)()
+        nd = ctypes.c_int32()
+        _lib.check(self._L.gpugo_poll(self._h, arr, max_done, ctypes.byref(nd)), "gpugo_poll")
+        out = []
+        for i in range(nd.value):
+            t = int(arr[i].ticket)
+            p, boxes, lbs, xhat, arrs, tr, keep = self._pending.pop(t)
+            out.append((t, _result(p, arr[i].result, boxes, lbs, xhat, arrs)))
+        return out
+
+    def free_bytes(self) -> int:
+        out = ctypes.c_int64()
+        _lib.check(self._L.gpugo_engine_free_bytes(self._h, ctypes.byref(out)), "gpugo_engine_free_bytes")
+        return out.value
+
+    def solve_all(self, problems: list[Problem], iters_per_run: int = 0, box_cap: int = 16):
+        """Admit as many problems as fit, run, collect, refill; returns results in input order."""
+        results: list[SolveResult | None] = [None] * len(problems)
+        tickets: dict[int, int] = {}
+        nxt = 0
+        while nxt < len(problems) or tickets:
+            while nxt < len(problems):
+                t = self.submit(problems[nxt], box_cap=box_cap)
+                if t is None:
+                    break
+                tickets[t] = nxt
+                nxt += 1
+            if not tickets:
+                raise GpugoError(-7, f"problem {nxt} does not fit an empty engine")
+            self.run(iters_per_run)
+            for t, r in self.poll():
+                results[tickets.pop(t)] = r
+        return results

@@ -1,0 +1,1465 @@
+// engine.cu -- persistent interval branch-and-bound engine for GB300 (sm_103a).
+//
+// One cooperative kernel runs the reference's iteration loop
+// (GPUGO_1.1/1-Ackley/ackley50.py:950-1396) for every resident instance at once.
+// Each iteration has four phases separated by grid barriers:
+//
+//   A  term tables for each instance's selected parent        (families.cuh)
+//   B  children: lower bound, sample upper bounds -> atomicMin(UB), KKT test,
+//      survivors appended to the instance's box pool          (sampling + ruleOutGPU,
+//                                                              ackley50.py:602-766)
+//   D  pool: drop entries with LB > UB when UB moved, argmin   (ackley50.py:1154-1166,
+//      per 2048-entry tile                                      :768-810, :1273)
+//   E  one warp per instance: pop the best entry, width/gap rule, decode the
+//      next parent into the parent table                       (ackley50.py:1269-1370)
+//
+// Work in A, B and D is a flat list over (instance, item) built by the block that
+// arrives last at the preceding barrier, so one instance or thousands share the
+// same launch.  Samples of a child are evaluated only when its LB is not above the
+// running UB: a skipped child's smallest sampled upper bound is at least its LB,
+// which exceeds the UB, so the final UB of the iteration is unchanged.
+// Every device-side wait is bounded by a %globaltimer budget.
+#include <cuda_runtime.h>
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "ia.cuh"
+#include "families.cuh"
+#include "../../include/gpugo.h"
+
+namespace gg {
+
+constexpr int TD = 2048;           // pool entries per phase-D tile
+constexpr int MAX_THREADS = 512;
+
+// instance life cycle
+enum { ST_FREE = 0, ST_EXPAND = 1, ST_REPOP = 2, ST_DONE = 3 };
+
+struct State {
+  int status;                 // ST_*
+  int outcome;                // GPUGO_CERTIFIED / FINISHED / ITER_LIMIT or GPUGO_ERR_*
+  int cur;                    // live pool buffer
+  int cyc;                    // 1-based first split coordinate of the current parent
+  long long iter;             // expansions so far == parent-table row of the current parent
+  unsigned long long ub;      // ord_key of the UB (atomicMin target)
+  unsigned long long ub_start;
+  unsigned long long ub_who;  // row << 40 | code << 8 | sample index of the point that set the UB
+  long long count;            // entries in the live buffer
+  long long count_new;        // entries written to the other buffer by a compaction
+  long long count_before;     // live entries before this iteration's appends
+  long long removed_new;      // this iteration's appends dropped by the compaction
+  long long out_count;        // boxes emitted by the width rule
+  double out_lb_min;
+  long long bounded;          // children bounded
+  long long samples;          // children whose samples were evaluated
+  long long ubc_count;        // UB candidates recorded this iteration
+  long long m_children;       // children of the current parent
+  long long n_surv_last;
+  int has_who;
+  int pad;
+};
+
+struct Ctl {
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int error;
+  int nA;                     // instances expanding this iteration
+  int nE;                     // instances active this iteration
+  int pad;
+  long long totA, totB, totD; // flat work sizes
+  long long iters;            // iterations run by the last launch
+};
+
+struct KArgs {
+  Desc* desc;
+  State* st;
+  Ctl* ctl;
+  int* idsA;                  // [max_slots]
+  long long* prefA;           // [max_slots + 1]
+  long long* prefB;
+  int* idsE;
+  long long* prefD;
+  int max_slots;
+  long long max_iters;        // iterations in this launch (<= 0: until idle)
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ double atomic_ub_read(const unsigned long long* p) {
+  return ord_val(*(volatile const unsigned long long*)p);
+}
+
+// ---------------------------------------------------------------------------
+// block-wide helpers
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ T block_exclusive_scan(T v, T* total) {
+  __shared__ T s_warp[MAX_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    T w = (lane < nw) ? s_warp[lane] : (T)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) s_warp[lane] = w;
+  }
+  __syncthreads();
+  T base = (wid > 0) ? s_warp[wid - 1] : (T)0;
+  T tot = s_warp[nw - 1];
+  __syncthreads();
+  *total = tot;
+  return base + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// work lists (run by the last block at a barrier)
+// ---------------------------------------------------------------------------
+__device__ long long children_of(const Desc& D, int cyc) {
+  int g = group_size(D.n, D.group, cyc);
+  long long m = 1;
+  for (int i = 0; i < g; ++i) m *= D.wid;
+  return m;
+}
+
+// lists for phases A, B, E from the instance states
+__device__ void build_lists_AE(const KArgs& a) {
+  const int S = a.max_slots;
+  const int per = (S + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(S, lo + per);
+  long long cA = 0, cE = 0, sA = 0, sB = 0;
+  for (int s = lo; s < hi; ++s) {
+    int stt = a.st[s].status;
+    if (stt == ST_EXPAND) { cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children; }
+    if (stt == ST_EXPAND || stt == ST_REPOP) cE++;
+  }
+  long long tA, tE, tSA, tSB;
+  long long oA = block_exclusive_scan(cA, &tA);
+  long long oE = block_exclusive_scan(cE, &tE);
+  long long oSA = block_exclusive_scan(sA, &tSA);
+  long long oSB = block_exclusive_scan(sB, &tSB);
+  for (int s = lo; s < hi; ++s) {
+    int stt = a.st[s].status;
+    if (stt == ST_EXPAND) {
+      a.idsA[oA] = s;
+      a.prefA[oA] = oSA;
+      a.prefB[oA] = oSB;
+      oA++;
+      oSA += a.desc[s].a_items;
+      oSB += a.st[s].m_children;
+    }
+    if (stt == ST_EXPAND || stt == ST_REPOP) a.idsE[oE++] = s;
+  }
+  if (threadIdx.x == 0) {
+    a.prefA[tA] = tSA;
+    a.prefB[tA] = tSB;
+    a.ctl->nA = (int)tA;
+    a.ctl->nE = (int)tE;
+    a.ctl->totA = tSA;
+    a.ctl->totB = tSB;
+  }
+}
+
+__device__ __forceinline__ long long pool_tiles(const Desc& D, const State& st) {
+  long long c = st.count < D.pool_cap ? st.count : D.pool_cap;
+  return (c + TD - 1) / TD;
+}
+
+// pool tiles per active instance (after phase B's appends)
+__device__ void build_list_D(const KArgs& a) {
+  const int nE = a.ctl->nE;
+  const int per = (nE + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(nE, lo + per);
+  long long t = 0;
+  for (int k = lo; k < hi; ++k) t += pool_tiles(a.desc[a.idsE[k]], a.st[a.idsE[k]]);
+  long long tot;
+  long long o = block_exclusive_scan(t, &tot);
+  for (int k = lo; k < hi; ++k) {
+    a.prefD[k] = o;
+    o += pool_tiles(a.desc[a.idsE[k]], a.st[a.idsE[k]]);
+  }
+  if (threadIdx.x == 0) {
+    a.prefD[nE] = tot;
+    a.ctl->totD = tot;
+  }
+}
+
+// Grid barrier; the last block to arrive runs `tail` before releasing the others.
+// Returns false when an error is pending (a wait expired somewhere).
+template <typename Tail>
+__device__ bool grid_barrier(const KArgs& a, Tail tail) {
+  __shared__ int s_last, s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int gen = *(volatile unsigned int*)&a.ctl->bar_gen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(&a.ctl->bar_count, 1u);
+    s_last = (arrived == gridDim.x - 1);
+    s_ok = 1;
+    if (!s_last) {
+      unsigned long long t0 = gtimer();
+      while (*(volatile unsigned int*)&a.ctl->bar_gen == gen) {
+        if (*(volatile int*)&a.ctl->error) { s_ok = 0; break; }
+        if (gtimer() - t0 > a.timeout_ns) {
+          atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  if (s_last) {
+    tail();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      a.ctl->bar_count = 0;
+      __threadfence();
+      atomicAdd(&a.ctl->bar_gen, 1u);
+    }
+  }
+  __syncthreads();
+  bool ok = s_ok && (*(volatile int*)&a.ctl->error == 0);
+  __syncthreads();
+  return ok;
+}
+
+struct NoTail { __device__ void operator()() const {} };
+
+// locate the list position k with pref[k] <= item < pref[k+1], starting the linear
+// walk from a hint (consecutive items mostly share an instance)
+__device__ __forceinline__ int find_seg(const long long* pref, int n, long long item, int hint) {
+  int k = hint;
+  if (k < 0 || k >= n || pref[k] > item) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (pref[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  }
+  while (k + 1 < n && pref[k + 1] <= item) k++;
+  return k;
+}
+
+// ---------------------------------------------------------------------------
+// phase A: term tables
+// ---------------------------------------------------------------------------
+__device__ void phase_tables(const KArgs& a) {
+  const long long tot = a.ctl->totA;
+  const int nA = a.ctl->nA;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int hint = -1;
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < tot; it += stride) {
+    int k = find_seg(a.prefA, nA, it, hint);
+    hint = k;
+    int s = a.idsA[k];
+    const Desc& D = a.desc[s];
+    const State& st = a.st[s];
+    build_item(D, D.parents + 2LL * D.n * st.iter, st.cyc, it - a.prefA[k]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase B: children
+// ---------------------------------------------------------------------------
+__device__ void phase_children(const KArgs& a) {
+  const long long tot = a.ctl->totB;
+  const int nA = a.ctl->nA;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  int hint = -1;
+  // the loop runs whole warps so that every lane joins the collectives below
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < tot; base += stride) {
+    long long it = base + threadIdx.x;
+    bool valid = it < tot;
+    int k = valid ? find_seg(a.prefB, nA, it, hint) : -1;
+    if (valid) hint = k;
+    int s = valid ? a.idsA[k] : -1;
+    double lb = 0.0;
+    bool keep = false;
+    bool sampled = false;
+    unsigned long long code = 0;
+    if (valid) {
+      const Desc& D = a.desc[s];
+      State& st = a.st[s];
+      code = (unsigned long long)(it - a.prefB[k]);
+      ChildCtx C;
+      C.c0 = st.cyc - 1;
+      C.gsz = group_size(D.n, D.group, st.cyc);
+      lb = child_lb(D, C, code);
+      double ub = atomic_ub_read(&st.ub);
+      if (lb <= ub) {
+        int jb;
+        double sm = child_samp(D, C, code, &jb);
+        sampled = true;
+        if (sm == 0.0) sm = 0.0;  // -0 -> +0
+        double ub0 = ord_val(st.ub_start);
+        if (sm < ub0) {
+          long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+          if (slot < D.ubc_cap) {
+            D.ubc_val[slot] = sm;
+            D.ubc_id[slot] = (code << 8) | (unsigned long long)jb;
+          }
+        }
+        if (sm < ub) {
+          atomicMin(&st.ub, ord_key(sm));
+          ub = atomic_ub_read(&st.ub);
+        }
+        if (lb <= ub) keep = !child_deriv(D, C, code);
+      }
+    }
+    // warp-aggregated statistics and appends, grouped by instance
+    unsigned int active = __ballot_sync(0xffffffffu, valid);
+    while (active) {
+      int leader = __ffs(active) - 1;
+      int ls = __shfl_sync(0xffffffffu, s, leader);
+      unsigned int same = __ballot_sync(0xffffffffu, valid && s == ls);
+      unsigned int kmask = __ballot_sync(0xffffffffu, valid && s == ls && keep);
+      unsigned int smask = __ballot_sync(0xffffffffu, valid && s == ls && sampled);
+      long long basepos = 0;
+      if (lane == leader) {
+        State& st = a.st[ls];
+        atomicAdd((unsigned long long*)&st.bounded, (unsigned long long)__popc(same));
+        if (smask) atomicAdd((unsigned long long*)&st.samples, (unsigned long long)__popc(smask));
+        if (kmask) basepos = (long long)atomicAdd((unsigned long long*)&st.count, (unsigned long long)__popc(kmask));
+      }
+      basepos = __shfl_sync(0xffffffffu, basepos, leader);
+      if (valid && s == ls && keep) {
+        const Desc& D = a.desc[s];
+        State& st = a.st[s];
+        long long pos = basepos + __popc(kmask & ((1u << lane) - 1u));
+        if (pos < D.pool_cap) {
+          D.pool_lb[st.cur][pos] = lb;
+          D.pool_key[st.cur][pos] = ((unsigned long long)st.iter << 32) | code;
+        } else {
+          atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
+        }
+      }
+      active &= ~same;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase D: pool compaction + per-tile argmin
+// ---------------------------------------------------------------------------
+struct Best {
+  unsigned long long lbk, key, idx;
+};
+
+__device__ __forceinline__ bool best_less(const Best& x, const Best& y) {
+  if (x.lbk != y.lbk) return x.lbk < y.lbk;
+  return x.key < y.key;
+}
+
+__device__ __forceinline__ Best warp_min(Best b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.lbk = __shfl_xor_sync(0xffffffffu, b.lbk, o);
+    c.key = __shfl_xor_sync(0xffffffffu, b.key, o);
+    c.idx = __shfl_xor_sync(0xffffffffu, b.idx, o);
+    if (best_less(c, b)) b = c;
+  }
+  return b;
+}
+
+__device__ void phase_pool(const KArgs& a) {
+  __shared__ Best s_b[MAX_THREADS / 32];
+  const long long tot = a.ctl->totD;
+  const int nE = a.ctl->nE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int hint = -1;
+  for (long long t = blockIdx.x; t < tot; t += gridDim.x) {
+    int k = find_seg(a.prefD, nE, t, hint);
+    hint = k;
+    int s = a.idsE[k];
+    const Desc& D = a.desc[s];
+    State& st = a.st[s];
+    const long long tile = t - a.prefD[k];
+    const long long cnt = st.count < D.pool_cap ? st.count : D.pool_cap;
+    const bool compact = st.ub != st.ub_start;
+    const double ub = ord_val(st.ub);
+    const int cur = st.cur;
+    const long long lo = tile * TD, hi = min(cnt, lo + TD);
+    Best b;
+    b.lbk = ~0ULL; b.key = ~0ULL; b.idx = ~0ULL;
+    long long removed_new = 0;
+    for (long long e0 = lo; e0 < hi; e0 += blockDim.x) {
+      long long e = e0 + threadIdx.x;
+      bool in = e < hi;
+      double lbv = in ? D.pool_lb[cur][e] : 0.0;
+      unsigned long long key = in ? D.pool_key[cur][e] : 0ULL;
+      bool keep = in && (!compact || !(lbv > ub));
+      unsigned long long pos = (unsigned long long)e;
+      if (compact) {
+        if (in && !keep && e >= st.count_before) removed_new++;
+        unsigned int km = __ballot_sync(0xffffffffu, keep);
+        unsigned long long wbase = 0;
+        if (lane == 0 && km) wbase = atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)__popc(km));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (keep) {
+          pos = wbase + __popc(km & ((1u << lane) - 1u));
+          D.pool_lb[cur ^ 1][pos] = lbv;
+          D.pool_key[cur ^ 1][pos] = key;
+        }
+      }
+      if (keep) {
+        Best c;
+        c.lbk = ord_key(lbv); c.key = key; c.idx = pos;
+        if (best_less(c, b)) b = c;
+      }
+    }
+    if (compact) {
+      for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
+      if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
+    }
+    b = warp_min(b);
+    if (lane == 0) s_b[wid] = b;
+    __syncthreads();
+    if (wid == 0) {
+      Best c = (lane < nw) ? s_b[lane] : Best{~0ULL, ~0ULL, ~0ULL};
+      c = warp_min(c);
+      if (lane == 0) {
+        unsigned long long* tb = D.tile_best + 3 * tile;
+        tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase E: selection (one warp per active instance)
+// ---------------------------------------------------------------------------
+__device__ void phase_select(const KArgs& a) {
+  const int nE = a.ctl->nE;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int k = gw; k < nE; k += nwarps) {
+    int s = a.idsE[k];
+    const Desc& D = a.desc[s];
+    State& st = a.st[s];
+    const int n = D.n;
+    const bool expanded = (st.status == ST_EXPAND);
+    const bool compact = st.ub != st.ub_start;
+    long long cnt = st.count;
+    if (cnt > D.pool_cap) cnt = D.pool_cap;  // overflow already flagged
+    // minimiser point: the recorded sample whose upper bound equals the new UB
+    if (expanded && compact) {
+      long long nc = st.ubc_count < D.ubc_cap ? st.ubc_count : D.ubc_cap;
+      const double ubv = ord_val(st.ub);
+      unsigned long long who = ~0ULL;
+      for (long long c = lane; c < nc; c += 32)
+        if (D.ubc_val[c] == ubv && D.ubc_id[c] < who) who = D.ubc_id[c];
+      for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long y = __shfl_xor_sync(0xffffffffu, who, o);
+        who = y < who ? y : who;
+      }
+      if (lane == 0) {
+        if (who != ~0ULL) { st.ub_who = ((unsigned long long)st.iter << 40) | who; st.has_who = 1; }
+        else if (st.ubc_count > D.ubc_cap) st.has_who = 0;
+      }
+    }
+    __syncwarp();
+    long long n_surv = 0;
+    if (compact) {
+      n_surv = (cnt - st.count_before) - st.removed_new;
+      cnt = st.count_new;
+    } else {
+      n_surv = cnt - st.count_before;
+    }
+    // reduce the tile minima
+    Best b;
+    b.lbk = ~0ULL; b.key = ~0ULL; b.idx = ~0ULL;
+    const long long tiles = pool_tiles(D, st);  // tiles of phase D (count before compaction)
+    for (long long t = lane; t < tiles; t += 32) {
+      const unsigned long long* tb = D.tile_best + 3 * t;
+      Best c; c.lbk = tb[0]; c.key = tb[1]; c.idx = tb[2];
+      if (best_less(c, b)) b = c;
+    }
+    b = warp_min(b);
+    __syncwarp();
+    if (lane == 0) {
+      if (compact) { st.cur ^= 1; st.count_new = 0; }
+      st.count = cnt;
+      st.removed_new = 0;
+      if (expanded) {
+        st.n_surv_last = n_surv;
+        if (st.iter < D.trace_cap) {
+          D.tr_ub[st.iter] = ord_val(st.ub);
+          D.tr_surv[st.iter] = n_surv;
+          D.tr_pool[st.iter] = cnt;
+          D.tr_sel[st.iter] = -1;
+        }
+      }
+    }
+    __syncwarp();
+    // decide (lane 0), then decode the next parent with the whole warp
+    int decision = 0;  // 0 stop, 1 emit (repop), 2 expand
+    unsigned long long key = 0;
+    double width = 0.0;
+    int ccyc = 1;
+    if (lane == 0) {
+      if (st.outcome < 0) {
+        decision = 0;
+      } else if (cnt == 0 || b.idx == ~0ULL) {
+        st.outcome = GPUGO_FINISHED;
+        decision = 0;
+      } else {
+        double lbbest = ord_val(b.lbk);
+        double lbstar = lbbest < st.out_lb_min ? lbbest : st.out_lb_min;
+        if (D.stop_mode == STOP_GAP && ord_val(st.ub) - lbstar <= D.gap_tol) {
+          st.outcome = GPUGO_CERTIFIED;
+          decision = 0;
+        } else {
+          // pop: swap-remove
+          const int c = st.cur;
+          long long last = cnt - 1;
+          D.pool_lb[c][b.idx] = D.pool_lb[c][last];
+          D.pool_key[c][b.idx] = D.pool_key[c][last];
+          st.count = last;
+          key = b.key;
+          long long prow = (long long)(key >> 32);
+          unsigned long long code = key & 0xffffffffULL;
+          ccyc = D.pcyc[prow];
+          const double* pb = D.parents + 2LL * n * prow;
+          int gsz = group_size(n, D.group, ccyc);
+          iv x0 = child_iv(D, pb, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
+          width = __dsub_rn(x0.hi, x0.lo);
+          if (width < D.width_tol && ccyc == D.max_cyc) {
+            decision = 1;
+            long long o = st.out_count;
+            if (o < D.out_cap) { D.out_key[o] = key; D.out_lb[o] = lbbest; }
+            st.out_count = o + 1;
+            if (lbbest < st.out_lb_min) st.out_lb_min = lbbest;
+          } else if (st.iter + 1 >= D.parent_cap) {
+            st.outcome = GPUGO_ERR_PARENT_OVERFLOW;
+            decision = 0;
+          } else {
+            decision = 2;
+            if (st.iter < D.trace_cap) D.tr_sel[st.iter] = (long long)key;
+          }
+        }
+      }
+    }
+    decision = __shfl_sync(0xffffffffu, decision, 0);
+    key = __shfl_sync(0xffffffffu, key, 0);
+    ccyc = __shfl_sync(0xffffffffu, ccyc, 0);
+    if (decision == 2) {
+      const long long prow = (long long)(key >> 32);
+      const unsigned long long code = key & 0xffffffffULL;
+      const double* pb = D.parents + 2LL * n * prow;
+      double* nb = D.parents + 2LL * n * (st.iter + 1);
+      const int gsz = group_size(n, D.group, ccyc);
+      for (int i = lane; i < n; i += 32) {
+        iv x = child_iv(D, pb, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
+        nb[2 * i] = x.lo;
+        nb[2 * i + 1] = x.hi;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (decision == 0) {
+        st.status = ST_DONE;
+        if (st.outcome == 0) st.outcome = GPUGO_FINISHED;
+      } else if (decision == 1) {
+        st.status = ST_REPOP;
+      } else {
+        long long row = st.iter + 1;
+        int ncyc = (ccyc == D.max_cyc) ? 1 : ccyc + D.group;
+        D.pcyc[row] = ncyc;
+        st.iter = row;
+        st.cyc = ncyc;
+        st.m_children = children_of(D, ncyc);
+        if (D.max_iter > 0 && row >= D.max_iter) {
+          st.status = ST_DONE;
+          st.outcome = GPUGO_ITER_LIMIT;
+        } else {
+          st.status = ST_EXPAND;
+        }
+      }
+      st.ub_start = st.ub;
+      st.count_before = st.count;
+      st.ubc_count = 0;
+    }
+    __syncwarp();
+  }
+}
+
+struct TailAE {
+  const KArgs* a;
+  __device__ void operator()() const { build_lists_AE(*a); }
+};
+struct TailD {
+  const KArgs* a;
+  __device__ void operator()() const { build_list_D(*a); }
+};
+
+__global__ void __launch_bounds__(256) solve_kernel(KArgs a) {
+  TailAE tae{&a};
+  TailD td{&a};
+  if (!grid_barrier(a, tae)) return;
+  long long it = 0;
+  while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
+    if (a.ctl->nA > 0) {
+      phase_tables(a);
+      if (!grid_barrier(a, NoTail{})) return;
+      phase_children(a);
+    }
+    if (!grid_barrier(a, td)) return;
+    phase_pool(a);
+    if (!grid_barrier(a, NoTail{})) return;
+    phase_select(a);
+    if (!grid_barrier(a, tae)) return;
+    ++it;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->iters = it;
+}
+
+// one thread per newly admitted slot
+__global__ void init_slots_kernel(Desc* desc, State* st, const int* slots, int m) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  int s = slots[t];
+  init_consts(desc[s]);
+}
+
+// standalone table build and per-child evaluation (gpugo_eval_children)
+__global__ void eval_init_kernel(Desc* desc) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) init_consts(desc[0]);
+}
+
+__global__ void eval_tables_kernel(Desc* desc, int cyc) {
+  const Desc& D = desc[0];
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < D.a_items; t += (long long)gridDim.x * blockDim.x)
+    build_item(D, D.parents, cyc, t);
+}
+
+__global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long long* codes, long long m, double ub,
+                                     double* lb_out, double* samp_out, int* flag_out) {
+  const Desc& D = desc[0];
+  ChildCtx C;
+  C.c0 = cyc - 1;
+  C.gsz = group_size(D.n, D.group, cyc);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long code = codes[t];
+    double lb = child_lb(D, C, code);
+    int jb;
+    double sm = child_samp(D, C, code, &jb);
+    lb_out[t] = lb;
+    samp_out[t] = sm;
+    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, C, code);
+  }
+}
+
+// FP64 peak probe: 8 independent DFMA chains per thread, 4096 steps each
+__global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, double seed, int steps) {
+  double a0 = seed + threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double m = 0.999999999, c = 1e-9;
+  for (int i = 0; i < steps; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = __fma_rn(a0, m, c); a1 = __fma_rn(a1, m, c); a2 = __fma_rn(a2, m, c); a3 = __fma_rn(a3, m, c);
+      a4 = __fma_rn(a4, m, c); a5 = __fma_rn(a5, m, c); a6 = __fma_rn(a6, m, c); a7 = __fma_rn(a7, m, c);
+    }
+  }
+  double r = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (r == 12345.0) out[blockIdx.x] = r;  // keeps the chains live
+}
+
+}  // namespace gg
+
+// ===========================================================================
+// host side
+// ===========================================================================
+using namespace gg;
+
+namespace {
+
+struct HostSlot {
+  bool used = false;
+  int64_t ticket = -1;
+  gpugo_spec spec{};
+  std::vector<double> dom, coef;
+  size_t arena_off = 0, arena_bytes = 0;
+  Desc desc{};
+  double* boxes_out = nullptr;
+  double* box_lb_out = nullptr;
+  int64_t cap = 0;
+  double* xhat_out = nullptr;
+  gpugo_trace trace{};
+  bool has_trace = false;
+};
+
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0;
+  std::map<size_t, size_t> free_;  // offset -> size
+  void init(char* b, size_t s) { base = b; size = s; free_.clear(); free_[0] = s; }
+  bool alloc(size_t bytes, size_t* off) {
+    bytes = (bytes + 255) & ~size_t(255);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        *off = it->first;
+        size_t rem = it->second - bytes, noff = it->first + bytes;
+        free_.erase(it);
+        if (rem) free_[noff] = rem;
+        return true;
+      }
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    bytes = (bytes + 255) & ~size_t(255);
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+    }
+  }
+  size_t free_bytes() const { size_t s = 0; for (auto& kv : free_) s += kv.second; return s; }
+};
+
+}  // namespace
+
+struct gpugo_engine {
+  int dev = 0, nsm = 0, threads = 256, blocks = 0;
+  int max_slots = 0;
+  double timeout_s = 60.0;
+  cudaStream_t stream = nullptr;
+  Desc* d_desc = nullptr;
+  State* d_state = nullptr;
+  Ctl* d_ctl = nullptr;
+  int* d_ids = nullptr;          // idsA | idsE | init list
+  long long* d_pref = nullptr;   // prefA | prefB | prefD
+  char* d_arena = nullptr;
+  Arena arena;
+  std::vector<HostSlot> slots;
+  std::vector<int> pending_init;
+  int64_t next_ticket = 1;
+  std::vector<State> h_state;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_run_ms = 0.0, total_run_ms = 0.0;
+  int64_t launches = 0, iterations = 0, h2d = 0, d2h = 0;
+};
+
+namespace {
+
+int cuda_err(cudaError_t e) {
+  if (e == cudaSuccess) return GPUGO_OK;
+  fprintf(stderr, "gpugo: CUDA error %s\n", cudaGetErrorString(e));
+  return GPUGO_ERR_CUDA;
+}
+#define CK(x) do { int _r = cuda_err(x); if (_r) return _r; } while (0)
+
+int ilog2_exact(int w) {
+  if (w <= 0 || (w & (w - 1))) return -1;
+  int l = 0;
+  while ((1 << l) < w) ++l;
+  return l;
+}
+
+int validate(const gpugo_spec* s) {
+  if (!s || !s->domain || !s->coef) return GPUGO_ERR_INVALID;
+  if (s->family < 1 || s->family > 4) return GPUGO_ERR_INVALID;
+  if (s->n < 1 || s->n > 4096) return GPUGO_ERR_INVALID;
+  if (s->family == GPUGO_CHAINED && s->n < 2) return GPUGO_ERR_INVALID;
+  if (s->wid < 2 || s->group < 1 || s->samples < 1 || s->samples > 255) return GPUGO_ERR_INVALID;
+  if (s->stop_mode != GPUGO_STOP_WIDTH && s->stop_mode != GPUGO_STOP_GAP) return GPUGO_ERR_INVALID;
+  int g = std::min(s->group, s->n);
+  double m = std::pow((double)s->wid, (double)g);
+  if (m > 4294967296.0) return GPUGO_ERR_INVALID;
+  for (int i = 0; i < s->n; ++i)
+    if (!(s->domain[2 * i] < s->domain[2 * i + 1])) return GPUGO_ERR_INVALID;
+  int64_t need = 0;
+  switch (s->family) {
+    case GPUGO_COSQUAD: need = 3LL * s->n; break;
+    case GPUGO_CHAINED: need = 2LL * (s->n - 1); break;
+    case GPUGO_EXPSQRT: need = 2LL + s->n; break;
+    case GPUGO_PRODCOS: need = 1; break;
+  }
+  if (s->ncoef < need) return GPUGO_ERR_INVALID;
+  if (s->family == GPUGO_EXPSQRT && !(s->coef[0] > 0 && s->coef[1] > 0)) return GPUGO_ERR_INVALID;
+  if (s->family == GPUGO_PRODCOS && !(s->coef[0] > 0)) return GPUGO_ERR_INVALID;
+  if (s->wid > 64 && s->family == GPUGO_CHAINED) return GPUGO_ERR_INVALID;  // w^3 gradient table
+  return GPUGO_OK;
+}
+
+struct Layout {
+  int64_t cst, tab, t_off[T_NOFF], a_items;
+  int64_t pool_cap, parent_cap, tiles_cap, ubc_cap, out_cap, trace_cap;
+  int64_t bytes;
+  // byte offsets
+  int64_t o_dom, o_coef, o_cst, o_tab, o_par, o_pcyc, o_plb0, o_plb1, o_pk0, o_pk1, o_tile, o_ubcv, o_ubci,
+      o_outk, o_outl, o_trub, o_trs, o_trp, o_trsel;
+};
+
+int64_t max_children(const gpugo_spec* s) {
+  int g = std::min(s->group, s->n);
+  int64_t m = 1;
+  for (int i = 0; i < g; ++i) m *= s->wid;
+  return m;
+}
+
+void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) {
+  const int64_t n = s->n, w = s->wid, S = s->samples;
+  memset(L, 0, sizeof(*L));
+  switch (s->family) {
+    case GPUGO_COSQUAD: L->cst = 6 * n + 2; break;
+    case GPUGO_CHAINED: L->cst = 8 * n; break;
+    case GPUGO_EXPSQRT: L->cst = 8 + 3 * n; break;
+    default: L->cst = 4 + 2 * n; break;
+  }
+  int64_t o = 0;
+  auto put = [&](int idx, int64_t doubles) { L->t_off[idx] = o; o += (doubles + 1) & ~int64_t(1); };
+  switch (s->family) {
+    case GPUGO_COSQUAD:
+      put(T_LO, n * w); put(T_SHI, n * w * S); put(T_PRB, (n * w + 7) / 8);
+      L->a_items = n * w * (S + 1);
+      break;
+    case GPUGO_CHAINED:
+      put(T_LO, (n - 1) * w * w); put(T_SHI, (n - 1) * w * w * S); put(T_PRB, (n * w * w * w + 7) / 8);
+      L->a_items = (n - 1) * w * w * (S + 1) + n * w * w * w;
+      break;
+    case GPUGO_EXPSQRT:
+      put(T_SQ, 2 * n * w); put(T_CS, 2 * n * w); put(T_XI, 2 * n * w); put(T_SN, 2 * n * w);
+      put(T_ZB, (n * w + 7) / 8); put(T_SQS, 2 * n * w * S); put(T_CSS, 2 * n * w * S);
+      L->a_items = n * w * (S + 1);
+      break;
+    default:
+      put(T_CR, 2 * n * w); put(T_SQ4, 2 * n * w); put(T_SNA, 2 * n * w); put(T_XD2, 2 * n * w);
+      put(T_XI4, 2 * n * w); put(T_CRS, 2 * n * w * S); put(T_SQS4, 2 * n * w * S);
+      L->a_items = n * w * (S + 1);
+      break;
+  }
+  L->tab = o;
+  const int64_t M = max_children(s);
+  L->pool_cap = s->pool_cap > 0 ? s->pool_cap : std::max<int64_t>(1 << 16, std::min<int64_t>(4 * M, 1 << 24));
+  L->parent_cap = s->parent_cap > 0 ? s->parent_cap : std::max<int64_t>(64, std::min<int64_t>(1 << 16, (1LL << 24) / (2 * n)));
+  if (s->max_iter > 0) L->parent_cap = std::min<int64_t>(L->parent_cap, s->max_iter + 1);
+  L->tiles_cap = (L->pool_cap + TD - 1) / TD;
+  L->ubc_cap = 4096;
+  L->out_cap = std::max<int64_t>(out_cap, 1);
+  L->trace_cap = trace_cap;
+  int64_t b = 0;
+  auto take = [&](int64_t bytes) { int64_t r = b; b += (bytes + 255) & ~int64_t(255); return r; };
+  L->o_dom = take(8 * 2 * n);
+  L->o_coef = take(8 * std::max<int64_t>(s->ncoef, 1));
+  L->o_cst = take(8 * L->cst);
+  L->o_tab = take(8 * L->tab);
+  L->o_par = take(8 * 2 * n * L->parent_cap);
+  L->o_pcyc = take(4 * L->parent_cap);
+  L->o_plb0 = take(8 * L->pool_cap);
+  L->o_plb1 = take(8 * L->pool_cap);
+  L->o_pk0 = take(8 * L->pool_cap);
+  L->o_pk1 = take(8 * L->pool_cap);
+  L->o_tile = take(24 * L->tiles_cap);
+  L->o_ubcv = take(8 * L->ubc_cap);
+  L->o_ubci = take(8 * L->ubc_cap);
+  L->o_outk = take(8 * L->out_cap);
+  L->o_outl = take(8 * L->out_cap);
+  L->o_trub = take(8 * std::max<int64_t>(trace_cap, 1));
+  L->o_trs = take(8 * std::max<int64_t>(trace_cap, 1));
+  L->o_trp = take(8 * std::max<int64_t>(trace_cap, 1));
+  L->o_trsel = take(8 * std::max<int64_t>(trace_cap, 1));
+  L->bytes = b;
+}
+
+void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
+  memset(D, 0, sizeof(*D));
+  D->family = s->family; D->n = s->n; D->wid = s->wid; D->group = s->group; D->S = s->samples;
+  D->stop_mode = s->stop_mode;
+  D->max_cyc = 1 + s->group * ((s->n - 1) / s->group);
+  D->wlog = ilog2_exact(s->wid);
+  D->width_tol = s->width_tol; D->gap_tol = s->gap_tol;
+  D->max_iter = s->max_iter;
+  D->pool_cap = L.pool_cap; D->parent_cap = L.parent_cap; D->out_cap = L.out_cap; D->trace_cap = L.trace_cap;
+  D->tiles_cap = L.tiles_cap; D->ubc_cap = L.ubc_cap; D->a_items = L.a_items;
+  for (int i = 0; i < T_NOFF; ++i) D->t_off[i] = L.t_off[i];
+  D->dom = (const double*)(base + L.o_dom);
+  D->coef = (const double*)(base + L.o_coef);
+  D->cst = (double*)(base + L.o_cst);
+  D->tab = (double*)(base + L.o_tab);
+  D->parents = (double*)(base + L.o_par);
+  D->pcyc = (int*)(base + L.o_pcyc);
+  D->pool_lb[0] = (double*)(base + L.o_plb0);
+  D->pool_lb[1] = (double*)(base + L.o_plb1);
+  D->pool_key[0] = (unsigned long long*)(base + L.o_pk0);
+  D->pool_key[1] = (unsigned long long*)(base + L.o_pk1);
+  D->tile_best = (unsigned long long*)(base + L.o_tile);
+  D->ubc_val = (double*)(base + L.o_ubcv);
+  D->ubc_id = (unsigned long long*)(base + L.o_ubci);
+  D->out_key = (unsigned long long*)(base + L.o_outk);
+  D->out_lb = (double*)(base + L.o_outl);
+  D->tr_ub = (double*)(base + L.o_trub);
+  D->tr_surv = (long long*)(base + L.o_trs);
+  D->tr_pool = (long long*)(base + L.o_trp);
+  D->tr_sel = (long long*)(base + L.o_trsel);
+}
+
+inline int64_t children_host(const gpugo_spec* s, int cyc) {
+  int g = std::min(s->group, s->n - cyc + 1);
+  int64_t m = 1;
+  for (int i = 0; i < g; ++i) m *= s->wid;
+  return m;
+}
+
+inline int digit_host(const gpugo_spec* s, int c0, int gsz, uint64_t code, int i) {
+  int k = i - c0;
+  if (k < 0 || k >= gsz) return 0;
+  for (int t = 0; t < k; ++t) code /= (uint64_t)s->wid;
+  return (int)(code % (uint64_t)s->wid);
+}
+
+// child box on the host; round-to-nearest arithmetic identical to child_iv
+void child_box_host(const gpugo_spec* s, const double* pb, int cyc, uint64_t code, double* out) {
+  const int n = s->n, c0 = cyc - 1, gsz = std::min(s->group, n - cyc + 1);
+  for (int i = 0; i < n; ++i) {
+    double lo = pb[2 * i], hi = pb[2 * i + 1];
+    int k = i - c0;
+    if (k >= 0 && k < gsz) {
+      int d = digit_host(s, c0, gsz, code, i);
+      volatile double w = (hi - lo) / (double)s->wid;
+      volatile double a = w * (double)d;
+      volatile double b = w * (double)(d + 1);
+      out[2 * i] = a + lo;
+      out[2 * i + 1] = b + lo;
+    } else {
+      out[2 * i] = lo;
+      out[2 * i + 1] = hi;
+    }
+  }
+}
+
+inline double ord_val_host(uint64_t k) {
+  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+}
+inline uint64_t ord_key_host(double x) {
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+int collect(gpugo_engine* E, int slot, gpugo_result* res) {
+  int64_t d2h0 = E->d2h;
+  auto D2H = [&](void* dst, const void* src, size_t bytes) {
+    E->d2h += (int64_t)bytes;
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+  };
+  HostSlot& h = E->slots[slot];
+  const State& st = E->h_state[slot];
+  const gpugo_spec* s = &h.spec;
+  const Desc& D = h.desc;
+  const int n = s->n;
+  memset(res, 0, sizeof(*res));
+  res->ub = ord_val_host(st.ub);
+  res->boxes_bounded = st.bounded;
+  res->samples_evaluated = st.samples;
+  res->status = st.outcome;
+  // rows 0..iter of the parent table were expanded, except a parent selected
+  // right before the iteration limit
+  res->iterations = (st.outcome == GPUGO_ITER_LIMIT) ? st.iter : st.iter + 1;
+  const int64_t cnt = std::min<int64_t>(st.count, D.pool_cap);
+  res->pool_size = cnt;
+  std::vector<double> plb(cnt);
+  std::vector<unsigned long long> pkey(cnt);
+  if (cnt) {
+    CK(D2H(plb.data(), D.pool_lb[st.cur], 8 * cnt));
+    CK(D2H(pkey.data(), D.pool_key[st.cur], 8 * cnt));
+  }
+  const int64_t rows = std::min<int64_t>(st.iter + 1, D.parent_cap);
+  std::vector<double> par(2 * n * rows);
+  std::vector<int> pcyc(rows);
+  CK(D2H(par.data(), D.parents, 8 * 2 * n * rows));
+  CK(D2H(pcyc.data(), D.pcyc, 4 * rows));
+  const int64_t nout = std::min<int64_t>(st.out_count, D.out_cap);
+  std::vector<unsigned long long> okey(nout);
+  std::vector<double> olb(nout);
+  if (nout) {
+    CK(D2H(okey.data(), D.out_key, 8 * nout));
+    CK(D2H(olb.data(), D.out_lb, 8 * nout));
+  }
+  double lbstar = st.out_lb_min;
+  for (int64_t i = 0; i < cnt; ++i) if (plb[i] < lbstar) lbstar = plb[i];
+  res->lb = lbstar;
+  int64_t written = 0;
+  auto emit = [&](unsigned long long key, double lb) {
+    if (written < h.cap && h.boxes_out) {
+      int64_t prow = (int64_t)(key >> 32);
+      child_box_host(s, &par[2 * n * prow], pcyc[prow], key & 0xffffffffULL, h.boxes_out + 2 * n * written);
+      if (h.box_lb_out) h.box_lb_out[written] = lb;
+      written++;
+    }
+  };
+  for (int64_t i = 0; i < nout; ++i) emit(okey[i], olb[i]);
+  int64_t total = st.out_count;
+  if (s->stop_mode == GPUGO_STOP_GAP && cnt) {
+    std::vector<int64_t> idx(cnt);
+    for (int64_t i = 0; i < cnt; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) {
+      if (plb[x] != plb[y]) return plb[x] < plb[y];
+      return pkey[x] < pkey[y];
+    });
+    for (int64_t i = 0; i < cnt && written < h.cap; ++i) emit(pkey[idx[i]], plb[idx[i]]);
+    total += cnt;
+  }
+  res->n_boxes = total;
+  res->n_out = (int32_t)written;
+  res->has_xhat = 0;
+  if (st.has_who && h.xhat_out) {
+    int64_t prow = (int64_t)(st.ub_who >> 40);
+    uint64_t code = (st.ub_who >> 8) & 0xffffffffULL;
+    int j = (int)(st.ub_who & 0xff);
+    if (prow < rows) {
+      std::vector<double> box(2 * n);
+      child_box_host(s, &par[2 * n * prow], pcyc[prow], code, box.data());
+      for (int i = 0; i < n; ++i) {
+        volatile double inc = (box[2 * i + 1] - box[2 * i]) / (double)(s->samples + 1);
+        volatile double step = inc * (double)(j + 1);
+        h.xhat_out[i] = box[2 * i] + step;
+      }
+      res->has_xhat = 1;
+    }
+  }
+  if (h.has_trace && h.trace.cap > 0) {
+    int64_t k = std::min<int64_t>(std::min<int64_t>(h.trace.cap, D.trace_cap), res->iterations);
+    if (k > 0) {
+      CK(D2H(h.trace.ub, D.tr_ub, 8 * k));
+      CK(D2H(h.trace.n_surv, D.tr_surv, 8 * k));
+      CK(D2H(h.trace.pool, D.tr_pool, 8 * k));
+      CK(D2H(h.trace.sel, D.tr_sel, 8 * k));
+    }
+  }
+  res->d2h_bytes = E->d2h - d2h0;
+  return GPUGO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gpugo_strerror(int code) {
+  switch (code) {
+    case GPUGO_OK: return "ok";
+    case GPUGO_ERR_INVALID: return "invalid problem or argument";
+    case GPUGO_ERR_CUDA: return "CUDA runtime error";
+    case GPUGO_ERR_NOMEM: return "out of device or host memory";
+    case GPUGO_ERR_POOL_OVERFLOW: return "box pool capacity exceeded";
+    case GPUGO_ERR_PARENT_OVERFLOW: return "parent table capacity exceeded";
+    case GPUGO_ERR_TIMEOUT: return "a bounded device wait expired";
+    case GPUGO_ERR_BUSY: return "no free slot or pool memory";
+    case GPUGO_ERR_NOT_FOUND: return "unknown ticket";
+    case GPUGO_ERR_NO_DEVICE: return "no CUDA device";
+    case GPUGO_CERTIFIED: return "certified";
+    case GPUGO_FINISHED: return "finished";
+    case GPUGO_ITER_LIMIT: return "iteration limit";
+  }
+  return "unknown";
+}
+
+int gpugo_device_info(int32_t* sm_out, int32_t* num_sms_out) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return GPUGO_ERR_NO_DEVICE;
+  int dev;
+  CK(cudaGetDevice(&dev));
+  cudaDeviceProp p;
+  CK(cudaGetDeviceProperties(&p, dev));
+  if (sm_out) *sm_out = p.major * 10 + p.minor;
+  if (num_sms_out) *num_sms_out = p.multiProcessorCount;
+  return GPUGO_OK;
+}
+
+int gpugo_fp64_peak(int32_t repeats, double* tflops_out, double* ms_out) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
+  int dev;
+  CK(cudaGetDevice(&dev));
+  cudaDeviceProp p;
+  CK(cudaGetDeviceProperties(&p, dev));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fp64_probe_kernel, 256, 0));
+  const int blocks = p.multiProcessorCount * std::max(occ, 1);
+  const int steps = 4096;
+  double* d_out = nullptr;
+  CK(cudaMalloc(&d_out, 8 * blocks));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int r = 0; r < std::max(repeats, 1) + 1; ++r) {
+    cudaEventRecord(e0);
+    fp64_probe_kernel<<<blocks, 256>>>(d_out, 1.0, steps);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r > 0 && ms < best) best = ms;  // first launch is warm-up
+  }
+  int rc = cuda_err(cudaGetLastError());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d_out);
+  if (rc) return rc;
+  const double flops = 2.0 * 8 * 16 * (double)steps * 256.0 * blocks;
+  if (tflops_out) *tflops_out = flops / (best * 1e-3) / 1e12;
+  if (ms_out) *ms_out = best;
+  return GPUGO_OK;
+}
+
+int gpugo_instance_bytes(const gpugo_spec* spec, int64_t* bytes_out) {
+  int rc = validate(spec);
+  if (rc) return rc;
+  Layout L;
+  layout(spec, 1, 0, &L);
+  *bytes_out = L.bytes;
+  return GPUGO_OK;
+}
+
+int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
+  if (!cfg || !out || cfg->max_slots < 1 || cfg->max_slots > 8192 || cfg->arena_bytes <= 0) return GPUGO_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
+  gpugo_engine* E = new (std::nothrow) gpugo_engine();
+  if (!E) return GPUGO_ERR_NOMEM;
+  E->max_slots = cfg->max_slots;
+  E->threads = cfg->threads > 0 ? cfg->threads : 256;
+  if (E->threads != 256) { delete E; return GPUGO_ERR_INVALID; }
+  E->timeout_s = cfg->wait_timeout_s > 0 ? cfg->wait_timeout_s : 60.0;
+  int rc = GPUGO_OK;
+  do {
+    if ((rc = cuda_err(cudaGetDevice(&E->dev)))) break;
+    cudaDeviceProp p;
+    if ((rc = cuda_err(cudaGetDeviceProperties(&p, E->dev)))) break;
+    E->nsm = p.multiProcessorCount;
+    if (!p.cooperativeLaunch) { rc = GPUGO_ERR_CUDA; break; }
+    int occ = 0;
+    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel, E->threads, 0)))) break;
+    if (occ < 1) { rc = GPUGO_ERR_CUDA; break; }
+    if (cfg->blocks_per_sm > 0) occ = std::min(occ, cfg->blocks_per_sm);
+    E->blocks = occ * E->nsm;
+    if ((rc = cuda_err(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking)))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_desc, sizeof(Desc) * E->max_slots)))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_state, sizeof(State) * E->max_slots)))) break;
+    if ((rc = cuda_err(cudaMemset(E->d_state, 0, sizeof(State) * E->max_slots)))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_ctl, sizeof(Ctl))))) break;
+    if ((rc = cuda_err(cudaMemset(E->d_ctl, 0, sizeof(Ctl))))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_ids, sizeof(int) * 3 * E->max_slots)))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
+    if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
+    E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
+    if ((rc = cuda_err(cudaEventCreate(&E->ev0)))) break;
+    if ((rc = cuda_err(cudaEventCreate(&E->ev1)))) break;
+  } while (0);
+  if (rc) { gpugo_engine_destroy(E); return rc; }
+  E->slots.resize(E->max_slots);
+  E->h_state.resize(E->max_slots);
+  *out = E;
+  return GPUGO_OK;
+}
+
+int gpugo_engine_destroy(gpugo_engine* E) {
+  if (!E) return GPUGO_OK;
+  if (E->stream) cudaStreamSynchronize(E->stream);
+  cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
+  cudaFree(E->d_ids); cudaFree(E->d_pref); cudaFree(E->d_arena);
+  if (E->ev0) cudaEventDestroy(E->ev0);
+  if (E->ev1) cudaEventDestroy(E->ev1);
+  if (E->stream) cudaStreamDestroy(E->stream);
+  delete E;
+  return GPUGO_OK;
+}
+
+int gpugo_engine_stats(gpugo_engine* E, gpugo_stats* out) {
+  if (!E || !out) return GPUGO_ERR_INVALID;
+  out->last_run_ms = E->last_run_ms;
+  out->total_run_ms = E->total_run_ms;
+  out->kernel_launches = E->launches;
+  out->iterations = E->iterations;
+  out->h2d_bytes = E->h2d;
+  out->d2h_bytes = E->d2h;
+  return GPUGO_OK;
+}
+
+int gpugo_engine_free_bytes(gpugo_engine* E, int64_t* free_out) {
+  if (!E || !free_out) return GPUGO_ERR_INVALID;
+  *free_out = (int64_t)E->arena.free_bytes();
+  return GPUGO_OK;
+}
+
+int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* box_lb_out, int64_t cap,
+                 double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+  if (!E) return GPUGO_ERR_INVALID;
+  int rc = validate(spec);
+  if (rc) return rc;
+  int slot = -1;
+  for (int s = 0; s < E->max_slots; ++s) if (!E->slots[s].used) { slot = s; break; }
+  if (slot < 0) return GPUGO_ERR_BUSY;
+  Layout L;
+  layout(spec, cap, trace ? trace->cap : 0, &L);
+  size_t off;
+  if (!E->arena.alloc((size_t)L.bytes, &off)) return GPUGO_ERR_BUSY;
+  HostSlot& h = E->slots[slot];
+  h = HostSlot();
+  h.used = true;
+  h.ticket = E->next_ticket++;
+  h.spec = *spec;
+  h.dom.assign(spec->domain, spec->domain + 2 * spec->n);
+  h.coef.assign(spec->coef, spec->coef + spec->ncoef);
+  h.spec.domain = h.dom.data();
+  h.spec.coef = h.coef.data();
+  h.arena_off = off;
+  h.arena_bytes = (size_t)L.bytes;
+  h.boxes_out = boxes_out; h.box_lb_out = box_lb_out; h.cap = cap; h.xhat_out = xhat_out;
+  if (trace) { h.trace = *trace; h.has_trace = true; }
+  char* base = E->d_arena + off;
+  fill_desc(&h.spec, L, base, &h.desc);
+  cudaStream_t st = E->stream;
+  rc = GPUGO_OK;
+  do {
+    if ((rc = cuda_err(cudaMemcpyAsync((void*)h.desc.dom, h.dom.data(), 8 * h.dom.size(), cudaMemcpyHostToDevice, st)))) break;
+    if ((rc = cuda_err(cudaMemcpyAsync((void*)h.desc.coef, h.coef.data(), 8 * h.coef.size(), cudaMemcpyHostToDevice, st)))) break;
+    if ((rc = cuda_err(cudaMemcpyAsync(h.desc.parents, h.dom.data(), 8 * h.dom.size(), cudaMemcpyHostToDevice, st)))) break;
+    int one = 1;
+    if ((rc = cuda_err(cudaMemcpyAsync(h.desc.pcyc, &one, 4, cudaMemcpyHostToDevice, st)))) break;
+    if ((rc = cuda_err(cudaMemcpyAsync(E->d_desc + slot, &h.desc, sizeof(Desc), cudaMemcpyHostToDevice, st)))) break;
+    State s0;
+    memset(&s0, 0, sizeof(s0));
+    s0.status = ST_EXPAND;
+    s0.cyc = 1;
+    double ub0 = spec->ub_init;
+    if (ub0 == 0.0) ub0 = 0.0;
+    s0.ub = ord_key_host(ub0);
+    s0.ub_start = s0.ub;
+    s0.out_lb_min = INFINITY;
+    s0.m_children = children_host(spec, 1);
+    if ((rc = cuda_err(cudaMemcpyAsync(E->d_state + slot, &s0, sizeof(State), cudaMemcpyHostToDevice, st)))) break;
+    if ((rc = cuda_err(cudaStreamSynchronize(st)))) break;
+    E->h2d += (int64_t)(8 * h.dom.size() * 2 + 8 * h.coef.size() + 4 + sizeof(Desc) + sizeof(State));
+  } while (0);
+  if (rc) { E->arena.release(off, h.arena_bytes); h = HostSlot(); return rc; }
+  E->pending_init.push_back(slot);
+  if (ticket_out) *ticket_out = h.ticket;
+  return GPUGO_OK;
+}
+
+int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
+  if (!E) return GPUGO_ERR_INVALID;
+  cudaStream_t st = E->stream;
+  if (!E->pending_init.empty()) {
+    int m = (int)E->pending_init.size();
+    int* d_list = E->d_ids + 2 * E->max_slots;
+    CK(cudaMemcpyAsync(d_list, E->pending_init.data(), 4 * m, cudaMemcpyHostToDevice, st));
+    init_slots_kernel<<<(m + 127) / 128, 128, 0, st>>>(E->d_desc, E->d_state, d_list, m);
+    CK(cudaGetLastError());
+    E->h2d += 4 * m;
+    E->launches++;
+    E->pending_init.clear();
+  }
+  CK(cudaMemsetAsync(E->d_ctl, 0, sizeof(Ctl), st));
+  KArgs a;
+  a.desc = E->d_desc;
+  a.st = E->d_state;
+  a.ctl = E->d_ctl;
+  a.idsA = E->d_ids;
+  a.idsE = E->d_ids + E->max_slots;
+  a.prefA = E->d_pref;
+  a.prefB = E->d_pref + (E->max_slots + 1);
+  a.prefD = E->d_pref + 2 * (E->max_slots + 1);
+  a.max_slots = E->max_slots;
+  a.max_iters = max_iters;
+  a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
+  void* args[] = {&a};
+  CK(cudaEventRecord(E->ev0, st));
+  CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, 0, st));
+  CK(cudaEventRecord(E->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, E->ev0, E->ev1);
+  E->last_run_ms = ms;
+  E->total_run_ms += ms;
+  E->launches++;
+  Ctl c;
+  CK(cudaMemcpy(&c, E->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(E->h_state.data(), E->d_state, sizeof(State) * E->max_slots, cudaMemcpyDeviceToHost));
+  E->iterations += c.iters;
+  E->d2h += (int64_t)(sizeof(Ctl) + sizeof(State) * E->max_slots);
+  int active = 0;
+  for (int s = 0; s < E->max_slots; ++s)
+    if (E->slots[s].used && (E->h_state[s].status == ST_EXPAND || E->h_state[s].status == ST_REPOP)) active++;
+  if (active_out) *active_out = active;
+  if (c.error) return c.error;
+  return GPUGO_OK;
+}
+
+int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_done_out) {
+  if (!E) return GPUGO_ERR_INVALID;
+  int k = 0;
+  for (int s = 0; s < E->max_slots && k < max_done; ++s) {
+    HostSlot& h = E->slots[s];
+    if (!h.used || E->h_state[s].status != ST_DONE) continue;
+    gpugo_result r;
+    int rc = collect(E, s, &r);
+    if (rc) return rc;
+    done[k].ticket = h.ticket;
+    done[k].result = r;
+    k++;
+    E->arena.release(h.arena_off, h.arena_bytes);
+    State z;
+    memset(&z, 0, sizeof(z));
+    CK(cudaMemcpy(E->d_state + s, &z, sizeof(State), cudaMemcpyHostToDevice));
+    E->h_state[s] = z;
+    h = HostSlot();
+  }
+  if (n_done_out) *n_done_out = k;
+  return GPUGO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single solve: a cached one-slot engine
+// ---------------------------------------------------------------------------
+static std::mutex g_mu;
+static gpugo_engine* g_single = nullptr;
+static int64_t g_single_bytes = 0;
+
+int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, double* box_lb_out, int64_t cap,
+                double* xhat_out, gpugo_trace* trace) {
+  if (!res) return GPUGO_ERR_INVALID;
+  int rc = validate(spec);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Layout L;
+  layout(spec, cap, trace ? trace->cap : 0, &L);
+  if (!g_single || g_single_bytes < L.bytes) {
+    if (g_single) { gpugo_engine_destroy(g_single); g_single = nullptr; }
+    gpugo_engine_cfg cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.max_slots = 1;
+    cfg.threads = 256;
+    cfg.arena_bytes = std::max<int64_t>(L.bytes, 64LL << 20);
+    cfg.wait_timeout_s = 60.0;
+    if ((rc = gpugo_engine_create(&cfg, &g_single))) return rc;
+    g_single_bytes = cfg.arena_bytes;
+  }
+  int64_t ticket;
+  const int64_t h2d0 = g_single->h2d, d2h0 = g_single->d2h;
+  if ((rc = gpugo_submit(g_single, spec, boxes_out, box_lb_out, cap, xhat_out, trace, &ticket))) return rc;
+  int32_t active = 1;
+  double total_ms = 0.0;
+  while (active > 0) {
+    rc = gpugo_run(g_single, 0, &active);
+    total_ms += g_single->last_run_ms;
+    if (rc) {
+      // drop the slot so the engine stays usable
+      gpugo_done d;
+      int32_t nd = 0;
+      g_single->h_state[0].status = ST_DONE;
+      if (g_single->h_state[0].outcome == 0) g_single->h_state[0].outcome = rc;
+      gpugo_poll(g_single, &d, 1, &nd);
+      if (nd) *res = d.result;
+      res->status = rc;
+      return rc;
+    }
+  }
+  gpugo_done d;
+  int32_t nd = 0;
+  if ((rc = gpugo_poll(g_single, &d, 1, &nd))) return rc;
+  if (nd != 1) return GPUGO_ERR_CUDA;
+  *res = d.result;
+  res->device_ms = total_ms;
+  res->h2d_bytes = g_single->h2d - h2d0;
+  res->d2h_bytes = g_single->d2h - d2h0;
+  return res->status < 0 ? res->status : GPUGO_OK;
+}
+
+int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes,
+                        int64_t m, double ub, double* lb_out, double* samp_out, int32_t* flag_out) {
+  int rc = validate(spec);
+  if (rc) return rc;
+  if (!parent_box || (!codes && m > 0) || m < 0 || cyc < 1 || cyc > spec->n) return GPUGO_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
+  int64_t M = children_host(spec, cyc);
+  for (int64_t t = 0; t < m; ++t) if ((int64_t)codes[t] >= M) return GPUGO_ERR_INVALID;
+  gpugo_spec s2 = *spec;
+  s2.pool_cap = 1;
+  s2.parent_cap = 1;
+  Layout L;
+  layout(&s2, 1, 0, &L);
+  char* base = nullptr;
+  Desc* d_desc = nullptr;
+  unsigned long long* d_codes = nullptr;
+  double *d_lb = nullptr, *d_samp = nullptr;
+  int* d_flag = nullptr;
+  rc = GPUGO_OK;
+  do {
+    if ((rc = cuda_err(cudaMalloc(&base, (size_t)L.bytes)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_desc, sizeof(Desc))))) break;
+    size_t mm = (size_t)std::max<int64_t>(m, 1);
+    if ((rc = cuda_err(cudaMalloc(&d_codes, 8 * mm)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_lb, 8 * mm)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_samp, 8 * mm)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_flag, 4 * mm)))) break;
+    Desc D;
+    fill_desc(&s2, L, base, &D);
+    if ((rc = cuda_err(cudaMemcpy((void*)D.dom, spec->domain, 8 * 2 * spec->n, cudaMemcpyHostToDevice)))) break;
+    if ((rc = cuda_err(cudaMemcpy((void*)D.coef, spec->coef, 8 * spec->ncoef, cudaMemcpyHostToDevice)))) break;
+    if ((rc = cuda_err(cudaMemcpy(D.parents, parent_box, 8 * 2 * spec->n, cudaMemcpyHostToDevice)))) break;
+    if ((rc = cuda_err(cudaMemcpy(d_desc, &D, sizeof(Desc), cudaMemcpyHostToDevice)))) break;
+    if (m > 0 && (rc = cuda_err(cudaMemcpy(d_codes, codes, 8 * m, cudaMemcpyHostToDevice)))) break;
+    eval_init_kernel<<<1, 32>>>(d_desc);
+    if ((rc = cuda_err(cudaGetLastError()))) break;
+    int blocks = (int)std::min<int64_t>((L.a_items + 255) / 256, 4096);
+    eval_tables_kernel<<<std::max(blocks, 1), 256>>>(d_desc, cyc);
+    if ((rc = cuda_err(cudaGetLastError()))) break;
+    if (m > 0) {
+      int b2 = (int)std::min<int64_t>((m + 255) / 256, 4096);
+      eval_children_kernel<<<b2, 256>>>(d_desc, cyc, d_codes, m, ub, d_lb, d_samp, d_flag);
+      if ((rc = cuda_err(cudaGetLastError()))) break;
+    }
+    if ((rc = cuda_err(cudaDeviceSynchronize()))) break;
+    if (m > 0) {
+      if ((rc = cuda_err(cudaMemcpy(lb_out, d_lb, 8 * m, cudaMemcpyDeviceToHost)))) break;
+      if ((rc = cuda_err(cudaMemcpy(samp_out, d_samp, 8 * m, cudaMemcpyDeviceToHost)))) break;
+      if ((rc = cuda_err(cudaMemcpy(flag_out, d_flag, 4 * m, cudaMemcpyDeviceToHost)))) break;
+    }
+  } while (0);
+  cudaFree(base); cudaFree(d_desc); cudaFree(d_codes); cudaFree(d_lb); cudaFree(d_samp); cudaFree(d_flag);
+  return rc;
+}
+
+}  // extern "C"

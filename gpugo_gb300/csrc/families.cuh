@@ -1,0 +1,535 @@
+// families.cuh -- objective code lists split into per-coordinate term tables
+// (built once per iteration for the selected parent) and per-child reductions.
+//
+// The reference evaluates, for every child box, its value code list (e.g.
+// GPUGO_1.1/7-Rastrigin/rastrigin50.py:161-196), its sample code list at numSamples
+// diagonal points (:245-299) and its derivative code list (:340-372), all from
+// scratch (ackley50.py:602-766).  Every per-coordinate sub-expression of these code
+// lists depends on one child digit only (two for the chained family's terms,
+// three for its gradient), so it is computed once per parent and digit value
+// and stored in a table; a child then only runs the reductions that combine the
+// terms.  Reductions run in the reference's order (left to right from [0,0]),
+// so every bound is bit-identical to evaluating the code list per child.
+// Where the lower (upper) bound of a sum depends only on the lower (upper)
+// bounds of its terms, only that side is reduced.
+#pragma once
+#include "ia.cuh"
+
+namespace gg {
+
+enum { FAM_COSQUAD = 1, FAM_CHAINED = 2, FAM_EXPSQRT = 3, FAM_PRODCOS = 4 };
+enum { STOP_WIDTH = 0, STOP_GAP = 1 };
+
+constexpr double TWO_PI = 0x1.921fb54442d18p+2;   // 2*math.pi in the reference
+constexpr double E_LO = 0x1.5bf0a8b145769p+1;     // RN(e), below e
+constexpr double E_HI = 0x1.5bf0a8b14576ap+1;     // next double, above e
+
+// Table offsets (doubles) within an instance's table region.
+enum {
+  T_LO = 0, T_SHI, T_PRB,                               // cosquad / chained
+  T_SQ = 0, T_CS, T_XI, T_SN, T_ZB, T_SQS, T_CSS,       // expsqrt
+  T_CR = 0, T_SQ4, T_SNA, T_XD2, T_XI4, T_CRS, T_SQS4,  // prodcos
+  T_NOFF = 8
+};
+
+// Derived-constant offsets (doubles) within an instance's constant region.
+struct CstLayout {
+  // cosquad: K[n] A2[n] A[n] B[n] BK[2n] BSUM[2]
+  // chained: P[n] Q[n] P4[n] P2[n] Q2[n] M2Q[n] C202[2n]
+  // expsqrt: A B INV_N[2] APE[2] ABN[2] K[n] KN[2n]
+  // prodcos: INV_D[2] INV_D2[2] RSQ[2n]
+};
+
+struct Desc {
+  int family, n, wid, group, S, stop_mode, max_cyc, wlog;
+  double width_tol, gap_tol;
+  long long max_iter;
+  long long pool_cap, parent_cap, out_cap, trace_cap, tiles_cap, ubc_cap;
+  long long a_items;                 // table-build work items per iteration
+  long long t_off[T_NOFF];           // table offsets (doubles)
+  const double* dom;                 // [2n]
+  const double* coef;
+  double* cst;                       // derived constants
+  double* tab;                       // tables
+  double* parents;                   // [parent_cap][2n]
+  int* pcyc;                         // [parent_cap]
+  double* pool_lb[2];
+  unsigned long long* pool_key[2];
+  unsigned long long* tile_best;     // [tiles_cap][3]
+  double* ubc_val;                   // [ubc_cap] sample minima below the iteration's starting UB
+  unsigned long long* ubc_id;        // [ubc_cap] code << 8 | sample index
+  unsigned long long* out_key;       // [out_cap] emitted boxes (width rule)
+  double* out_lb;
+  double* tr_ub;                     // trace rows [trace_cap]
+  long long* tr_surv;
+  long long* tr_pool;
+  long long* tr_sel;
+};
+
+// ---------------------------------------------------------------------------
+// child geometry
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int group_size(int n, int group, int cyc) {
+  int g = n - cyc + 1;
+  return g < group ? g : group;
+}
+
+// digit of coordinate i (0-based) in child code; 0 for coordinates outside the split group
+__device__ __forceinline__ int digit(const Desc& D, int c0, int gsz, unsigned long long code, int i) {
+  int k = i - c0;
+  if (k < 0 || k >= gsz) return 0;
+  if (D.wlog >= 0) return (int)((code >> (k * D.wlog)) & (unsigned long long)(D.wid - 1));
+  for (int t = 0; t < k; ++t) code /= (unsigned long long)D.wid;
+  return (int)(code % (unsigned long long)D.wid);
+}
+
+// number of digit values of coordinate i this iteration
+__device__ __forceinline__ int ndig(const Desc& D, int c0, int gsz, int i) {
+  if (i < 0 || i >= D.n) return 0;
+  int k = i - c0;
+  return (k >= 0 && k < gsz) ? D.wid : 1;
+}
+
+// child interval of coordinate i for digit d (ackley50.py:583-586, :903-906)
+__device__ __forceinline__ iv child_iv(const Desc& D, const double* pbox, int c0, int gsz, int i, int d) {
+  double lo = pbox[2 * i], hi = pbox[2 * i + 1];
+  int k = i - c0;
+  if (k >= 0 && k < gsz) {
+    double w = __ddiv_rn(__dsub_rn(hi, lo), (double)D.wid);
+    return mk(__dadd_rn(__dmul_rn(w, (double)d), lo), __dadd_rn(__dmul_rn(w, (double)(d + 1)), lo));
+  }
+  return mk(lo, hi);
+}
+
+// sample point j of an interval (ackley50.py:288-290)
+__device__ __forceinline__ double sample_pt(iv x, int S, int j) {
+  double inc = __ddiv_rn(__dsub_rn(x.hi, x.lo), (double)(S + 1));
+  return __dadd_rn(x.lo, __dmul_rn(inc, (double)(j + 1)));
+}
+
+__device__ __forceinline__ int kkt_prune(iv d, iv x, double dlo, double dhi) {
+  if (d.lo > 0 && x.lo != dlo) return 1;
+  if (d.hi < 0 && x.hi != dhi) return 1;
+  return 0;
+}
+
+__device__ __forceinline__ iv ldiv(const double* p) { return mk(p[0], p[1]); }
+__device__ __forceinline__ void stiv(double* p, iv v) { p[0] = v.lo; p[1] = v.hi; }
+
+// ---------------------------------------------------------------------------
+// derived constants (one thread per instance)
+// ---------------------------------------------------------------------------
+__device__ void init_consts(const Desc& D) {
+  const int n = D.n;
+  const double* c = D.coef;
+  double* k = D.cst;
+  switch (D.family) {
+    case FAM_COSQUAD: {
+      double bl = 0.0, bh = 0.0;
+      for (int i = 0; i < n; ++i) {
+        double a = c[i], b = c[n + i];
+        double K = __dmul_rn(TWO_PI, c[2 * n + i]);
+        k[i] = K;
+        k[n + i] = __dmul_rn(2.0, a);
+        k[2 * n + i] = a;
+        k[3 * n + i] = b;
+        k[4 * n + 2 * i] = __dmul_rd(b, K);
+        k[4 * n + 2 * i + 1] = __dmul_ru(b, K);
+        bl = __dadd_rd(bl, b);
+        bh = __dadd_ru(bh, b);
+      }
+      k[6 * n] = bl;
+      k[6 * n + 1] = bh;
+      break;
+    }
+    case FAM_CHAINED: {
+      for (int i = 0; i < n - 1; ++i) {
+        double p = c[i], q = c[n - 1 + i];
+        k[i] = p; k[n + i] = q;
+        k[2 * n + i] = __dmul_rn(4.0, p);
+        k[3 * n + i] = __dmul_rn(2.0, p);
+        k[4 * n + i] = __dmul_rn(2.0, q);
+        k[5 * n + i] = __dmul_rn(-2.0, q);
+      }
+      for (int j = 1; j < n - 1; ++j) {
+        k[6 * n + 2 * j] = __dadd_rd(k[4 * n + j], k[3 * n + j - 1]);
+        k[6 * n + 2 * j + 1] = __dadd_ru(k[4 * n + j], k[3 * n + j - 1]);
+      }
+      break;
+    }
+    case FAM_EXPSQRT: {
+      double A = c[0], B = c[1], dn = (double)n;
+      k[0] = A; k[1] = B;
+      k[2] = __ddiv_rd(1.0, dn); k[3] = __ddiv_ru(1.0, dn);
+      k[4] = __dadd_rd(A, E_LO); k[5] = __dadd_ru(A, E_HI);
+      k[6] = __ddiv_rd(__dmul_rd(A, B), dn); k[7] = __ddiv_ru(__dmul_ru(A, B), dn);
+      for (int i = 0; i < n; ++i) {
+        double K = __dmul_rn(TWO_PI, c[2 + i]);
+        k[8 + i] = K;
+        k[8 + n + 2 * i] = __ddiv_rd(K, dn);
+        k[8 + n + 2 * i + 1] = __ddiv_ru(K, dn);
+      }
+      break;
+    }
+    case FAM_PRODCOS: {
+      double d = c[0];
+      k[0] = __drcp_rd(d); k[1] = __drcp_ru(d);
+      k[2] = __dmul_rn(2.0, k[0]); k[3] = __dmul_rn(2.0, k[1]);
+      for (int i = 0; i < n; ++i) {
+        double ii = (double)(i + 1);
+        k[4 + 2 * i] = __drcp_rd(__dsqrt_ru(ii));
+        k[4 + 2 * i + 1] = __drcp_ru(__dsqrt_rd(ii));
+      }
+      break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// table build: one work item -> one table entry
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long table_items(const Desc& D) { return D.a_items; }
+
+// chained family: gradient of coordinate j given its (up to) three child intervals
+__device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv Xp) {
+  const int n = D.n;
+  const double* k = D.cst;
+  iv d;
+  if (j == 0) {
+    d = times(plus(X, -1.0), k[4 * n + 0]);
+    iv t = times(mul(minus(sqr(X), Xp), X), k[2 * n + 0]);
+    d = add(d, t);
+  } else if (j == n - 1) {
+    d = times(minus(X, sqr(Xm)), k[3 * n + n - 2]);
+  } else {
+    d = times(minus(sqr(X), Xp), k[2 * n + j]);
+    d = add(d, mk(k[6 * n + 2 * j], k[6 * n + 2 * j + 1]));
+    d = plus(mul(d, X), k[5 * n + j]);
+    iv t = times(sqr(Xm), k[3 * n + j - 1]);
+    d = minus(d, t);
+  }
+  return d;
+}
+
+__device__ void build_item(const Desc& D, const double* pbox, int cyc, long long t) {
+  const int n = D.n, w = D.wid, S = D.S;
+  const int c0 = cyc - 1, gsz = group_size(n, D.group, cyc);
+  const double* k = D.cst;
+  double* T = D.tab;
+  const long long* off = D.t_off;
+  switch (D.family) {
+    case FAM_COSQUAD: {
+      int j = (int)(t % (S + 1));
+      long long r = t / (S + 1);
+      int d = (int)(r % w), i = (int)(r / w);
+      if (d >= ndig(D, c0, gsz, i)) return;
+      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      double K = k[i], a = k[2 * n + i], b = k[3 * n + i];
+      long long e = (long long)i * w + d;
+      if (j == S) {
+        iv term = minus(times(sqr(X), a), times(cos_iv(times(X, K)), b));
+        T[off[T_LO] + e] = term.lo;
+        iv g = add(times(X, k[n + i]), mul(sin_iv(times(X, K)), mk(k[4 * n + 2 * i], k[4 * n + 2 * i + 1])));
+        ((unsigned char*)(T + off[T_PRB]))[e] = (unsigned char)kkt_prune(g, X, D.dom[2 * i], D.dom[2 * i + 1]);
+      } else {
+        double x = sample_pt(X, S, j);
+        iv P = mk(x, x);
+        iv term = minus(times(sqr(P), a), times(cos_iv(times(P, K)), b));
+        T[off[T_SHI] + e * S + j] = term.hi;
+      }
+      return;
+    }
+    case FAM_CHAINED: {
+      const long long w2 = (long long)w * w;
+      const long long part1 = (long long)(n - 1) * w2 * (S + 1);
+      if (t < part1) {
+        int j = (int)(t % (S + 1));
+        long long r = t / (S + 1);
+        int d1 = (int)(r % w); r /= w;
+        int d0 = (int)(r % w);
+        int i = (int)(r / w);
+        if (d0 >= ndig(D, c0, gsz, i) || d1 >= ndig(D, c0, gsz, i + 1)) return;
+        iv X = child_iv(D, pbox, c0, gsz, i, d0);
+        iv Y = child_iv(D, pbox, c0, gsz, i + 1, d1);
+        if (j < S) {
+          double x = sample_pt(X, S, j), y = sample_pt(Y, S, j);
+          X = mk(x, x); Y = mk(y, y);
+        }
+        iv u = times(sqr(plus(X, -1.0)), k[n + i]);
+        iv v = times(sqr(minus(sqr(X), Y)), k[i]);
+        iv term = add(v, u);
+        long long e = (long long)i * w2 + (long long)d0 * w + d1;
+        if (j == S) T[off[T_LO] + e] = term.lo;
+        else T[off[T_SHI] + e * S + j] = term.hi;
+      } else {
+        long long r = t - part1;
+        const long long w3 = w2 * w;
+        int j = (int)(r / w3);
+        long long e = r % w3;
+        int dm = (int)(e / w2), d = (int)((e / w) % w), dp = (int)(e % w);
+        int nm = (j > 0) ? ndig(D, c0, gsz, j - 1) : 1;
+        int np = (j + 1 < n) ? ndig(D, c0, gsz, j + 1) : 1;
+        if (dm >= nm || d >= ndig(D, c0, gsz, j) || dp >= np) return;
+        iv X = child_iv(D, pbox, c0, gsz, j, d);
+        iv Xm = (j > 0) ? child_iv(D, pbox, c0, gsz, j - 1, dm) : X;
+        iv Xp = (j + 1 < n) ? child_iv(D, pbox, c0, gsz, j + 1, dp) : X;
+        iv g = chained_grad(D, j, Xm, X, Xp);
+        ((unsigned char*)(T + off[T_PRB]))[(long long)j * w3 + e] =
+            (unsigned char)kkt_prune(g, X, D.dom[2 * j], D.dom[2 * j + 1]);
+      }
+      return;
+    }
+    case FAM_EXPSQRT: {
+      int j = (int)(t % (S + 1));
+      long long r = t / (S + 1);
+      int d = (int)(r % w), i = (int)(r / w);
+      if (d >= ndig(D, c0, gsz, i)) return;
+      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      double K = k[8 + i];
+      long long e = (long long)i * w + d;
+      if (j == S) {
+        stiv(T + off[T_SQ] + 2 * e, sqr(X));
+        stiv(T + off[T_CS] + 2 * e, cos_iv(times(X, K)));
+        stiv(T + off[T_XI] + 2 * e, X);
+        stiv(T + off[T_SN] + 2 * e, sin_iv(times(X, K)));
+        ((unsigned char*)(T + off[T_ZB]))[e] = (unsigned char)((X.lo > 0 || X.hi < 0) ? 0 : 1);
+      } else {
+        double x = sample_pt(X, S, j);
+        iv P = mk(x, x);
+        stiv(T + off[T_SQS] + 2 * (e * S + j), sqr(P));
+        stiv(T + off[T_CSS] + 2 * (e * S + j), cos_iv(times(P, K)));
+      }
+      return;
+    }
+    case FAM_PRODCOS: {
+      int j = (int)(t % (S + 1));
+      long long r = t / (S + 1);
+      int d = (int)(r % w), i = (int)(r / w);
+      if (d >= ndig(D, c0, gsz, i)) return;
+      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
+      long long e = (long long)i * w + d;
+      if (j == S) {
+        iv a = mul(X, RSQ);
+        stiv(T + off[T_CR] + 2 * e, cos_iv(a));
+        stiv(T + off[T_SQ4] + 2 * e, sqr(X));
+        stiv(T + off[T_SNA] + 2 * e, sin_iv(a));
+        stiv(T + off[T_XD2] + 2 * e, mul(X, mk(k[2], k[3])));
+        stiv(T + off[T_XI4] + 2 * e, X);
+      } else {
+        double x = sample_pt(X, S, j);
+        iv P = mk(x, x);
+        stiv(T + off[T_CRS] + 2 * (e * S + j), cos_iv(mul(P, RSQ)));
+        stiv(T + off[T_SQS4] + 2 * (e * S + j), sqr(P));
+      }
+      return;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-child reductions
+// ---------------------------------------------------------------------------
+struct ChildCtx {
+  int c0, gsz;
+};
+
+__device__ __noinline__ double child_lb(const Desc& D, ChildCtx C, unsigned long long code) {
+  const int n = D.n, w = D.wid;
+  const double* T = D.tab;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  switch (D.family) {
+    case FAM_COSQUAD: {
+      double s = 0.0;
+      const double* tl = T + off[T_LO];
+      for (int i = 0; i < n; ++i) s = __dadd_rd(s, tl[i * w + digit(D, C.c0, C.gsz, code, i)]);
+      return __dadd_rd(s, k[6 * n]);
+    }
+    case FAM_CHAINED: {
+      double f = 0.0;
+      const double* tl = T + off[T_LO];
+      int dcur = digit(D, C.c0, C.gsz, code, 0);
+      for (int i = 0; i < n - 1; ++i) {
+        int dn = digit(D, C.c0, C.gsz, code, i + 1);
+        f = __dadd_rd(f, tl[(long long)i * w * w + dcur * w + dn]);
+        dcur = dn;
+      }
+      return f;
+    }
+    case FAM_EXPSQRT: {
+      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        s = add(s, ldiv(T + off[T_SQ] + 2 * e));
+      }
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        c = add(c, ldiv(T + off[T_CS] + 2 * e));
+      }
+      iv inv_n = mk(k[2], k[3]);
+      iv t = sqrt_iv(mul(s, inv_n));
+      t = times(exp_iv(times(t, -k[1])), -k[0]);
+      iv u = exp_iv(mul(c, inv_n));
+      return add(minus(t, u), mk(k[4], k[5])).lo;
+    }
+    case FAM_PRODCOS: {
+      iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        pr = mul(pr, ldiv(T + off[T_CR] + 2 * e));
+      }
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        s = add(s, ldiv(T + off[T_SQ4] + 2 * e));
+      }
+      s = plus(mul(s, mk(k[0], k[1])), 1.0);
+      return add(s, pr).lo;
+    }
+  }
+  return 0.0;
+}
+
+// smallest sampled upper bound; *jbest receives its sample index
+__device__ __noinline__ double child_samp(const Desc& D, ChildCtx C, unsigned long long code, int* jbest) {
+  const int n = D.n, w = D.wid, S = D.S;
+  const double* T = D.tab;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  double best = 0.0;
+  int jb = 0;
+  for (int j = 0; j < S; ++j) {
+    double fh;
+    switch (D.family) {
+      case FAM_COSQUAD: {
+        double s = 0.0;
+        const double* th = T + off[T_SHI];
+        for (int i = 0; i < n; ++i) s = __dadd_ru(s, th[((long long)i * w + digit(D, C.c0, C.gsz, code, i)) * S + j]);
+        fh = __dadd_ru(s, k[6 * n + 1]);
+        break;
+      }
+      case FAM_CHAINED: {
+        double f = 0.0;
+        const double* th = T + off[T_SHI];
+        int dcur = digit(D, C.c0, C.gsz, code, 0);
+        for (int i = 0; i < n - 1; ++i) {
+          int dn = digit(D, C.c0, C.gsz, code, i + 1);
+          f = __dadd_ru(f, th[((long long)i * w * w + dcur * w + dn) * S + j]);
+          dcur = dn;
+        }
+        fh = f;
+        break;
+      }
+      case FAM_EXPSQRT: {
+        iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+        for (int i = 0; i < n; ++i) {
+          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+          s = add(s, ldiv(T + off[T_SQS] + 2 * (e * S + j)));
+        }
+        for (int i = 0; i < n; ++i) {
+          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+          c = add(c, ldiv(T + off[T_CSS] + 2 * (e * S + j)));
+        }
+        iv inv_n = mk(k[2], k[3]);
+        iv t = sqrt_iv(mul(s, inv_n));
+        t = times(exp_iv(times(t, -k[1])), -k[0]);
+        iv u = exp_iv(mul(c, inv_n));
+        fh = add(minus(t, u), mk(k[4], k[5])).hi;
+        break;
+      }
+      default: {  // FAM_PRODCOS
+        iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
+        for (int i = 0; i < n; ++i) {
+          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+          pr = mul(pr, ldiv(T + off[T_CRS] + 2 * (e * S + j)));
+        }
+        for (int i = 0; i < n; ++i) {
+          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+          s = add(s, ldiv(T + off[T_SQS4] + 2 * (e * S + j)));
+        }
+        s = plus(mul(s, mk(k[0], k[1])), 1.0);
+        fh = add(s, pr).hi;
+        break;
+      }
+    }
+    if (j == 0 || best > fh) { best = fh; jb = j; }
+  }
+  *jbest = jb;
+  return best;
+}
+
+// 1 when the generalized KKT test rules the child out
+__device__ __noinline__ int child_deriv(const Desc& D, ChildCtx C, unsigned long long code) {
+  const int n = D.n, w = D.wid;
+  const double* T = D.tab;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  switch (D.family) {
+    case FAM_COSQUAD: {
+      const unsigned char* pr = (const unsigned char*)(T + off[T_PRB]);
+      for (int i = 0; i < n; ++i)
+        if (pr[i * w + digit(D, C.c0, C.gsz, code, i)]) return 1;
+      return 0;
+    }
+    case FAM_CHAINED: {
+      const unsigned char* pr = (const unsigned char*)(T + off[T_PRB]);
+      const long long w2 = (long long)w * w, w3 = w2 * w;
+      int dm = 0, d = digit(D, C.c0, C.gsz, code, 0);
+      for (int j = 0; j < n; ++j) {
+        int dp = (j + 1 < n) ? digit(D, C.c0, C.gsz, code, j + 1) : 0;
+        if (pr[(long long)j * w3 + (long long)dm * w2 + (long long)d * w + dp]) return 1;
+        dm = d; d = dp;
+      }
+      return 0;
+    }
+    case FAM_EXPSQRT: {
+      const unsigned char* zb = (const unsigned char*)(T + off[T_ZB]);
+      int origin = 1;
+      for (int i = 0; i < n; ++i)
+        if (!zb[i * w + digit(D, C.c0, C.gsz, code, i)]) { origin = 0; break; }
+      if (origin) return 0;
+      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        s = add(s, ldiv(T + off[T_SQ] + 2 * e));
+      }
+      iv inv_n = mk(k[2], k[3]);
+      iv r = sqrt_iv(mul(s, inv_n));
+      iv g = exp_iv(times(r, -k[1]));
+      g = mul(div(g, r), mk(k[6], k[7]));
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        c = add(c, ldiv(T + off[T_CS] + 2 * e));
+      }
+      iv u = exp_iv(mul(c, inv_n));
+      for (int j = 0; j < n; ++j) {
+        long long e = (long long)j * w + digit(D, C.c0, C.gsz, code, j);
+        iv X = ldiv(T + off[T_XI] + 2 * e);
+        iv dd = mul(g, X);
+        iv h = mul(mul(ldiv(T + off[T_SN] + 2 * e), u), mk(k[8 + n + 2 * j], k[8 + n + 2 * j + 1]));
+        dd = add(dd, h);
+        if (kkt_prune(dd, X, D.dom[2 * j], D.dom[2 * j + 1])) return 1;
+      }
+      return 0;
+    }
+    case FAM_PRODCOS: {
+      iv P = mk(1.0, 1.0);
+      for (int i = 0; i < n; ++i) {
+        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
+        P = mul(P, ldiv(T + off[T_CR] + 2 * e));
+      }
+      for (int j = 0; j < n; ++j) {
+        long long e = (long long)j * w + digit(D, C.c0, C.gsz, code, j);
+        iv q = div(P, ldiv(T + off[T_CR] + 2 * e));
+        q = mul(mul(q, ldiv(T + off[T_SNA] + 2 * e)), mk(k[4 + 2 * j], k[4 + 2 * j + 1]));
+        q = add(q, ldiv(T + off[T_XD2] + 2 * e));
+        iv X = ldiv(T + off[T_XI4] + 2 * e);
+        if (kkt_prune(q, X, D.dom[2 * j], D.dom[2 * j + 1])) return 1;
+      }
+      return 0;
+    }
+  }
+  return 0;
+}
+
+}  // namespace gg

@@ -1,0 +1,190 @@
+/*
+ * gpugo.h -- C ABI of the GB300 interval branch-and-bound solver (libgpugo.so).
+ *
+ * The reference (CMU GPUGO, Python + Numba CUDA) has no function-call API: each
+ * script is the per-problem call.  Its constants go in (objective code lists,
+ * domain, split rule, sample count, width tolerance, initial UB) and the
+ * enclosure plus the surviving boxes are printed.  Citations below name the
+ * reference lines each entry point replaces (paths within the GPUGO project).
+ *
+ * Conventions
+ *   - Every function returns GPUGO_OK (0) or a negative GPUGO_ERR_* code.
+ *   - All pointers in these signatures are HOST pointers.  Device memory is
+ *     owned by the library (one arena per engine, allocated at creation).
+ *   - An engine is single-producer: one host thread submits, runs and polls.
+ *   - Device-side waits are bounded; an expired wait returns GPUGO_ERR_TIMEOUT
+ *     and leaves the CUDA context usable.
+ */
+#ifndef GPUGO_H
+#define GPUGO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status / error codes */
+#define GPUGO_OK                   0
+#define GPUGO_ERR_INVALID         -1   /* bad spec or argument */
+#define GPUGO_ERR_CUDA            -2   /* CUDA runtime error */
+#define GPUGO_ERR_NOMEM           -3   /* arena or host allocation failed */
+#define GPUGO_ERR_POOL_OVERFLOW   -4   /* box pool capacity exceeded */
+#define GPUGO_ERR_PARENT_OVERFLOW -5   /* parent table capacity exceeded */
+#define GPUGO_ERR_TIMEOUT         -6   /* a bounded device wait expired */
+#define GPUGO_ERR_BUSY            -7   /* no free slot or pool memory: retry after a run */
+#define GPUGO_ERR_NOT_FOUND       -8   /* unknown ticket */
+#define GPUGO_ERR_NO_DEVICE       -9   /* no CUDA device */
+
+/* per-instance outcome (gpugo_result.status) */
+#define GPUGO_CERTIFIED   1   /* UB - LB <= gap_tol (gap mode) */
+#define GPUGO_FINISHED    2   /* list exhausted (width mode: every remaining box met the width rule) */
+#define GPUGO_ITER_LIMIT  3   /* max_iter expansions reached */
+
+/* objective families (coefficient layout in gpugo_spec.coef) */
+#define GPUGO_COSQUAD 1   /* sum a_i x_i^2 - b_i cos(K_i x_i) + sum b_i,  K_i = fl(fl(2pi) c_i); coef a[n] b[n] c[n]  (rastrigin50.py:161-188) */
+#define GPUGO_CHAINED 2   /* sum_{i<n} p_i (x_{i+1} - x_i^2)^2 + q_i (1 - x_i)^2; coef p[n-1] q[n-1]       (rosenbrock50.py:168-198) */
+#define GPUGO_EXPSQRT 3   /* -A exp(-B sqrt(mean x^2)) - exp(mean cos(K_i x_i)) + A + e; coef A B w[n]     (ackley50.py:166-212) */
+#define GPUGO_PRODCOS 4   /* 1 + sum x_i^2 / d - prod cos(x_i / sqrt(i)); coef d                          (griewank50.py:161-198) */
+
+#define GPUGO_STOP_WIDTH 0   /* reference rule: emit a box when width(x_1) < width_tol at the last cycle (ackley50.py:1306-1343) */
+#define GPUGO_STOP_GAP   1   /* certify when UB - LB <= gap_tol */
+
+/* One problem: the constants of a reference script made explicit. */
+typedef struct gpugo_spec {
+    int32_t family;        /* GPUGO_COSQUAD .. GPUGO_PRODCOS */
+    int32_t n;             /* variables (reference: 50..10000, hard-coded per script) */
+    int32_t wid;           /* parts per split coordinate (reference wid = 4, ackley50.py:527) */
+    int32_t group;         /* coordinates split per iteration (reference cycleSize = 10, :530) */
+    int32_t samples;       /* sample points per child (reference numSamples = 10, :1015) */
+    int32_t stop_mode;     /* GPUGO_STOP_WIDTH or GPUGO_STOP_GAP */
+    double  width_tol;     /* reference widthTolerance = 1e-4 (:1010) */
+    double  gap_tol;       /* UB - LB tolerance in gap mode */
+    double  ub_init;       /* initial UB (reference lowestUpperVal, :994); +inf allowed */
+    const double* domain;  /* [2n] lo_1, hi_1, ..., lo_n, hi_n (reference initialRegion, :958) */
+    const double* coef;    /* family coefficients, see above */
+    int64_t ncoef;
+    int64_t max_iter;      /* 0: unlimited expansions */
+    int64_t pool_cap;      /* 0: default list capacity (entries) */
+    int64_t parent_cap;    /* 0: default parent-table rows */
+} gpugo_spec;
+
+typedef struct gpugo_result {
+    double  lb;                 /* guaranteed lower bound of the global minimum */
+    double  ub;                 /* guaranteed upper bound (smallest sampled upper bound) */
+    int64_t n_boxes;            /* minimiser boxes available (may exceed the caller's cap) */
+    int64_t iterations;         /* expansions (the reference's `iter`) */
+    int64_t boxes_bounded;      /* child boxes bounded */
+    int64_t pool_size;          /* live list entries at exit */
+    int32_t status;             /* GPUGO_CERTIFIED / FINISHED / ITER_LIMIT, or a GPUGO_ERR_* code */
+    int32_t n_out;              /* boxes written to the caller's buffers */
+    int64_t samples_evaluated;  /* children whose sample points were evaluated */
+    int32_t has_xhat;           /* 1 when xhat_out holds the point that achieved ub */
+    int32_t reserved;
+    double  device_ms;          /* device time of the solve (persistent-kernel launches) */
+    int64_t h2d_bytes;          /* host -> device bytes copied for this solve */
+    int64_t d2h_bytes;          /* device -> host bytes copied for this solve */
+} gpugo_result;
+
+/* Trace of one solve, one row per expansion (optional). */
+typedef struct gpugo_trace {
+    int64_t  cap;        /* rows available */
+    double*  ub;         /* UB after the sampling step */
+    int64_t* n_surv;     /* survivors appended (the reference's atomic_index) */
+    int64_t* pool;       /* live list length after the update */
+    int64_t* sel;        /* (parent << 32 | child code) selected as next parent, -1 at exit */
+} gpugo_trace;
+
+/*
+ * Solve one problem to completion on the current CUDA device.
+ * Replaces one run of a reference script: the host loop ackley50.py:950-1396 with
+ * its kernels sampling (:602-684), ruleOutGPU (:686-766), constructFlagArr (:768-810)
+ * and the selection step (:1269-1370); the printed enclosure (:1384-1387) is
+ * res->lb / res->ub and the printed output regions are boxes_out.
+ *   boxes_out  [cap][2n] minimiser boxes (width mode: emitted boxes in emission
+ *              order; gap mode: emitted boxes, then the remaining list by LB)
+ *   box_lb_out [cap] their lower bounds (may be NULL)
+ *   xhat_out   [n] the sample point that achieved res->ub (may be NULL)
+ *   trace      per-expansion record (may be NULL)
+ */
+int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, double* box_lb_out,
+                int64_t cap, double* xhat_out, gpugo_trace* trace);
+
+/*
+ * One bound/prune pass over given children of one parent box: for each child
+ * code, the lower bound (value code list, e.g. rastrigin50.py:111-196), the
+ * smallest sampled upper bound (sample code list, :199-299) and the ruleOutGPU
+ * flag (value test against `ub`, then the derivative code list, :302-372).
+ * Replaces one launch of sampling + ruleOutGPU (ackley50.py:602-766) restricted
+ * to the listed threads.  cyc is the 1-based first split coordinate.
+ */
+int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_t cyc,
+                        const uint64_t* codes, int64_t m, double ub,
+                        double* lb_out, double* samp_out, int32_t* flag_out);
+
+/* ---------------------------------------------------------------------------
+ * Engines: many solves share one persistent kernel (batching and serving).
+ * ------------------------------------------------------------------------- */
+typedef struct gpugo_engine gpugo_engine;
+
+typedef struct gpugo_engine_cfg {
+    int32_t max_slots;          /* instances resident at once (<= 8192) */
+    int32_t threads;            /* threads per block (0: 256) */
+    int64_t arena_bytes;        /* device memory for pools, tables and parent tables */
+    double  wait_timeout_s;     /* bound of every device-side wait (0: 60 s) */
+    int32_t blocks_per_sm;      /* 0: occupancy maximum */
+    int32_t reserved;
+} gpugo_engine_cfg;
+
+typedef struct gpugo_done {
+    int64_t ticket;
+    gpugo_result result;
+} gpugo_done;
+
+int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out);
+int gpugo_engine_destroy(gpugo_engine* eng);
+
+/* Admit one problem if a slot and pool memory are free (GPUGO_ERR_BUSY otherwise).
+ * Output buffers are host memory owned by the caller and filled by gpugo_poll. */
+int gpugo_submit(gpugo_engine* eng, const gpugo_spec* spec, double* boxes_out, double* box_lb_out,
+                 int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out);
+
+/* Run the persistent kernel for at most max_iters iterations (0: until every
+ * admitted instance has finished).  Returns the number of instances still active
+ * through *active_out. */
+int gpugo_run(gpugo_engine* eng, int64_t max_iters, int32_t* active_out);
+
+/* Collect finished instances (results and boxes), freeing their slots. */
+int gpugo_poll(gpugo_engine* eng, gpugo_done* done, int32_t max_done, int32_t* n_done_out);
+
+/* Counters of an engine since its creation. */
+typedef struct gpugo_stats {
+    double  last_run_ms;        /* device time of the last gpugo_run (CUDA events on the engine stream) */
+    double  total_run_ms;
+    int64_t kernel_launches;    /* kernels this engine launched */
+    int64_t iterations;         /* persistent-kernel iterations run */
+    int64_t h2d_bytes, d2h_bytes;
+} gpugo_stats;
+
+int gpugo_engine_stats(gpugo_engine* eng, gpugo_stats* out);
+
+/* Free bytes of the engine's arena (admission control). */
+int gpugo_engine_free_bytes(gpugo_engine* eng, int64_t* free_out);
+
+/* Arena bytes one problem needs when admitted. */
+int gpugo_instance_bytes(const gpugo_spec* spec, int64_t* bytes_out);
+
+const char* gpugo_strerror(int code);
+
+/* Library version and the device it runs on (sm number, e.g. 103). */
+int gpugo_device_info(int32_t* sm_out, int32_t* num_sms_out);
+
+/* FP64 throughput probe: independent DFMA chains on every SM, timed with CUDA
+ * events (best of `repeats`); FMA counts 2 flops.  No reference counterpart: the
+ * roofline denominator for the FP64-bound bound kernels. */
+int gpugo_fp64_peak(int32_t repeats, double* tflops_out, double* ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUGO_H */

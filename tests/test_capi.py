@@ -1,0 +1,57 @@
+"""The C-ABI library loads and exports every entry point include/gpugo.h declares.
+
+No compute call is made here: this runs without a GPU.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "gpugo.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gpugo_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from gpugo_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def test_exports_match_header(lib):
+    from gpugo_gb300 import _lib
+    declared = _declared()
+    assert declared, "no declarations found"
+    assert sorted(_lib.EXPORTS) == declared
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_strerror(lib):
+    assert lib.gpugo_strerror(0) == b"ok"
+    assert lib.gpugo_strerror(-4) == b"box pool capacity exceeded"
+
+
+def test_instance_bytes_validates(lib):
+    import numpy as np
+    import gpugo_gb300 as G
+    p = G.config2()
+    assert G.instance_bytes(p) > 0
+    bad = G.config2()
+    bad.domain[0], bad.domain[1] = 1.0, -1.0
+    with pytest.raises(G.GpugoError):
+        G.instance_bytes(bad)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from gpugo_gb300 import _lib, build
+    monkeypatch.setattr(build, "LIB", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError):
+        _lib.load()

@@ -1,0 +1,173 @@
+"""GPU path (libgpugo.so through its C ABI) against the CPU oracle.
+
+Integer work must match bit for bit: the survivor count per iteration, the
+list length, the selected parent per iteration and the UB sequence.  Every
+bound is produced by the same operation sequence on both sides, so lower
+bounds, sampled upper bounds and final enclosures are compared exactly too.
+"""
+import os
+from types import SimpleNamespace as NS
+
+import numpy as np
+import pytest
+
+import gpugo_gb300 as G
+from gpugo_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.npz")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from gpugo_gb300 import build
+    build.build()
+    sm, nsm = G.device_info()
+    assert sm >= 100, f"unexpected device sm_{sm}"
+
+
+def _same(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return a.shape == b.shape and np.all((a == b) | (np.isnan(a) & np.isnan(b)))
+
+
+def _ref_problem(g, name):
+    return P.Problem(int(g[name + "_family"][0]), 50, g[name + "_domain"], g[name + "_coef"], wid=4, group=10,
+                     samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6)
+
+
+@pytest.mark.parametrize("name", ["rastrigin", "rosenbrock", "ackley", "griewank"])
+def test_children_reference_setups(oracle_lib, name):
+    """50-variable reference scripts (wid 4, cycles of 10): per-child bounds and flags."""
+    g = np.load(GOLD)
+    p = _ref_problem(g, name)
+    rng = np.random.default_rng(3)
+    for k, cyc in enumerate([1, 11, 41]):
+        pbox = g[name + "_parents"][k]
+        codes = np.concatenate([rng.integers(0, 4 ** 10, 3000), [0, 4 ** 10 - 1]]).astype(np.uint64)
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, codes, 1e300)
+        ub = float(np.quantile(lb_o, 0.5))
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, codes, ub)
+        lb_g, s_g, f_g = G.eval_children(p, pbox, cyc, codes, ub)
+        assert _same(lb_g, lb_o), name
+        assert _same(s_g, s_o), name
+        assert _same(f_g, f_o), name
+
+
+CFGS = [
+    ("cfg1", lambda: P.config1()),
+    ("cfg2", lambda: P.config2()),
+    ("expsqrt5", lambda: P.instance(P.EXPSQRT, 5, 11, 1e-6)),
+    ("prodcos4", lambda: P.instance(P.PRODCOS, 4, 12, 1e-6)),
+    ("cosquad7", lambda: P.instance(P.COSQUAD, 7, 13, 1e-6)),
+    ("chained3", lambda: P.instance(P.CHAINED, 3, 14, 1e-6)),
+    ("expsqrt12", lambda: P.instance(P.EXPSQRT, 12, 15, 1e-4)),
+    ("prodcos10", lambda: P.instance(P.PRODCOS, 10, 16, 1e-6)),
+]
+
+
+@pytest.mark.parametrize("name,make", CFGS, ids=[c[0] for c in CFGS])
+def test_children_baseline_families(oracle_lib, name, make):
+    p = make()
+    rng = np.random.default_rng(4)
+    pbox = p.domain.copy()
+    M = p.children_per_iter
+    codes = np.unique(np.concatenate([rng.integers(0, M, 4000), [0, M - 1]])).astype(np.uint64)
+    for cyc in sorted({1, 1 + p.group * ((p.n - 1) // p.group)}):
+        Mc = p.wid ** min(p.group, p.n - cyc + 1)
+        cc = codes[codes < Mc]
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, cc, 1e300)
+        ub = float(np.quantile(lb_o, 0.3))
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, cc, ub)
+        lb_g, s_g, f_g = G.eval_children(p, pbox, cyc, cc, ub)
+        assert _same(lb_g, lb_o) and _same(s_g, s_o) and _same(f_g, f_o)
+
+
+def _compare_solves(p, oracle_lib, box_cap=4096):
+    ro = oracle_lib.solve(p, box_cap=box_cap, trace_cap=100000)
+    rg = G.solve(p, box_cap=box_cap, trace_cap=100000)
+    assert rg.iterations == ro.iterations
+    for k in ("ub", "n_surv", "pool", "sel"):
+        assert _same(rg.trace[k], ro.trace[k]), k
+    assert rg.lb == ro.lb and rg.ub == ro.ub
+    assert rg.pool_size == ro.pool_size and rg.n_boxes == ro.n_boxes
+    assert _same(rg.boxes.reshape(len(rg.boxes), -1), ro.boxes)
+    assert _same(rg.box_lbs, ro.box_lbs)
+    return rg, ro
+
+
+@pytest.mark.parametrize("name,make", CFGS[:6], ids=[c[0] for c in CFGS[:6]])
+def test_solve_trace_parity(oracle_lib, name, make):
+    p = make()
+    p.max_iter = 3000
+    rg, ro = _compare_solves(p, oracle_lib)
+    assert rg.status == G.CERTIFIED and ro.status == 0
+    assert rg.lb <= 0.0 <= rg.ub and rg.ub - rg.lb <= p.gap_tol
+    # the minimiser point achieves the UB: a plain FP64 evaluation lies in the enclosure
+    assert rg.xhat is not None
+    fx = p.evaluate(rg.xhat)
+    assert rg.lb - 1e-12 <= fx <= rg.ub + 1e-12
+
+
+def test_solve_width_mode_parity(oracle_lib):
+    p = P.instance(P.COSQUAD, 4, 99, tol=0.0, split=(4, 2))
+    p.stop_mode = P.STOP_WIDTH
+    p.width_tol = 1e-3
+    p.ub_init = 1e6
+    rg, ro = _compare_solves(p, oracle_lib)
+    assert rg.status == G.FINISHED and rg.n_boxes >= 1
+
+
+def test_solve_reference_rastrigin_iterations(oracle_lib):
+    """The 50-variable Rastrigin script's loop (4^10 children per iteration), 4 iterations."""
+    g = np.load(GOLD)
+    p = _ref_problem(g, "rastrigin")
+    p.max_iter = 4
+    rg, ro = _compare_solves(p, oracle_lib, box_cap=16)
+    assert rg.status == G.ITER_LIMIT and rg.boxes_bounded == 4 * 4 ** 10
+
+
+def test_engine_batch_matches_single(oracle_lib):
+    """Each result is the same alone and in a mixed batch."""
+    probs = [make() for _, make in CFGS] + P.config4(count=24, seed=77, nmax=12)
+    for p in probs:
+        p.max_iter = 2000
+    singles = [G.solve(p, box_cap=8, trace_cap=4096) for p in probs]
+    with G.Engine(max_slots=16, arena_bytes=2 << 30) as eng:
+        batch = eng.solve_all(probs, box_cap=8)
+    for p, a, b in zip(probs, singles, batch):
+        assert (a.lb, a.ub, a.iterations, a.status, a.pool_size) == (b.lb, b.ub, b.iterations, b.status, b.pool_size), p.tag
+        assert _same(a.boxes, b.boxes)
+
+
+def test_pool_overflow_reports_error():
+    """Host-side fault injection: a pool too small for the survivors."""
+    p = P.config2()
+    p.pool_cap = 4
+    with pytest.raises(G.GpugoError) as e:
+        G.solve(p)
+    assert e.value.code == -4
+    # the library stays usable afterwards
+    r = G.solve(P.config1())
+    assert r.certified
+
+
+def test_parent_overflow_reports_error():
+    p = P.config2()
+    p.parent_cap = 3
+    with pytest.raises(G.GpugoError) as e:
+        G.solve(p)
+    assert e.value.code == -5
+
+
+def test_bounded_wait_expires_cleanly():
+    """A device wait budget of ~zero makes every grid barrier give up: the run
+    returns GPUGO_ERR_TIMEOUT and the context stays usable."""
+    with G.Engine(max_slots=2, arena_bytes=256 << 20, wait_timeout_s=1e-9) as eng:
+        eng.submit(P.config2())
+        with pytest.raises(G.GpugoError) as e:
+            eng.run()
+        assert e.value.code == -6
+    r = G.solve(P.config1())
+    assert r.certified

@@ -1,0 +1,71 @@
+"""The CPU oracle against golden vectors produced by the reference's own code.
+
+tests/golden/make_golden.py executed the reference's device functions
+(rastrigin50.py, rosenbrock50.py, ackley50.py, griewank50.py with the updated
+interval library) on fixed parent boxes and child codes.
+"""
+import os
+from types import SimpleNamespace as NS
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def _problem(g, name):
+    return NS(family=int(g[name + "_family"][0]), n=50, wid=4, group=10, samples=10, stop_mode=0,
+              width_tol=1e-4, gap_tol=0.0, ub_init=1e6, domain=g[name + "_domain"], coef=g[name + "_coef"])
+
+
+def _eval(oracle_lib, g, name):
+    p = _problem(g, name)
+    par, pidx, cyc, code = g[name + "_parents"], g[name + "_parent_idx"], g[name + "_cyc"], g[name + "_code"]
+    out = {"lb": [], "samp": [], "dflag": [], "flag_below": []}
+    for k in range(code.size):
+        lb, samp, flag, dflag = oracle_lib.eval_children(p, par[pidx[k]], int(cyc[k]), np.array([code[k]]), 1e300)
+        out["lb"].append(lb[0]); out["samp"].append(samp[0]); out["dflag"].append(dflag[0])
+        ref_lb = g[name + "_lb"][k]
+        _, _, fb, _ = oracle_lib.eval_children(p, par[pidx[k]], int(cyc[k]), np.array([code[k]]),
+                                               ref_lb - abs(ref_lb) * 1e-9 - 1e-300)
+        out["flag_below"].append(fb[0])
+    return {k: np.array(v) for k, v in out.items()}
+
+
+@pytest.mark.parametrize("name", ["rastrigin", "rosenbrock"])
+def test_bit_exact_families(oracle_lib, gold, name):
+    """Same interval semantics as the reference: every bound identical bit for bit."""
+    r = _eval(oracle_lib, gold, name)
+    np.testing.assert_array_equal(r["lb"], gold[name + "_lb"])
+    np.testing.assert_array_equal(r["samp"], gold[name + "_samp"])
+    np.testing.assert_array_equal(r["dflag"], gold[name + "_dflag"])
+    np.testing.assert_array_equal(r["flag_below"], gold[name + "_flag_below"])
+
+
+@pytest.mark.parametrize("name", ["ackley", "griewank"])
+def test_enclosure_families(oracle_lib, gold, name):
+    """Constants the reference rounds to nearest (1/n, e, 1/sqrt(i), 1/d) are carried
+    as enclosures here, so bounds may only be wider, by a few ulps."""
+    r = _eval(oracle_lib, gold, name)
+    ref_lb, ref_s = gold[name + "_lb"], gold[name + "_samp"]
+    assert np.all(r["lb"] <= ref_lb)
+    assert np.all(r["samp"] >= ref_s)
+    np.testing.assert_allclose(r["lb"], ref_lb, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(r["samp"], ref_s, rtol=1e-13, atol=1e-13)
+    m = gold[name + "_dflag"] >= 0
+    np.testing.assert_array_equal(r["dflag"][m], gold[name + "_dflag"][m])
+
+
+def test_box_decoder(oracle_lib, gold):
+    """completeRegion / selectVarInSubRegion (ackley50.py:482-594, :820-948)."""
+    p = _problem(gold, "rastrigin")
+    for t in range(gold["decoder_code"].size):
+        pb = gold["rastrigin_parents"][gold["decoder_parent_idx"][t]]
+        box = oracle_lib.child_box(p, pb, int(gold["decoder_cyc"][t]), int(gold["decoder_code"][t]))
+        np.testing.assert_array_equal(box, gold["decoder_complete"][t])
+        np.testing.assert_array_equal(box, gold["decoder_select"][t])
