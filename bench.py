@@ -137,7 +137,6 @@ def run_gpugo(args, dist):
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
-    G.build.build() if False else None
     L = _lib.load()
     p = P.config2()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # 256 MiB > 129 MB L2

@@ -89,11 +89,15 @@ class Problem:
 
 
 def default_split(n: int) -> tuple[int, int]:
-    """Split rule (wid, group) giving 1K-64K children per iteration."""
-    table = {1: (64, 1), 2: (64, 2), 3: (16, 3), 4: (8, 4), 5: (4, 5), 6: (4, 6), 7: (4, 7), 8: (4, 8)}
+    """Split rule (wid, group) for generated instances: an odd number of parts,
+    so that a minimiser at the centre of a symmetric domain lies inside one child
+    instead of on the shared corner of all of them (where every child has the same
+    LB and the reference's first-in-list tie-break expands them breadth first),
+    with 700-16K children per iteration and cycles of 8 coordinates above n = 8."""
+    table = {1: (63, 1), 2: (31, 2), 3: (9, 3), 4: (7, 4), 5: (5, 5), 6: (5, 6), 7: (3, 7)}
     if n in table:
         return table[n]
-    return (4, 8) if n % 8 == 0 else (2, min(n, 14))
+    return (3, 8)
 
 
 def _rng(seed: int) -> np.random.Generator:
