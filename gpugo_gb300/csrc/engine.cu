@@ -40,7 +40,7 @@
 namespace gg {
 
 constexpr int TD = 2048;           // pool entries per phase-D tile
-constexpr int MAX_THREADS = 512;
+constexpr int MAX_THREADS = 512;  // block size is 256 or 512
 
 // instance life cycle
 enum { ST_FREE = 0, ST_EXPAND = 1, ST_REPOP = 2, ST_DONE = 3 };
@@ -92,6 +92,8 @@ struct KArgs {
   int max_slots;
   long long max_iters;        // iterations in this launch (<= 0: until idle)
   unsigned long long timeout_ns;
+  unsigned long long* stamps; // optional: %globaltimer at each barrier release, 5 per iteration
+  long long stamp_cap;
 };
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -624,22 +626,31 @@ struct TailD {
   __device__ void operator()() const { build_list_D(*a); }
 };
 
-__global__ void __launch_bounds__(256) solve_kernel(KArgs a) {
+__device__ __forceinline__ void stamp(const KArgs& a, long long it, int k) {
+  if (a.stamps && blockIdx.x == 0 && threadIdx.x == 0 && (it * 5 + k) < a.stamp_cap) a.stamps[it * 5 + k] = gtimer();
+}
+
+__global__ void __launch_bounds__(MAX_THREADS) solve_kernel(KArgs a) {
   TailAE tae{&a};
   TailD td{&a};
   if (!grid_barrier(a, tae)) return;
   long long it = 0;
   while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
+    stamp(a, it, 0);
     if (a.ctl->nA > 0) {
       phase_tables(a);
       if (!grid_barrier(a, NoTail{})) return;
+      stamp(a, it, 1);
       phase_children(a);
     }
     if (!grid_barrier(a, td)) return;
+    stamp(a, it, 2);
     phase_pool(a);
     if (!grid_barrier(a, NoTail{})) return;
+    stamp(a, it, 3);
     phase_select(a);
     if (!grid_barrier(a, tae)) return;
+    stamp(a, it, 4);
     ++it;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->iters = it;
@@ -773,6 +784,10 @@ struct gpugo_engine {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_run_ms = 0.0, total_run_ms = 0.0;
   int64_t launches = 0, iterations = 0, h2d = 0, d2h = 0;
+  // phase timestamps (debug aid, enabled by GPUGO_PHASE_STAMPS=<file>)
+  unsigned long long* d_stamps = nullptr;
+  long long stamp_cap = 0;
+  const char* stamp_path = nullptr;
 };
 
 namespace {
@@ -1158,7 +1173,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
   if (!E) return GPUGO_ERR_NOMEM;
   E->max_slots = cfg->max_slots;
   E->threads = cfg->threads > 0 ? cfg->threads : 256;
-  if (E->threads != 256) { delete E; return GPUGO_ERR_INVALID; }
+  if (E->threads != 256 && E->threads != 512) { delete E; return GPUGO_ERR_INVALID; }
   E->timeout_s = cfg->wait_timeout_s > 0 ? cfg->wait_timeout_s : 60.0;
   int rc = GPUGO_OK;
   do {
@@ -1182,6 +1197,11 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
+    if (const char* sp = getenv("GPUGO_PHASE_STAMPS")) {
+      E->stamp_path = sp;
+      E->stamp_cap = 5 * 65536;
+      if ((rc = cuda_err(cudaMalloc(&E->d_stamps, 8 * E->stamp_cap)))) break;
+    }
     if ((rc = cuda_err(cudaEventCreate(&E->ev0)))) break;
     if ((rc = cuda_err(cudaEventCreate(&E->ev1)))) break;
   } while (0);
@@ -1196,7 +1216,7 @@ int gpugo_engine_destroy(gpugo_engine* E) {
   if (!E) return GPUGO_OK;
   if (E->stream) cudaStreamSynchronize(E->stream);
   cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
-  cudaFree(E->d_ids); cudaFree(E->d_pref); cudaFree(E->d_arena);
+  cudaFree(E->d_ids); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->stream) cudaStreamDestroy(E->stream);
@@ -1303,6 +1323,8 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
+  a.stamps = E->d_stamps;
+  a.stamp_cap = E->stamp_cap;
   void* args[] = {&a};
   CK(cudaEventRecord(E->ev0, st));
   CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, 0, st));
@@ -1318,6 +1340,16 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   CK(cudaMemcpy(E->h_state.data(), E->d_state, sizeof(State) * E->max_slots, cudaMemcpyDeviceToHost));
   E->iterations += c.iters;
   E->d2h += (int64_t)(sizeof(Ctl) + sizeof(State) * E->max_slots);
+  if (E->d_stamps && c.iters > 0) {
+    long long k = std::min<long long>(5 * c.iters, E->stamp_cap);
+    std::vector<unsigned long long> ts(k);
+    CK(cudaMemcpy(ts.data(), E->d_stamps, 8 * k, cudaMemcpyDeviceToHost));
+    if (FILE* f = fopen(E->stamp_path, "a")) {
+      fprintf(f, "run blocks=%d threads=%d iters=%lld\n", E->blocks, E->threads, (long long)c.iters);
+      for (long long i = 0; i < k; ++i) fprintf(f, "%llu%c", ts[i], (i % 5 == 4) ? '\n' : ' ');
+      fclose(f);
+    }
+  }
   int active = 0;
   for (int s = 0; s < E->max_slots; ++s)
     if (E->slots[s].used && (E->h_state[s].status == ST_EXPAND || E->h_state[s].status == ST_REPOP)) active++;

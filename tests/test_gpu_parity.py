@@ -92,7 +92,7 @@ def _compare_solves(p, oracle_lib, box_cap=4096):
         assert _same(rg.trace[k], ro.trace[k]), k
     assert rg.lb == ro.lb and rg.ub == ro.ub
     assert rg.pool_size == ro.pool_size and rg.n_boxes == ro.n_boxes
-    assert _same(rg.boxes.reshape(len(rg.boxes), -1), ro.boxes)
+    assert _same(rg.boxes.reshape(rg.boxes.shape[0], 2 * p.n), ro.boxes.reshape(ro.boxes.shape[0], 2 * p.n))
     assert _same(rg.box_lbs, ro.box_lbs)
     return rg, ro
 
