@@ -45,6 +45,10 @@ constexpr int MAX_THREADS = 512;  // block size is 256 or 512
 // instance life cycle
 enum { ST_FREE = 0, ST_EXPAND = 1, ST_REPOP = 2, ST_DONE = 3 };
 
+// Pools up to this many entries are compacted and searched by one block right
+// after the instance's children are done; larger pools take the grid-wide path.
+constexpr long long POOL_BLOCK_MAX = 1LL << 15;
+
 struct State {
   int status;                 // ST_*
   int outcome;                // GPUGO_CERTIFIED / FINISHED / ITER_LIMIT or GPUGO_ERR_*
@@ -55,16 +59,16 @@ struct State {
   unsigned long long ub_start;
   unsigned long long ub_who;  // row << 40 | code << 8 | sample index of the point that set the UB
   long long count;            // entries in the live buffer
-  long long count_new;        // entries written to the other buffer by a compaction
+  long long count_new;        // entries written to the other buffer by a grid-wide compaction
   long long count_before;     // live entries before this iteration's appends
-  long long removed_new;      // this iteration's appends dropped by the compaction
+  long long removed_new;      // this iteration's appends dropped by a grid-wide compaction
   long long out_count;        // boxes emitted by the width rule
   double out_lb_min;
   long long bounded;          // children bounded
   long long samples;          // children whose samples were evaluated
   long long ubc_count;        // UB candidates recorded this iteration
   long long m_children;       // children of the current parent
-  long long n_surv_last;
+  long long b_done;           // children of this iteration already processed
   int has_who;
   int pad;
 };
@@ -75,24 +79,29 @@ struct Ctl {
   int error;
   int nA;                     // instances expanding this iteration
   int nE;                     // instances active this iteration
-  int pad;
+  int nBig;                   // instances whose pool takes the grid-wide path
   long long totA, totB, totD; // flat work sizes
   long long iters;            // iterations run by the last launch
+  int q_tail;                 // ready queue: slots reserved
+  int q_head;                 // ready queue: slots claimed
+  int n_big_q;                // big list length (appended during the children phase)
+  unsigned int epoch;         // iteration tag of the ready-queue entries
 };
 
 struct KArgs {
   Desc* desc;
   State* st;
   Ctl* ctl;
-  int* idsA;                  // [max_slots]
-  long long* prefA;           // [max_slots + 1]
-  long long* prefB;
-  int* idsE;
-  long long* prefD;
+  int* idsA;                  // [max_slots] expanding instances
+  long long* prefA;           // [max_slots + 1] table items prefix
+  long long* prefB;           // [max_slots + 1] children prefix
+  int* idsE;                  // [max_slots] big-pool instances (grid-wide path)
+  long long* prefD;           // [max_slots + 1] pool tiles prefix of big instances
+  unsigned long long* queue;  // [max_slots] ready queue entries: epoch << 32 | slot
   int max_slots;
   long long max_iters;        // iterations in this launch (<= 0: until idle)
   unsigned long long timeout_ns;
-  unsigned long long* stamps; // optional: %globaltimer at each barrier release, 5 per iteration
+  unsigned long long* stamps; // optional: %globaltimer at each barrier release
   long long stamp_cap;
 };
 
@@ -105,6 +114,10 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __device__ __forceinline__ double atomic_ub_read(const unsigned long long* p) {
   return ord_val(*(volatile const unsigned long long*)p);
 }
+
+// Reads of values other blocks wrote during the current phase bypass L1.
+template <typename T>
+__device__ __forceinline__ T vload(const T& x) { return *(volatile const T*)&x; }
 
 // ---------------------------------------------------------------------------
 // block-wide helpers
@@ -138,6 +151,42 @@ __device__ T block_exclusive_scan(T v, T* total) {
   return base + x - v;
 }
 
+struct Best {
+  unsigned long long lbk, key, idx;
+};
+
+__device__ __forceinline__ bool best_less(const Best& x, const Best& y) {
+  if (x.lbk != y.lbk) return x.lbk < y.lbk;
+  return x.key < y.key;
+}
+
+__device__ __forceinline__ Best best_none() { Best b; b.lbk = ~0ULL; b.key = ~0ULL; b.idx = ~0ULL; return b; }
+
+__device__ __forceinline__ Best warp_min(Best b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.lbk = __shfl_xor_sync(0xffffffffu, b.lbk, o);
+    c.key = __shfl_xor_sync(0xffffffffu, b.key, o);
+    c.idx = __shfl_xor_sync(0xffffffffu, b.idx, o);
+    if (best_less(c, b)) b = c;
+  }
+  return b;
+}
+
+// every thread of the block returns the block minimum
+__device__ Best block_min(Best b) {
+  __shared__ Best s_b[MAX_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  b = warp_min(b);
+  if (lane == 0) s_b[wid] = b;
+  __syncthreads();
+  Best c = (lane < nw) ? s_b[lane] : best_none();
+  c = warp_min(c);
+  __syncthreads();
+  return c;
+}
+
 // ---------------------------------------------------------------------------
 // work lists (run by the last block at a barrier)
 // ---------------------------------------------------------------------------
@@ -148,22 +197,26 @@ __device__ long long children_of(const Desc& D, int cyc) {
   return m;
 }
 
-// lists for phases A, B, E from the instance states
-__device__ void build_lists_AE(const KArgs& a) {
+// Lists for the next iteration: expanding instances (tables, children) and the
+// ready queue pre-filled with instances that only pop (width-rule emissions).
+__device__ void build_lists(const KArgs& a) {
   const int S = a.max_slots;
   const int per = (S + blockDim.x - 1) / blockDim.x;
   const int lo = threadIdx.x * per, hi = min(S, lo + per);
-  long long cA = 0, cE = 0, sA = 0, sB = 0;
+  long long cA = 0, cE = 0, cR = 0, sA = 0, sB = 0;
   for (int s = lo; s < hi; ++s) {
     int stt = a.st[s].status;
     if (stt == ST_EXPAND) { cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children; }
+    if (stt == ST_REPOP) cR++;
     if (stt == ST_EXPAND || stt == ST_REPOP) cE++;
   }
-  long long tA, tE, tSA, tSB;
+  long long tA, tE, tR, tSA, tSB;
   long long oA = block_exclusive_scan(cA, &tA);
   long long oE = block_exclusive_scan(cE, &tE);
+  long long oR = block_exclusive_scan(cR, &tR);
   long long oSA = block_exclusive_scan(sA, &tSA);
   long long oSB = block_exclusive_scan(sB, &tSB);
+  (void)oE;
   for (int s = lo; s < hi; ++s) {
     int stt = a.st[s].status;
     if (stt == ST_EXPAND) {
@@ -174,7 +227,7 @@ __device__ void build_lists_AE(const KArgs& a) {
       oSA += a.desc[s].a_items;
       oSB += a.st[s].m_children;
     }
-    if (stt == ST_EXPAND || stt == ST_REPOP) a.idsE[oE++] = s;
+    if (stt == ST_REPOP) a.queue[oR++] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
   }
   if (threadIdx.x == 0) {
     a.prefA[tA] = tSA;
@@ -183,6 +236,11 @@ __device__ void build_lists_AE(const KArgs& a) {
     a.ctl->nE = (int)tE;
     a.ctl->totA = tSA;
     a.ctl->totB = tSB;
+    a.ctl->q_tail = (int)tR;
+    a.ctl->q_head = 0;
+    a.ctl->n_big_q = 0;
+    a.ctl->nBig = 0;
+    a.ctl->epoch = a.ctl->epoch + 1;
   }
 }
 
@@ -191,11 +249,11 @@ __device__ __forceinline__ long long pool_tiles(const Desc& D, const State& st) 
   return (c + TD - 1) / TD;
 }
 
-// pool tiles per active instance (after phase B's appends)
-__device__ void build_list_D(const KArgs& a) {
-  const int nE = a.ctl->nE;
-  const int per = (nE + blockDim.x - 1) / blockDim.x;
-  const int lo = threadIdx.x * per, hi = min(nE, lo + per);
+// pool tiles of the big-pool instances (grid-wide path)
+__device__ void build_list_big(const KArgs& a) {
+  const int nB = a.ctl->n_big_q;
+  const int per = (nB + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(nB, lo + per);
   long long t = 0;
   for (int k = lo; k < hi; ++k) t += pool_tiles(a.desc[a.idsE[k]], a.st[a.idsE[k]]);
   long long tot;
@@ -205,8 +263,9 @@ __device__ void build_list_D(const KArgs& a) {
     o += pool_tiles(a.desc[a.idsE[k]], a.st[a.idsE[k]]);
   }
   if (threadIdx.x == 0) {
-    a.prefD[nE] = tot;
+    a.prefD[nB] = tot;
     a.ctl->totD = tot;
+    a.ctl->nBig = nB;
   }
 }
 
@@ -231,7 +290,7 @@ __device__ bool grid_barrier(const KArgs& a, Tail tail) {
           s_ok = 0;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(32);
       }
     }
     __threadfence();
@@ -254,8 +313,7 @@ __device__ bool grid_barrier(const KArgs& a, Tail tail) {
 
 struct NoTail { __device__ void operator()() const {} };
 
-// locate the list position k with pref[k] <= item < pref[k+1], starting the linear
-// walk from a hint (consecutive items mostly share an instance)
+// list position k with pref[k] <= item < pref[k+1]; walks forward from a hint
 __device__ __forceinline__ int find_seg(const long long* pref, int n, long long item, int hint) {
   int k = hint;
   if (k < 0 || k >= n || pref[k] > item) {
@@ -271,14 +329,18 @@ __device__ __forceinline__ int find_seg(const long long* pref, int n, long long 
 }
 
 // ---------------------------------------------------------------------------
-// phase A: term tables
+// phase A: term tables; items are dealt round-robin over the blocks so that the
+// FP64 work of a single instance spreads over every SM
 // ---------------------------------------------------------------------------
 __device__ void phase_tables(const KArgs& a) {
   const long long tot = a.ctl->totA;
   const int nA = a.ctl->nA;
-  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long G = gridDim.x;
   int hint = -1;
-  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < tot; it += stride) {
+  for (long long r = 0;; ++r) {
+    long long it = (r * blockDim.x + threadIdx.x) * G + blockIdx.x;
+    if ((r * blockDim.x) * G >= tot) break;
+    if (it >= tot) continue;
     int k = find_seg(a.prefA, nA, it, hint);
     hint = k;
     int s = a.idsA[k];
@@ -289,24 +351,260 @@ __device__ void phase_tables(const KArgs& a) {
 }
 
 // ---------------------------------------------------------------------------
-// phase B: children
+// selection: one warp finishes an instance's iteration
 // ---------------------------------------------------------------------------
+// The point that set the UB: the smallest recorded (code, sample) whose sampled
+// upper bound equals the new UB.
+__device__ void locate_who(const Desc& D, State& st) {
+  const int lane = threadIdx.x & 31;
+  const long long ubc = vload(st.ubc_count);
+  long long nc = ubc < D.ubc_cap ? ubc : D.ubc_cap;
+  const double ubv = ord_val(vload(st.ub));
+  unsigned long long who = ~0ULL;
+  for (long long c = lane; c < nc; c += 32) {
+    double v = __ldcg(D.ubc_val + c);
+    unsigned long long id = __ldcg(D.ubc_id + c);
+    if (v == ubv && id < who) who = id;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long y = __shfl_xor_sync(0xffffffffu, who, o);
+    who = y < who ? y : who;
+  }
+  if (lane == 0) {
+    if (who != ~0ULL) { st.ub_who = ((unsigned long long)st.iter << 40) | who; st.has_who = 1; }
+    else if (ubc > D.ubc_cap) st.has_who = 0;
+  }
+  __syncwarp();
+}
+
+// Pop the best list entry and apply the width / gap rules (ackley50.py:1269-1370).
+// `cnt` live entries in buffer st.cur, `b` their minimum, `n_surv` survivors appended.
+__device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt, long long n_surv,
+                                 bool expanded) {
+  const int lane = threadIdx.x & 31;
+  const int n = D.n;
+  if (lane == 0) {
+    st.count = cnt;
+    if (expanded) {
+      st.bounded += st.m_children;
+      if (st.iter < D.trace_cap) {
+        D.tr_ub[st.iter] = ord_val(st.ub);
+        D.tr_surv[st.iter] = n_surv;
+        D.tr_pool[st.iter] = cnt;
+        D.tr_sel[st.iter] = -1;
+      }
+    }
+  }
+  __syncwarp();
+  int decision = 0;  // 0 stop, 1 emit (pop again next iteration), 2 expand
+  unsigned long long key = 0;
+  int ccyc = 1;
+  if (lane == 0) {
+    if (vload(st.outcome) < 0) {
+      decision = 0;
+    } else if (cnt == 0 || b.idx == ~0ULL) {
+      st.outcome = GPUGO_FINISHED;
+    } else {
+      double lbbest = ord_val(b.lbk);
+      double lbstar = lbbest < st.out_lb_min ? lbbest : st.out_lb_min;
+      if (D.stop_mode == STOP_GAP && ord_val(st.ub) - lbstar <= D.gap_tol) {
+        st.outcome = GPUGO_CERTIFIED;
+      } else {
+        const int c = st.cur;
+        long long last = cnt - 1;
+        D.pool_lb[c][b.idx] = __ldcg(D.pool_lb[c] + last);
+        D.pool_key[c][b.idx] = __ldcg(D.pool_key[c] + last);
+        st.count = last;
+        key = b.key;
+        long long prow = (long long)(key >> 32);
+        unsigned long long code = key & 0xffffffffULL;
+        ccyc = D.pcyc[prow];
+        const double* pb = D.parents + 2LL * n * prow;
+        int gsz = group_size(n, D.group, ccyc);
+        iv x0 = child_iv(D, pb, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
+        double width = __dsub_rn(x0.hi, x0.lo);
+        if (width < D.width_tol && ccyc == D.max_cyc) {
+          decision = 1;
+          long long o = st.out_count;
+          if (o < D.out_cap) { D.out_key[o] = key; D.out_lb[o] = lbbest; }
+          st.out_count = o + 1;
+          if (lbbest < st.out_lb_min) st.out_lb_min = lbbest;
+        } else if (st.iter + 1 >= D.parent_cap) {
+          st.outcome = GPUGO_ERR_PARENT_OVERFLOW;
+        } else {
+          decision = 2;
+          if (st.iter < D.trace_cap) D.tr_sel[st.iter] = (long long)key;
+        }
+      }
+    }
+  }
+  decision = __shfl_sync(0xffffffffu, decision, 0);
+  key = __shfl_sync(0xffffffffu, key, 0);
+  ccyc = __shfl_sync(0xffffffffu, ccyc, 0);
+  if (decision == 2) {
+    const long long prow = (long long)(key >> 32);
+    const unsigned long long code = key & 0xffffffffULL;
+    const double* pb = D.parents + 2LL * n * prow;
+    double* nb = D.parents + 2LL * n * (st.iter + 1);
+    const int gsz = group_size(n, D.group, ccyc);
+    for (int i = lane; i < n; i += 32) {
+      iv x = child_iv(D, pb, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
+      nb[2 * i] = x.lo;
+      nb[2 * i + 1] = x.hi;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    if (decision == 0) {
+      st.status = ST_DONE;
+      if (st.outcome == 0) st.outcome = GPUGO_FINISHED;
+    } else if (decision == 1) {
+      st.status = ST_REPOP;
+    } else {
+      long long row = st.iter + 1;
+      int ncyc = (ccyc == D.max_cyc) ? 1 : ccyc + D.group;
+      D.pcyc[row] = ncyc;
+      st.iter = row;
+      st.cyc = ncyc;
+      st.m_children = children_of(D, ncyc);
+      if (D.max_iter > 0 && row >= D.max_iter) {
+        st.status = ST_DONE;
+        st.outcome = GPUGO_ITER_LIMIT;
+      } else {
+        st.status = ST_EXPAND;
+      }
+    }
+    st.ub_start = st.ub;
+    st.count_before = st.count;
+    st.ubc_count = 0;
+    st.b_done = 0;
+    st.removed_new = 0;
+  }
+  __syncwarp();
+}
+
+// Block-level list update of one instance whose children are all done:
+// in-place compaction when the UB moved (list rule-out, ackley50.py:1154-1166),
+// argmin (ackley50.py:1273), then the selection.
+__device__ void block_instance(const KArgs& a, int s) {
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  const bool expanded = (vload(st.status) == ST_EXPAND);
+  const long long count = vload(st.count);
+  long long cnt = count < D.pool_cap ? count : D.pool_cap;
+  if (vload(st.outcome) < 0) cnt = 0;
+  const unsigned long long ubk = vload(st.ub);
+  const bool compact = ubk != vload(st.ub_start);
+  const double ub = ord_val(ubk);
+  const long long before = vload(st.count_before);
+  const int c = vload(st.cur);
+  if (expanded && compact && threadIdx.x < 32) locate_who(D, st);
+  Best b = best_none();
+  long long kept = 0, removed_new = 0;
+  for (long long base = 0; base < cnt; base += blockDim.x) {
+    long long e = base + threadIdx.x;
+    bool in = e < cnt;
+    double lbv = in ? __ldcg(D.pool_lb[c] + e) : 0.0;
+    unsigned long long key = in ? __ldcg(D.pool_key[c] + e) : 0ULL;
+    bool keep = in && !(compact && lbv > ub);
+    if (in && !keep && e >= before) removed_new++;
+    long long pos = e;
+    if (compact) {
+      long long tot;
+      long long off = block_exclusive_scan((long long)keep, &tot);  // synchronises: all reads done
+      pos = kept + off;
+      if (keep) {
+        D.pool_lb[c][pos] = lbv;
+        D.pool_key[c][pos] = key;
+      }
+      kept += tot;
+    }
+    if (keep) {
+      Best cb; cb.lbk = ord_key(lbv); cb.key = key; cb.idx = (unsigned long long)pos;
+      if (best_less(cb, b)) b = cb;
+    }
+  }
+  if (!compact) kept = cnt;
+  long long rn;
+  block_exclusive_scan(removed_new, &rn);
+  b = block_min(b);
+  if (threadIdx.x < 32) {
+    long long n_surv = (cnt - before) - rn;
+    finish_iteration(D, st, b, kept, n_surv, expanded);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// phase B: children; each block takes a contiguous range of the flat list
+// ---------------------------------------------------------------------------
+__device__ void drain_queue(const KArgs& a) {
+  __shared__ int s_s;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_s = -1;
+      for (;;) {
+        int h = *(volatile int*)&a.ctl->q_head;
+        int t = *(volatile int*)&a.ctl->q_tail;
+        if (h >= t) break;
+        if (atomicCAS(&a.ctl->q_head, h, h + 1) == h) {
+          // the slot was reserved before q_tail moved; its entry lands right after
+          const unsigned int ep = a.ctl->epoch;
+          unsigned long long t0 = gtimer();
+          unsigned long long v;
+          while (((v = *(volatile unsigned long long*)&a.queue[h]) >> 32) != ep) {
+            if (gtimer() - t0 > a.timeout_ns) { atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT); break; }
+          }
+          s_s = ((v >> 32) == ep) ? (int)(v & 0xffffffffu) : -1;
+          __threadfence();
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    int s = s_s;
+    __syncthreads();
+    if (s < 0) return;
+    const Desc& D = a.desc[s];
+    const State& st = a.st[s];
+    const long long cnt_now = vload(st.count);
+    if ((cnt_now < D.pool_cap ? cnt_now : D.pool_cap) > POOL_BLOCK_MAX) {
+      if (threadIdx.x == 0) {
+        int k = atomicAdd(&a.ctl->n_big_q, 1);
+        a.idsE[k] = s;
+      }
+      __syncthreads();
+    } else {
+      block_instance(a, s);
+    }
+    if (threadIdx.x == 0) __threadfence();
+  }
+}
+
+__device__ __forceinline__ void queue_push(const KArgs& a, int s) {
+  __threadfence();
+  int slot = atomicAdd(&a.ctl->q_tail, 1);
+  *(volatile unsigned long long*)&a.queue[slot] = ((unsigned long long)a.ctl->epoch << 32) | (unsigned)s;
+  __threadfence();
+}
+
 __device__ void phase_children(const KArgs& a) {
   const long long tot = a.ctl->totB;
   const int nA = a.ctl->nA;
-  const long long stride = (long long)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
+  // contiguous range of this block, whole warps
+  long long per = (tot + gridDim.x - 1) / gridDim.x;
+  per = (per + 31) & ~31LL;
+  const long long lo = min(tot, per * blockIdx.x), hi = min(tot, lo + per);
   int hint = -1;
-  // the loop runs whole warps so that every lane joins the collectives below
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < tot; base += stride) {
+  for (long long base = lo; base < hi; base += blockDim.x) {
     long long it = base + threadIdx.x;
-    bool valid = it < tot;
+    bool valid = it < hi;
     int k = valid ? find_seg(a.prefB, nA, it, hint) : -1;
     if (valid) hint = k;
     int s = valid ? a.idsA[k] : -1;
     double lb = 0.0;
-    bool keep = false;
-    bool sampled = false;
+    bool keep = false, sampled = false;
     unsigned long long code = 0;
     if (valid) {
       const Desc& D = a.desc[s];
@@ -322,8 +620,7 @@ __device__ void phase_children(const KArgs& a) {
         double sm = child_samp(D, C, code, &jb);
         sampled = true;
         if (sm == 0.0) sm = 0.0;  // -0 -> +0
-        double ub0 = ord_val(st.ub_start);
-        if (sm < ub0) {
+        if (sm < ord_val(st.ub_start)) {
           long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
           if (slot < D.ubc_cap) {
             D.ubc_val[slot] = sm;
@@ -337,18 +634,16 @@ __device__ void phase_children(const KArgs& a) {
         if (lb <= ub) keep = !child_deriv(D, C, code);
       }
     }
-    // warp-aggregated statistics and appends, grouped by instance
-    unsigned int active = __ballot_sync(0xffffffffu, valid);
+    // appends and sample counts, aggregated per warp and instance
+    unsigned int active = __ballot_sync(0xffffffffu, valid && (keep || sampled));
     while (active) {
       int leader = __ffs(active) - 1;
       int ls = __shfl_sync(0xffffffffu, s, leader);
-      unsigned int same = __ballot_sync(0xffffffffu, valid && s == ls);
       unsigned int kmask = __ballot_sync(0xffffffffu, valid && s == ls && keep);
       unsigned int smask = __ballot_sync(0xffffffffu, valid && s == ls && sampled);
       long long basepos = 0;
       if (lane == leader) {
         State& st = a.st[ls];
-        atomicAdd((unsigned long long*)&st.bounded, (unsigned long long)__popc(same));
         if (smask) atomicAdd((unsigned long long*)&st.samples, (unsigned long long)__popc(smask));
         if (kmask) basepos = (long long)atomicAdd((unsigned long long*)&st.count, (unsigned long long)__popc(kmask));
       }
@@ -364,43 +659,38 @@ __device__ void phase_children(const KArgs& a) {
           atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
         }
       }
-      active &= ~same;
+      active &= ~(kmask | smask);
     }
   }
-}
-
-// ---------------------------------------------------------------------------
-// phase D: pool compaction + per-tile argmin
-// ---------------------------------------------------------------------------
-struct Best {
-  unsigned long long lbk, key, idx;
-};
-
-__device__ __forceinline__ bool best_less(const Best& x, const Best& y) {
-  if (x.lbk != y.lbk) return x.lbk < y.lbk;
-  return x.key < y.key;
-}
-
-__device__ __forceinline__ Best warp_min(Best b) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    Best c;
-    c.lbk = __shfl_xor_sync(0xffffffffu, b.lbk, o);
-    c.key = __shfl_xor_sync(0xffffffffu, b.key, o);
-    c.idx = __shfl_xor_sync(0xffffffffu, b.idx, o);
-    if (best_less(c, b)) b = c;
+  // report this block's share of each instance; the block completing an instance queues it
+  __syncthreads();
+  if (threadIdx.x == 0 && lo < hi) {
+    int k = find_seg(a.prefB, nA, lo, -1);
+    for (; k < nA && a.prefB[k] < hi; ++k) {
+      long long seg_lo = max(lo, a.prefB[k]), seg_hi = min(hi, a.prefB[k + 1]);
+      long long n_here = seg_hi - seg_lo;
+      if (n_here <= 0) continue;
+      int s = a.idsA[k];
+      State& st = a.st[s];
+      __threadfence();
+      unsigned long long old = atomicAdd((unsigned long long*)&st.b_done, (unsigned long long)n_here);
+      if ((long long)old + n_here == st.m_children) queue_push(a, s);
+    }
   }
-  return b;
+  __syncthreads();
+  drain_queue(a);
 }
 
+// ---------------------------------------------------------------------------
+// grid-wide path for large pools: compaction + per-tile argmin, then selection
+// ---------------------------------------------------------------------------
 __device__ void phase_pool(const KArgs& a) {
-  __shared__ Best s_b[MAX_THREADS / 32];
   const long long tot = a.ctl->totD;
-  const int nE = a.ctl->nE;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nB = a.ctl->nBig;
+  const int lane = threadIdx.x & 31;
   int hint = -1;
   for (long long t = blockIdx.x; t < tot; t += gridDim.x) {
-    int k = find_seg(a.prefD, nE, t, hint);
+    int k = find_seg(a.prefD, nB, t, hint);
     hint = k;
     int s = a.idsE[k];
     const Desc& D = a.desc[s];
@@ -411,8 +701,7 @@ __device__ void phase_pool(const KArgs& a) {
     const double ub = ord_val(st.ub);
     const int cur = st.cur;
     const long long lo = tile * TD, hi = min(cnt, lo + TD);
-    Best b;
-    b.lbk = ~0ULL; b.key = ~0ULL; b.idx = ~0ULL;
+    Best b = best_none();
     long long removed_new = 0;
     for (long long e0 = lo; e0 < hi; e0 += blockDim.x) {
       long long e = e0 + threadIdx.x;
@@ -434,8 +723,7 @@ __device__ void phase_pool(const KArgs& a) {
         }
       }
       if (keep) {
-        Best c;
-        c.lbk = ord_key(lbv); c.key = key; c.idx = pos;
+        Best c; c.lbk = ord_key(lbv); c.key = key; c.idx = pos;
         if (best_less(c, b)) b = c;
       }
     }
@@ -443,213 +731,87 @@ __device__ void phase_pool(const KArgs& a) {
       for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
       if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
     }
-    b = warp_min(b);
-    if (lane == 0) s_b[wid] = b;
-    __syncthreads();
-    if (wid == 0) {
-      Best c = (lane < nw) ? s_b[lane] : Best{~0ULL, ~0ULL, ~0ULL};
-      c = warp_min(c);
-      if (lane == 0) {
-        unsigned long long* tb = D.tile_best + 3 * tile;
-        tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
-      }
+    b = block_min(b);
+    if (threadIdx.x == 0) {
+      unsigned long long* tb = D.tile_best + 3 * tile;
+      tb[0] = b.lbk; tb[1] = b.key; tb[2] = b.idx;
     }
     __syncthreads();
   }
 }
 
-// ---------------------------------------------------------------------------
-// phase E: selection (one warp per active instance)
-// ---------------------------------------------------------------------------
-__device__ void phase_select(const KArgs& a) {
-  const int nE = a.ctl->nE;
+__device__ void phase_select_big(const KArgs& a) {
+  const int nB = a.ctl->nBig;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int k = gw; k < nE; k += nwarps) {
+  for (int k = gw; k < nB; k += nwarps) {
     int s = a.idsE[k];
     const Desc& D = a.desc[s];
     State& st = a.st[s];
-    const int n = D.n;
     const bool expanded = (st.status == ST_EXPAND);
     const bool compact = st.ub != st.ub_start;
-    long long cnt = st.count;
-    if (cnt > D.pool_cap) cnt = D.pool_cap;  // overflow already flagged
-    // minimiser point: the recorded sample whose upper bound equals the new UB
-    if (expanded && compact) {
-      long long nc = st.ubc_count < D.ubc_cap ? st.ubc_count : D.ubc_cap;
-      const double ubv = ord_val(st.ub);
-      unsigned long long who = ~0ULL;
-      for (long long c = lane; c < nc; c += 32)
-        if (D.ubc_val[c] == ubv && D.ubc_id[c] < who) who = D.ubc_id[c];
-      for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long y = __shfl_xor_sync(0xffffffffu, who, o);
-        who = y < who ? y : who;
-      }
-      if (lane == 0) {
-        if (who != ~0ULL) { st.ub_who = ((unsigned long long)st.iter << 40) | who; st.has_who = 1; }
-        else if (st.ubc_count > D.ubc_cap) st.has_who = 0;
-      }
-    }
-    __syncwarp();
-    long long n_surv = 0;
-    if (compact) {
-      n_surv = (cnt - st.count_before) - st.removed_new;
-      cnt = st.count_new;
-    } else {
-      n_surv = cnt - st.count_before;
-    }
-    // reduce the tile minima
-    Best b;
-    b.lbk = ~0ULL; b.key = ~0ULL; b.idx = ~0ULL;
-    const long long tiles = pool_tiles(D, st);  // tiles of phase D (count before compaction)
+    long long cnt = st.count < D.pool_cap ? st.count : D.pool_cap;
+    if (expanded && compact) locate_who(D, st);
+    long long n_surv = (cnt - st.count_before) - (compact ? st.removed_new : 0);
+    Best b = best_none();
+    const long long tiles = pool_tiles(D, st);
     for (long long t = lane; t < tiles; t += 32) {
       const unsigned long long* tb = D.tile_best + 3 * t;
       Best c; c.lbk = tb[0]; c.key = tb[1]; c.idx = tb[2];
       if (best_less(c, b)) b = c;
     }
     b = warp_min(b);
-    __syncwarp();
-    if (lane == 0) {
-      if (compact) { st.cur ^= 1; st.count_new = 0; }
-      st.count = cnt;
-      st.removed_new = 0;
-      if (expanded) {
-        st.n_surv_last = n_surv;
-        if (st.iter < D.trace_cap) {
-          D.tr_ub[st.iter] = ord_val(st.ub);
-          D.tr_surv[st.iter] = n_surv;
-          D.tr_pool[st.iter] = cnt;
-          D.tr_sel[st.iter] = -1;
-        }
-      }
+    if (compact) {
+      cnt = st.count_new;
+      __syncwarp();
+      if (lane == 0) { st.cur ^= 1; st.count_new = 0; }
+      __syncwarp();
     }
-    __syncwarp();
-    // decide (lane 0), then decode the next parent with the whole warp
-    int decision = 0;  // 0 stop, 1 emit (repop), 2 expand
-    unsigned long long key = 0;
-    double width = 0.0;
-    int ccyc = 1;
-    if (lane == 0) {
-      if (st.outcome < 0) {
-        decision = 0;
-      } else if (cnt == 0 || b.idx == ~0ULL) {
-        st.outcome = GPUGO_FINISHED;
-        decision = 0;
-      } else {
-        double lbbest = ord_val(b.lbk);
-        double lbstar = lbbest < st.out_lb_min ? lbbest : st.out_lb_min;
-        if (D.stop_mode == STOP_GAP && ord_val(st.ub) - lbstar <= D.gap_tol) {
-          st.outcome = GPUGO_CERTIFIED;
-          decision = 0;
-        } else {
-          // pop: swap-remove
-          const int c = st.cur;
-          long long last = cnt - 1;
-          D.pool_lb[c][b.idx] = D.pool_lb[c][last];
-          D.pool_key[c][b.idx] = D.pool_key[c][last];
-          st.count = last;
-          key = b.key;
-          long long prow = (long long)(key >> 32);
-          unsigned long long code = key & 0xffffffffULL;
-          ccyc = D.pcyc[prow];
-          const double* pb = D.parents + 2LL * n * prow;
-          int gsz = group_size(n, D.group, ccyc);
-          iv x0 = child_iv(D, pb, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
-          width = __dsub_rn(x0.hi, x0.lo);
-          if (width < D.width_tol && ccyc == D.max_cyc) {
-            decision = 1;
-            long long o = st.out_count;
-            if (o < D.out_cap) { D.out_key[o] = key; D.out_lb[o] = lbbest; }
-            st.out_count = o + 1;
-            if (lbbest < st.out_lb_min) st.out_lb_min = lbbest;
-          } else if (st.iter + 1 >= D.parent_cap) {
-            st.outcome = GPUGO_ERR_PARENT_OVERFLOW;
-            decision = 0;
-          } else {
-            decision = 2;
-            if (st.iter < D.trace_cap) D.tr_sel[st.iter] = (long long)key;
-          }
-        }
-      }
-    }
-    decision = __shfl_sync(0xffffffffu, decision, 0);
-    key = __shfl_sync(0xffffffffu, key, 0);
-    ccyc = __shfl_sync(0xffffffffu, ccyc, 0);
-    if (decision == 2) {
-      const long long prow = (long long)(key >> 32);
-      const unsigned long long code = key & 0xffffffffULL;
-      const double* pb = D.parents + 2LL * n * prow;
-      double* nb = D.parents + 2LL * n * (st.iter + 1);
-      const int gsz = group_size(n, D.group, ccyc);
-      for (int i = lane; i < n; i += 32) {
-        iv x = child_iv(D, pb, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
-        nb[2 * i] = x.lo;
-        nb[2 * i + 1] = x.hi;
-      }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      if (decision == 0) {
-        st.status = ST_DONE;
-        if (st.outcome == 0) st.outcome = GPUGO_FINISHED;
-      } else if (decision == 1) {
-        st.status = ST_REPOP;
-      } else {
-        long long row = st.iter + 1;
-        int ncyc = (ccyc == D.max_cyc) ? 1 : ccyc + D.group;
-        D.pcyc[row] = ncyc;
-        st.iter = row;
-        st.cyc = ncyc;
-        st.m_children = children_of(D, ncyc);
-        if (D.max_iter > 0 && row >= D.max_iter) {
-          st.status = ST_DONE;
-          st.outcome = GPUGO_ITER_LIMIT;
-        } else {
-          st.status = ST_EXPAND;
-        }
-      }
-      st.ub_start = st.ub;
-      st.count_before = st.count;
-      st.ubc_count = 0;
-    }
-    __syncwarp();
+    finish_iteration(D, st, b, cnt, n_surv, expanded);
   }
 }
 
-struct TailAE {
+struct TailLists {
   const KArgs* a;
-  __device__ void operator()() const { build_lists_AE(*a); }
+  __device__ void operator()() const { build_lists(*a); }
 };
-struct TailD {
+struct TailAfterChildren {
   const KArgs* a;
-  __device__ void operator()() const { build_list_D(*a); }
+  __device__ void operator()() const {
+    const bool big = *(volatile int*)&a->ctl->n_big_q > 0;
+    if (big) build_list_big(*a);
+    else build_lists(*a);
+  }
 };
 
 __device__ __forceinline__ void stamp(const KArgs& a, long long it, int k) {
   if (a.stamps && blockIdx.x == 0 && threadIdx.x == 0 && (it * 5 + k) < a.stamp_cap) a.stamps[it * 5 + k] = gtimer();
 }
 
-__global__ void __launch_bounds__(MAX_THREADS) solve_kernel(KArgs a) {
-  TailAE tae{&a};
-  TailD td{&a};
-  if (!grid_barrier(a, tae)) return;
+__global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
+  TailLists tl{&a};
+  TailAfterChildren tc{&a};
+  // queue entries of earlier launches carry stale epochs
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_slots; i += gridDim.x * blockDim.x) a.queue[i] = 0ULL;
+  if (!grid_barrier(a, tl)) return;
   long long it = 0;
   while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
     stamp(a, it, 0);
-    if (a.ctl->nA > 0) {
-      phase_tables(a);
-      if (!grid_barrier(a, NoTail{})) return;
-      stamp(a, it, 1);
-      phase_children(a);
-    }
-    if (!grid_barrier(a, td)) return;
-    stamp(a, it, 2);
-    phase_pool(a);
+    phase_tables(a);
     if (!grid_barrier(a, NoTail{})) return;
-    stamp(a, it, 3);
-    phase_select(a);
-    if (!grid_barrier(a, tae)) return;
+    stamp(a, it, 1);
+    phase_children(a);
+    // queue slots are reset before the next iteration reuses them
+    if (!grid_barrier(a, tc)) return;
+    stamp(a, it, 2);
+    if (a.ctl->nBig > 0) {
+      phase_pool(a);
+      if (!grid_barrier(a, NoTail{})) return;
+      stamp(a, it, 3);
+      phase_select_big(a);
+      if (!grid_barrier(a, tl)) return;
+    }
     stamp(a, it, 4);
     ++it;
   }
@@ -774,6 +936,7 @@ struct gpugo_engine {
   State* d_state = nullptr;
   Ctl* d_ctl = nullptr;
   int* d_ids = nullptr;          // idsA | idsE | init list
+  unsigned long long* d_queue = nullptr;
   long long* d_pref = nullptr;   // prefA | prefB | prefD
   char* d_arena = nullptr;
   Arena arena;
@@ -1194,6 +1357,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaMalloc(&E->d_ctl, sizeof(Ctl))))) break;
     if ((rc = cuda_err(cudaMemset(E->d_ctl, 0, sizeof(Ctl))))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_ids, sizeof(int) * 3 * E->max_slots)))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_queue, sizeof(unsigned long long) * E->max_slots)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
@@ -1216,7 +1380,7 @@ int gpugo_engine_destroy(gpugo_engine* E) {
   if (!E) return GPUGO_OK;
   if (E->stream) cudaStreamSynchronize(E->stream);
   cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
-  cudaFree(E->d_ids); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps);
+  cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->stream) cudaStreamDestroy(E->stream);
@@ -1320,6 +1484,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.prefA = E->d_pref;
   a.prefB = E->d_pref + (E->max_slots + 1);
   a.prefD = E->d_pref + 2 * (E->max_slots + 1);
+  a.queue = E->d_queue;
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
