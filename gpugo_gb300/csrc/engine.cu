@@ -47,7 +47,10 @@ enum { ST_FREE = 0, ST_EXPAND = 1, ST_REPOP = 2, ST_DONE = 3 };
 
 // Pools up to this many entries are compacted and searched by one block right
 // after the instance's children are done; larger pools take the grid-wide path.
-constexpr long long POOL_BLOCK_MAX = 1LL << 15;
+constexpr long long POOL_BLOCK_MAX = 1LL << 12;
+
+// Shared memory per block holding one instance's term tables during phase B.
+constexpr int SMEM_TAB_BYTES = 96 * 1024;
 
 struct State {
   int status;                 // ST_*
@@ -589,6 +592,8 @@ __device__ __forceinline__ void queue_push(const KArgs& a, int s) {
 }
 
 __device__ void phase_children(const KArgs& a) {
+  extern __shared__ double s_tab[];
+  __shared__ int s_inst, s_cached;
   const long long tot = a.ctl->totB;
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
@@ -596,8 +601,27 @@ __device__ void phase_children(const KArgs& a) {
   long long per = (tot + gridDim.x - 1) / gridDim.x;
   per = (per + 31) & ~31LL;
   const long long lo = min(tot, per * blockIdx.x), hi = min(tot, lo + per);
+  if (threadIdx.x == 0) s_cached = -1;
   int hint = -1;
   for (long long base = lo; base < hi; base += blockDim.x) {
+    // a round inside one instance reads that instance's tables from shared memory
+    if (threadIdx.x == 0) {
+      long long last = min(hi, base + (long long)blockDim.x) - 1;
+      int k0 = find_seg(a.prefB, nA, base, -1);
+      int s0 = a.idsA[k0];
+      s_inst = (a.prefB[k0 + 1] > last && a.desc[s0].tab_doubles * 8 <= SMEM_TAB_BYTES) ? s0 : -1;
+    }
+    __syncthreads();
+    const int si = s_inst;
+    if (si >= 0 && si != s_cached) {
+      const Desc& D = a.desc[si];
+      const double2* src = (const double2*)D.tab;
+      double2* dst = (double2*)s_tab;
+      const long long n2 = (D.tab_doubles + 1) / 2;
+      for (long long t = threadIdx.x; t < n2; t += blockDim.x) dst[t] = src[t];
+      __syncthreads();
+      if (threadIdx.x == 0) s_cached = si;
+    }
     long long it = base + threadIdx.x;
     bool valid = it < hi;
     int k = valid ? find_seg(a.prefB, nA, it, hint) : -1;
@@ -609,15 +633,16 @@ __device__ void phase_children(const KArgs& a) {
     if (valid) {
       const Desc& D = a.desc[s];
       State& st = a.st[s];
+      const double* T = (s == si) ? s_tab : D.tab;
       code = (unsigned long long)(it - a.prefB[k]);
       ChildCtx C;
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
-      lb = child_lb(D, C, code);
+      lb = child_lb(D, T, C, code);
       double ub = atomic_ub_read(&st.ub);
       if (lb <= ub) {
         int jb;
-        double sm = child_samp(D, C, code, &jb);
+        double sm = child_samp(D, T, C, code, &jb);
         sampled = true;
         if (sm == 0.0) sm = 0.0;  // -0 -> +0
         if (sm < ord_val(st.ub_start)) {
@@ -631,10 +656,10 @@ __device__ void phase_children(const KArgs& a) {
           atomicMin(&st.ub, ord_key(sm));
           ub = atomic_ub_read(&st.ub);
         }
-        if (lb <= ub) keep = !child_deriv(D, C, code);
+        if (lb <= ub) keep = !child_deriv(D, T, C, code);
       }
     }
-    // appends and sample counts, aggregated per warp and instance
+  // appends and sample counts, aggregated per warp and instance
     unsigned int active = __ballot_sync(0xffffffffu, valid && (keep || sampled));
     while (active) {
       int leader = __ffs(active) - 1;
@@ -661,6 +686,7 @@ __device__ void phase_children(const KArgs& a) {
       }
       active &= ~(kmask | smask);
     }
+    __syncthreads();  // the shared tables may be replaced next round
   }
   // report this block's share of each instance; the block completing an instance queues it
   __syncthreads();
@@ -845,12 +871,12 @@ __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long lo
   C.gsz = group_size(D.n, D.group, cyc);
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x) {
     unsigned long long code = codes[t];
-    double lb = child_lb(D, C, code);
+    double lb = child_lb(D, D.tab, C, code);
     int jb;
-    double sm = child_samp(D, C, code, &jb);
+    double sm = child_samp(D, D.tab, C, code, &jb);
     lb_out[t] = lb;
     samp_out[t] = sm;
-    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, C, code);
+    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, D.tab, C, code);
   }
 }
 
@@ -1085,6 +1111,7 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->max_iter = s->max_iter;
   D->pool_cap = L.pool_cap; D->parent_cap = L.parent_cap; D->out_cap = L.out_cap; D->trace_cap = L.trace_cap;
   D->tiles_cap = L.tiles_cap; D->ubc_cap = L.ubc_cap; D->a_items = L.a_items;
+  D->tab_doubles = L.tab;
   for (int i = 0; i < T_NOFF; ++i) D->t_off[i] = L.t_off[i];
   D->dom = (const double*)(base + L.o_dom);
   D->coef = (const double*)(base + L.o_coef);
@@ -1346,7 +1373,8 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     E->nsm = p.multiProcessorCount;
     if (!p.cooperativeLaunch) { rc = GPUGO_ERR_CUDA; break; }
     int occ = 0;
-    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel, E->threads, 0)))) break;
+    if ((rc = cuda_err(cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TAB_BYTES)))) break;
+    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel, E->threads, SMEM_TAB_BYTES)))) break;
     if (occ < 1) { rc = GPUGO_ERR_CUDA; break; }
     if (cfg->blocks_per_sm > 0) occ = std::min(occ, cfg->blocks_per_sm);
     E->blocks = occ * E->nsm;
@@ -1492,7 +1520,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.stamp_cap = E->stamp_cap;
   void* args[] = {&a};
   CK(cudaEventRecord(E->ev0, st));
-  CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, 0, st));
+  CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, SMEM_TAB_BYTES, st));
   CK(cudaEventRecord(E->ev1, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;

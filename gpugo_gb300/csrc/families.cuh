@@ -46,6 +46,7 @@ struct Desc {
   long long max_iter;
   long long pool_cap, parent_cap, out_cap, trace_cap, tiles_cap, ubc_cap;
   long long a_items;                 // table-build work items per iteration
+  long long tab_doubles;             // table region size (doubles)
   long long t_off[T_NOFF];           // table offsets (doubles)
   const double* dom;                 // [2n]
   const double* coef;
@@ -334,9 +335,8 @@ struct ChildCtx {
   int c0, gsz;
 };
 
-__device__ __noinline__ double child_lb(const Desc& D, ChildCtx C, unsigned long long code) {
+__device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
   const int n = D.n, w = D.wid;
-  const double* T = D.tab;
   const double* k = D.cst;
   const long long* off = D.t_off;
   switch (D.family) {
@@ -391,9 +391,9 @@ __device__ __noinline__ double child_lb(const Desc& D, ChildCtx C, unsigned long
 }
 
 // smallest sampled upper bound; *jbest receives its sample index
-__device__ __noinline__ double child_samp(const Desc& D, ChildCtx C, unsigned long long code, int* jbest) {
+__device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                          int* jbest) {
   const int n = D.n, w = D.wid, S = D.S;
-  const double* T = D.tab;
   const double* k = D.cst;
   const long long* off = D.t_off;
   double best = 0.0;
@@ -459,9 +459,8 @@ __device__ __noinline__ double child_samp(const Desc& D, ChildCtx C, unsigned lo
 }
 
 // 1 when the generalized KKT test rules the child out
-__device__ __noinline__ int child_deriv(const Desc& D, ChildCtx C, unsigned long long code) {
+__device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
   const int n = D.n, w = D.wid;
-  const double* T = D.tab;
   const double* k = D.cst;
   const long long* off = D.t_off;
   switch (D.family) {
