@@ -31,6 +31,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "ia.cuh"
@@ -106,12 +107,20 @@ struct KArgs {
   unsigned long long timeout_ns;
   unsigned long long* stamps; // optional: %globaltimer at each barrier release
   long long stamp_cap;
+  unsigned long long* bstamps; // optional: per block, per iteration: 6 timestamps inside phases A and B
+  long long bstamp_iters;
+  long long cur_it;            // iteration index for bstamps (set by the kernel loop)
 };
 
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+
+__device__ __forceinline__ void bstamp(const KArgs& a, int k) {
+  if (a.bstamps && threadIdx.x == 0 && a.cur_it < a.bstamp_iters)
+    a.bstamps[(a.cur_it * gridDim.x + blockIdx.x) * 6 + k] = gtimer();
 }
 
 __device__ __forceinline__ double atomic_ub_read(const unsigned long long* p) {
@@ -336,6 +345,7 @@ __device__ __forceinline__ int find_seg(const long long* pref, int n, long long 
 // FP64 work of a single instance spreads over every SM
 // ---------------------------------------------------------------------------
 __device__ void phase_tables(const KArgs& a) {
+  bstamp(a, 0);
   const long long tot = a.ctl->totA;
   const int nA = a.ctl->nA;
   const long long G = gridDim.x;
@@ -351,6 +361,8 @@ __device__ void phase_tables(const KArgs& a) {
     const State& st = a.st[s];
     build_item(D, D.parents + 2LL * D.n * st.iter, st.cyc, it - a.prefA[k]);
   }
+  __syncthreads();
+  bstamp(a, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -592,6 +604,7 @@ __device__ __forceinline__ void queue_push(const KArgs& a, int s) {
 }
 
 __device__ void phase_children(const KArgs& a) {
+  bstamp(a, 2);
   extern __shared__ double s_tab[];
   __shared__ int s_inst, s_cached;
   const long long tot = a.ctl->totB;
@@ -690,6 +703,7 @@ __device__ void phase_children(const KArgs& a) {
   }
   // report this block's share of each instance; the block completing an instance queues it
   __syncthreads();
+  bstamp(a, 3);
   if (threadIdx.x == 0 && lo < hi) {
     int k = find_seg(a.prefB, nA, lo, -1);
     for (; k < nA && a.prefB[k] < hi; ++k) {
@@ -704,7 +718,10 @@ __device__ void phase_children(const KArgs& a) {
     }
   }
   __syncthreads();
+  bstamp(a, 4);
   drain_queue(a);
+  __syncthreads();
+  bstamp(a, 5);
 }
 
 // ---------------------------------------------------------------------------
@@ -823,6 +840,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   if (!grid_barrier(a, tl)) return;
   long long it = 0;
   while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
+    a.cur_it = it;
     stamp(a, it, 0);
     phase_tables(a);
     if (!grid_barrier(a, NoTail{})) return;
@@ -976,6 +994,8 @@ struct gpugo_engine {
   // phase timestamps (debug aid, enabled by GPUGO_PHASE_STAMPS=<file>)
   unsigned long long* d_stamps = nullptr;
   long long stamp_cap = 0;
+  unsigned long long* d_bstamps = nullptr;
+  long long bstamp_iters = 0;
   const char* stamp_path = nullptr;
 };
 
@@ -1393,6 +1413,8 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
       E->stamp_path = sp;
       E->stamp_cap = 5 * 65536;
       if ((rc = cuda_err(cudaMalloc(&E->d_stamps, 8 * E->stamp_cap)))) break;
+      E->bstamp_iters = 64;
+      if ((rc = cuda_err(cudaMalloc(&E->d_bstamps, 8 * 6 * (size_t)E->bstamp_iters * E->blocks)))) break;
     }
     if ((rc = cuda_err(cudaEventCreate(&E->ev0)))) break;
     if ((rc = cuda_err(cudaEventCreate(&E->ev1)))) break;
@@ -1408,7 +1430,7 @@ int gpugo_engine_destroy(gpugo_engine* E) {
   if (!E) return GPUGO_OK;
   if (E->stream) cudaStreamSynchronize(E->stream);
   cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
-  cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps);
+  cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps); cudaFree(E->d_bstamps);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->stream) cudaStreamDestroy(E->stream);
@@ -1518,6 +1540,9 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
   a.stamps = E->d_stamps;
   a.stamp_cap = E->stamp_cap;
+  a.bstamps = E->d_bstamps;
+  a.bstamp_iters = E->bstamp_iters;
+  a.cur_it = 0;
   void* args[] = {&a};
   CK(cudaEventRecord(E->ev0, st));
   CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, SMEM_TAB_BYTES, st));
@@ -1540,6 +1565,15 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
     if (FILE* f = fopen(E->stamp_path, "a")) {
       fprintf(f, "run blocks=%d threads=%d iters=%lld\n", E->blocks, E->threads, (long long)c.iters);
       for (long long i = 0; i < k; ++i) fprintf(f, "%llu%c", ts[i], (i % 5 == 4) ? '\n' : ' ');
+      fclose(f);
+    }
+    long long ki = std::min<long long>(c.iters, E->bstamp_iters);
+    std::vector<unsigned long long> bs(6 * ki * E->blocks);
+    CK(cudaMemcpy(bs.data(), E->d_bstamps, 8 * bs.size(), cudaMemcpyDeviceToHost));
+    std::string bp = std::string(E->stamp_path) + ".blocks";
+    if (FILE* f = fopen(bp.c_str(), "a")) {
+      fprintf(f, "run blocks=%d iters=%lld\n", E->blocks, ki);
+      for (size_t i = 0; i < bs.size(); ++i) fprintf(f, "%llu%c", bs[i], (i % 6 == 5) ? '\n' : ' ');
       fclose(f);
     }
   }
