@@ -90,6 +90,7 @@ struct Ctl {
   int q_head;                 // ready queue: slots claimed
   int n_big_q;                // big list length (appended during the children phase)
   unsigned int epoch;         // iteration tag of the ready-queue entries
+  unsigned long long chunk_next;  // children phase: next chunk to hand out
 };
 
 struct KArgs {
@@ -253,6 +254,7 @@ __device__ void build_lists(const KArgs& a) {
     a.ctl->n_big_q = 0;
     a.ctl->nBig = 0;
     a.ctl->epoch = a.ctl->epoch + 1;
+    a.ctl->chunk_next = 0;
   }
 }
 
@@ -603,28 +605,99 @@ __device__ __forceinline__ void queue_push(const KArgs& a, int s) {
   __threadfence();
 }
 
+// order used to pick a child's smallest sampled upper bound (see samp_better)
+constexpr int J_NONE = 0x7fffffff;
+__device__ __forceinline__ bool samp_less(double v, int j, double bv, int bj) {
+  if (j == J_NONE) return false;
+  if (bj == J_NONE) return true;
+  return samp_better(v, j, bv, bj);
+}
+
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// One candidate child (its LB is not above the running UB) processed by the whole
+// warp: its sample points spread over the lanes, then its KKT coordinates.
+// Returns true when the child survives.  Every lane returns the same value.
+__device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb) {
+  const int lane = threadIdx.x & 31;
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  ChildCtx C;
+  C.c0 = st.cyc - 1;
+  C.gsz = group_size(D.n, D.group, st.cyc);
+  double ub = atomic_ub_read(&st.ub);
+  if (lb > ub) return false;
+  double bv = 0.0;
+  int bj = J_NONE;
+  for (int j = lane; j < D.S; j += 32) {
+    double v = samp_one(D, T, C, code, j);
+    if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+    int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+    if (samp_less(ov, oj, bv, bj)) { bv = ov; bj = oj; }
+  }
+  double sm = bv;
+  if (sm == 0.0) sm = 0.0;  // -0 -> +0
+  if (lane == 0) {
+    atomicAdd((unsigned long long*)&st.samples, 1ULL);
+    if (sm < ord_val(st.ub_start)) {
+      long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+      if (slot < D.ubc_cap) {
+        D.ubc_val[slot] = sm;
+        D.ubc_id[slot] = (code << 8) | (unsigned long long)bj;
+      }
+    }
+    if (sm < ub) atomicMin(&st.ub, ord_key(sm));
+  }
+  __syncwarp();
+  ub = atomic_ub_read(&st.ub);
+  ub = shfl_d(ub, 0);
+  if (lb > ub) return false;
+  DerivPre P;
+  int skip = 0;
+  if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS) {
+    if (lane == 0) skip = deriv_pre(D, T, C, code, &P);
+    skip = __shfl_sync(0xffffffffu, skip, 0);
+    P.g.lo = shfl_d(P.g.lo, 0); P.g.hi = shfl_d(P.g.hi, 0);
+    P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
+  }
+  int pruned = 0;
+  if (!skip)
+    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, code, j, P);
+  return !__any_sync(0xffffffffu, pruned);
+}
+
 __device__ void phase_children(const KArgs& a) {
   bstamp(a, 2);
   extern __shared__ double s_tab[];
+  __shared__ long long s_base;
   __shared__ int s_inst, s_cached;
   const long long tot = a.ctl->totB;
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
-  // contiguous range of this block, whole warps
-  long long per = (tot + gridDim.x - 1) / gridDim.x;
-  per = (per + 31) & ~31LL;
-  const long long lo = min(tot, per * blockIdx.x), hi = min(tot, lo + per);
+  const long long CH = blockDim.x;
   if (threadIdx.x == 0) s_cached = -1;
   int hint = -1;
-  for (long long base = lo; base < hi; base += blockDim.x) {
-    // a round inside one instance reads that instance's tables from shared memory
+  for (;;) {
+    // chunks are handed out dynamically: candidate children cluster in code space
     if (threadIdx.x == 0) {
-      long long last = min(hi, base + (long long)blockDim.x) - 1;
-      int k0 = find_seg(a.prefB, nA, base, -1);
-      int s0 = a.idsA[k0];
-      s_inst = (a.prefB[k0 + 1] > last && a.desc[s0].tab_doubles * 8 <= SMEM_TAB_BYTES) ? s0 : -1;
+      long long base = (long long)atomicAdd(&a.ctl->chunk_next, 1ULL) * CH;
+      s_base = base;
+      s_inst = -1;
+      if (base < tot) {
+        long long last = min(tot, base + CH) - 1;
+        int k0 = find_seg(a.prefB, nA, base, -1);
+        int s0 = a.idsA[k0];
+        if (a.prefB[k0 + 1] > last && a.desc[s0].tab_doubles * 8 <= SMEM_TAB_BYTES) s_inst = s0;
+      }
     }
     __syncthreads();
+    const long long base = s_base;
+    if (base >= tot) break;
+    const long long hi = min(tot, base + CH);
     const int si = s_inst;
     if (si >= 0 && si != s_cached) {
       const Desc& D = a.desc[si];
@@ -641,52 +714,42 @@ __device__ void phase_children(const KArgs& a) {
     if (valid) hint = k;
     int s = valid ? a.idsA[k] : -1;
     double lb = 0.0;
-    bool keep = false, sampled = false;
+    bool cand = false;
     unsigned long long code = 0;
     if (valid) {
       const Desc& D = a.desc[s];
-      State& st = a.st[s];
+      const State& st = a.st[s];
       const double* T = (s == si) ? s_tab : D.tab;
       code = (unsigned long long)(it - a.prefB[k]);
       ChildCtx C;
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
       lb = child_lb(D, T, C, code);
-      double ub = atomic_ub_read(&st.ub);
-      if (lb <= ub) {
-        int jb;
-        double sm = child_samp(D, T, C, code, &jb);
-        sampled = true;
-        if (sm == 0.0) sm = 0.0;  // -0 -> +0
-        if (sm < ord_val(st.ub_start)) {
-          long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
-          if (slot < D.ubc_cap) {
-            D.ubc_val[slot] = sm;
-            D.ubc_id[slot] = (code << 8) | (unsigned long long)jb;
-          }
-        }
-        if (sm < ub) {
-          atomicMin(&st.ub, ord_key(sm));
-          ub = atomic_ub_read(&st.ub);
-        }
-        if (lb <= ub) keep = !child_deriv(D, T, C, code);
-      }
+      cand = lb <= atomic_ub_read(&st.ub);
     }
-  // appends and sample counts, aggregated per warp and instance
-    unsigned int active = __ballot_sync(0xffffffffu, valid && (keep || sampled));
+    bool keep = false;
+    unsigned int cm = __ballot_sync(0xffffffffu, cand);
+    while (cm) {
+      int b = __ffs(cm) - 1;
+      cm &= cm - 1;
+      int cs = __shfl_sync(0xffffffffu, s, b);
+      unsigned long long ccode = __shfl_sync(0xffffffffu, code, b);
+      double clb = shfl_d(lb, b);
+      const double* T = (cs == si) ? s_tab : a.desc[cs].tab;
+      bool kk = warp_candidate(a, cs, T, ccode, clb);
+      if (lane == b) keep = kk;
+    }
+    // survivors appended, aggregated per warp and instance
+    unsigned int active = __ballot_sync(0xffffffffu, keep);
     while (active) {
       int leader = __ffs(active) - 1;
       int ls = __shfl_sync(0xffffffffu, s, leader);
-      unsigned int kmask = __ballot_sync(0xffffffffu, valid && s == ls && keep);
-      unsigned int smask = __ballot_sync(0xffffffffu, valid && s == ls && sampled);
+      unsigned int kmask = __ballot_sync(0xffffffffu, keep && s == ls);
       long long basepos = 0;
-      if (lane == leader) {
-        State& st = a.st[ls];
-        if (smask) atomicAdd((unsigned long long*)&st.samples, (unsigned long long)__popc(smask));
-        if (kmask) basepos = (long long)atomicAdd((unsigned long long*)&st.count, (unsigned long long)__popc(kmask));
-      }
+      if (lane == leader)
+        basepos = (long long)atomicAdd((unsigned long long*)&a.st[ls].count, (unsigned long long)__popc(kmask));
       basepos = __shfl_sync(0xffffffffu, basepos, leader);
-      if (valid && s == ls && keep) {
+      if (keep && s == ls) {
         const Desc& D = a.desc[s];
         State& st = a.st[s];
         long long pos = basepos + __popc(kmask & ((1u << lane) - 1u));
@@ -697,27 +760,25 @@ __device__ void phase_children(const KArgs& a) {
           atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
         }
       }
-      active &= ~(kmask | smask);
+      active &= ~kmask;
     }
-    __syncthreads();  // the shared tables may be replaced next round
+    // report the chunk; the block completing an instance queues it
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int kk = find_seg(a.prefB, nA, base, -1);
+      for (; kk < nA && a.prefB[kk] < hi; ++kk) {
+        long long seg_lo = max(base, a.prefB[kk]), seg_hi = min(hi, a.prefB[kk + 1]);
+        long long n_here = seg_hi - seg_lo;
+        if (n_here <= 0) continue;
+        int sx = a.idsA[kk];
+        State& st = a.st[sx];
+        __threadfence();
+        unsigned long long old = atomicAdd((unsigned long long*)&st.b_done, (unsigned long long)n_here);
+        if ((long long)old + n_here == st.m_children) queue_push(a, sx);
+      }
+    }
   }
-  // report this block's share of each instance; the block completing an instance queues it
-  __syncthreads();
   bstamp(a, 3);
-  if (threadIdx.x == 0 && lo < hi) {
-    int k = find_seg(a.prefB, nA, lo, -1);
-    for (; k < nA && a.prefB[k] < hi; ++k) {
-      long long seg_lo = max(lo, a.prefB[k]), seg_hi = min(hi, a.prefB[k + 1]);
-      long long n_here = seg_hi - seg_lo;
-      if (n_here <= 0) continue;
-      int s = a.idsA[k];
-      State& st = a.st[s];
-      __threadfence();
-      unsigned long long old = atomicAdd((unsigned long long*)&st.b_done, (unsigned long long)n_here);
-      if ((long long)old + n_here == st.m_children) queue_push(a, s);
-    }
-  }
-  __syncthreads();
   bstamp(a, 4);
   drain_queue(a);
   __syncthreads();

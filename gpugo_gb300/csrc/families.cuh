@@ -335,6 +335,10 @@ struct ChildCtx {
   int c0, gsz;
 };
 
+__device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned long long code, int i) {
+  return (long long)i * D.wid + digit(D, C.c0, C.gsz, code, i);
+}
+
 __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
@@ -343,7 +347,7 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
     case FAM_COSQUAD: {
       double s = 0.0;
       const double* tl = T + off[T_LO];
-      for (int i = 0; i < n; ++i) s = __dadd_rd(s, tl[i * w + digit(D, C.c0, C.gsz, code, i)]);
+      for (int i = 0; i < n; ++i) s = __dadd_rd(s, tl[eidx(D, C, code, i)]);
       return __dadd_rd(s, k[6 * n]);
     }
     case FAM_CHAINED: {
@@ -359,14 +363,8 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
     }
     case FAM_EXPSQRT: {
       iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        s = add(s, ldiv(T + off[T_SQ] + 2 * e));
-      }
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        c = add(c, ldiv(T + off[T_CS] + 2 * e));
-      }
+      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
+      for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
       iv inv_n = mk(k[2], k[3]);
       iv t = sqrt_iv(mul(s, inv_n));
       t = times(exp_iv(times(t, -k[1])), -k[0]);
@@ -375,14 +373,8 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
     }
     case FAM_PRODCOS: {
       iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        pr = mul(pr, ldiv(T + off[T_CR] + 2 * e));
-      }
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        s = add(s, ldiv(T + off[T_SQ4] + 2 * e));
-      }
+      for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
+      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ4] + 2 * eidx(D, C, code, i)));
       s = plus(mul(s, mk(k[0], k[1])), 1.0);
       return add(s, pr).lo;
     }
@@ -390,144 +382,149 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
   return 0.0;
 }
 
-// smallest sampled upper bound; *jbest receives its sample index
-__device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
-                                          int* jbest) {
+// upper bound of f at sample point j of the child (one pass of the sample code list)
+__device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long code, int j) {
   const int n = D.n, w = D.wid, S = D.S;
   const double* k = D.cst;
   const long long* off = D.t_off;
+  switch (D.family) {
+    case FAM_COSQUAD: {
+      double s = 0.0;
+      const double* th = T + off[T_SHI];
+      for (int i = 0; i < n; ++i) s = __dadd_ru(s, th[eidx(D, C, code, i) * S + j]);
+      return __dadd_ru(s, k[6 * n + 1]);
+    }
+    case FAM_CHAINED: {
+      double f = 0.0;
+      const double* th = T + off[T_SHI];
+      int dcur = digit(D, C.c0, C.gsz, code, 0);
+      for (int i = 0; i < n - 1; ++i) {
+        int dn = digit(D, C.c0, C.gsz, code, i + 1);
+        f = __dadd_ru(f, th[((long long)i * w * w + dcur * w + dn) * S + j]);
+        dcur = dn;
+      }
+      return f;
+    }
+    case FAM_EXPSQRT: {
+      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQS] + 2 * (eidx(D, C, code, i) * S + j)));
+      for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CSS] + 2 * (eidx(D, C, code, i) * S + j)));
+      iv inv_n = mk(k[2], k[3]);
+      iv t = sqrt_iv(mul(s, inv_n));
+      t = times(exp_iv(times(t, -k[1])), -k[0]);
+      iv u = exp_iv(mul(c, inv_n));
+      return add(minus(t, u), mk(k[4], k[5])).hi;
+    }
+    default: {  // FAM_PRODCOS
+      iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
+      for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CRS] + 2 * (eidx(D, C, code, i) * S + j)));
+      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQS4] + 2 * (eidx(D, C, code, i) * S + j)));
+      s = plus(mul(s, mk(k[0], k[1])), 1.0);
+      return add(s, pr).hi;
+    }
+  }
+}
+
+// The sample code list keeps the first sample with the smallest upper bound
+// (rastrigin50.py:289-297): minimum over (value, sample index).
+__device__ __forceinline__ bool samp_better(double v, int j, double bv, int bj) {
+  // NaN at j = 0 sticks (best > x is false for every x); later NaNs never win
+  if (bj == 0 && bv != bv) return false;
+  if (j == 0 && v != v) return true;
+  if (v != v) return false;
+  if (bv != bv) return true;
+  return (v < bv) || (v == bv && j < bj);
+}
+
+// smallest sampled upper bound; *jbest receives its sample index
+__device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                          int* jbest) {
   double best = 0.0;
   int jb = 0;
-  for (int j = 0; j < S; ++j) {
-    double fh;
-    switch (D.family) {
-      case FAM_COSQUAD: {
-        double s = 0.0;
-        const double* th = T + off[T_SHI];
-        for (int i = 0; i < n; ++i) s = __dadd_ru(s, th[((long long)i * w + digit(D, C.c0, C.gsz, code, i)) * S + j]);
-        fh = __dadd_ru(s, k[6 * n + 1]);
-        break;
-      }
-      case FAM_CHAINED: {
-        double f = 0.0;
-        const double* th = T + off[T_SHI];
-        int dcur = digit(D, C.c0, C.gsz, code, 0);
-        for (int i = 0; i < n - 1; ++i) {
-          int dn = digit(D, C.c0, C.gsz, code, i + 1);
-          f = __dadd_ru(f, th[((long long)i * w * w + dcur * w + dn) * S + j]);
-          dcur = dn;
-        }
-        fh = f;
-        break;
-      }
-      case FAM_EXPSQRT: {
-        iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-        for (int i = 0; i < n; ++i) {
-          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-          s = add(s, ldiv(T + off[T_SQS] + 2 * (e * S + j)));
-        }
-        for (int i = 0; i < n; ++i) {
-          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-          c = add(c, ldiv(T + off[T_CSS] + 2 * (e * S + j)));
-        }
-        iv inv_n = mk(k[2], k[3]);
-        iv t = sqrt_iv(mul(s, inv_n));
-        t = times(exp_iv(times(t, -k[1])), -k[0]);
-        iv u = exp_iv(mul(c, inv_n));
-        fh = add(minus(t, u), mk(k[4], k[5])).hi;
-        break;
-      }
-      default: {  // FAM_PRODCOS
-        iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
-        for (int i = 0; i < n; ++i) {
-          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-          pr = mul(pr, ldiv(T + off[T_CRS] + 2 * (e * S + j)));
-        }
-        for (int i = 0; i < n; ++i) {
-          long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-          s = add(s, ldiv(T + off[T_SQS4] + 2 * (e * S + j)));
-        }
-        s = plus(mul(s, mk(k[0], k[1])), 1.0);
-        fh = add(s, pr).hi;
-        break;
-      }
-    }
+  for (int j = 0; j < D.S; ++j) {
+    double fh = samp_one(D, T, C, code, j);
     if (j == 0 || best > fh) { best = fh; jb = j; }
   }
   *jbest = jb;
   return best;
 }
 
-// 1 when the generalized KKT test rules the child out
-__device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
+// Per-child scalars of the derivative code lists that do not depend on the
+// coordinate: expsqrt g = A B exp(-B r) / (n r) and u = exp(mean cos) (ackley50.py:413-455),
+// prodcos P = prod cos(x_i / sqrt(i)) (griewank50.py:383-396).  Returns 1 when the
+// test is skipped (expsqrt box containing the origin, ackley50.py:402-409).
+struct DerivPre {
+  iv g, u;
+};
+
+__device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                      DerivPre* P) {
+  const int n = D.n;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  if (D.family == FAM_EXPSQRT) {
+    const unsigned char* zb = (const unsigned char*)(T + off[T_ZB]);
+    int origin = 1;
+    for (int i = 0; i < n; ++i)
+      if (!zb[eidx(D, C, code, i)]) { origin = 0; break; }
+    if (origin) return 1;
+    iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+    for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
+    iv inv_n = mk(k[2], k[3]);
+    iv r = sqrt_iv(mul(s, inv_n));
+    iv g = exp_iv(times(r, -k[1]));
+    P->g = mul(div(g, r), mk(k[6], k[7]));
+    for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
+    P->u = exp_iv(mul(c, inv_n));
+  } else if (D.family == FAM_PRODCOS) {
+    iv pr = mk(1.0, 1.0);
+    for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
+    P->g = pr;
+  }
+  return 0;
+}
+
+// generalized KKT test of coordinate j (rastrigin50.py:365-370); 1 = rule out
+__device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                           int j, const DerivPre& P) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
   const long long* off = D.t_off;
   switch (D.family) {
-    case FAM_COSQUAD: {
-      const unsigned char* pr = (const unsigned char*)(T + off[T_PRB]);
-      for (int i = 0; i < n; ++i)
-        if (pr[i * w + digit(D, C.c0, C.gsz, code, i)]) return 1;
-      return 0;
-    }
+    case FAM_COSQUAD:
+      return ((const unsigned char*)(T + off[T_PRB]))[eidx(D, C, code, j)];
     case FAM_CHAINED: {
-      const unsigned char* pr = (const unsigned char*)(T + off[T_PRB]);
       const long long w2 = (long long)w * w, w3 = w2 * w;
-      int dm = 0, d = digit(D, C.c0, C.gsz, code, 0);
-      for (int j = 0; j < n; ++j) {
-        int dp = (j + 1 < n) ? digit(D, C.c0, C.gsz, code, j + 1) : 0;
-        if (pr[(long long)j * w3 + (long long)dm * w2 + (long long)d * w + dp]) return 1;
-        dm = d; d = dp;
-      }
-      return 0;
+      int dm = (j > 0) ? digit(D, C.c0, C.gsz, code, j - 1) : 0;
+      int d = digit(D, C.c0, C.gsz, code, j);
+      int dp = (j + 1 < n) ? digit(D, C.c0, C.gsz, code, j + 1) : 0;
+      return ((const unsigned char*)(T + off[T_PRB]))[(long long)j * w3 + (long long)dm * w2 + (long long)d * w + dp];
     }
     case FAM_EXPSQRT: {
-      const unsigned char* zb = (const unsigned char*)(T + off[T_ZB]);
-      int origin = 1;
-      for (int i = 0; i < n; ++i)
-        if (!zb[i * w + digit(D, C.c0, C.gsz, code, i)]) { origin = 0; break; }
-      if (origin) return 0;
-      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        s = add(s, ldiv(T + off[T_SQ] + 2 * e));
-      }
-      iv inv_n = mk(k[2], k[3]);
-      iv r = sqrt_iv(mul(s, inv_n));
-      iv g = exp_iv(times(r, -k[1]));
-      g = mul(div(g, r), mk(k[6], k[7]));
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        c = add(c, ldiv(T + off[T_CS] + 2 * e));
-      }
-      iv u = exp_iv(mul(c, inv_n));
-      for (int j = 0; j < n; ++j) {
-        long long e = (long long)j * w + digit(D, C.c0, C.gsz, code, j);
-        iv X = ldiv(T + off[T_XI] + 2 * e);
-        iv dd = mul(g, X);
-        iv h = mul(mul(ldiv(T + off[T_SN] + 2 * e), u), mk(k[8 + n + 2 * j], k[8 + n + 2 * j + 1]));
-        dd = add(dd, h);
-        if (kkt_prune(dd, X, D.dom[2 * j], D.dom[2 * j + 1])) return 1;
-      }
-      return 0;
+      long long e = eidx(D, C, code, j);
+      iv X = ldiv(T + off[T_XI] + 2 * e);
+      iv dd = mul(P.g, X);
+      iv h = mul(mul(ldiv(T + off[T_SN] + 2 * e), P.u), mk(k[8 + n + 2 * j], k[8 + n + 2 * j + 1]));
+      dd = add(dd, h);
+      return kkt_prune(dd, X, D.dom[2 * j], D.dom[2 * j + 1]);
     }
-    case FAM_PRODCOS: {
-      iv P = mk(1.0, 1.0);
-      for (int i = 0; i < n; ++i) {
-        long long e = (long long)i * w + digit(D, C.c0, C.gsz, code, i);
-        P = mul(P, ldiv(T + off[T_CR] + 2 * e));
-      }
-      for (int j = 0; j < n; ++j) {
-        long long e = (long long)j * w + digit(D, C.c0, C.gsz, code, j);
-        iv q = div(P, ldiv(T + off[T_CR] + 2 * e));
-        q = mul(mul(q, ldiv(T + off[T_SNA] + 2 * e)), mk(k[4 + 2 * j], k[4 + 2 * j + 1]));
-        q = add(q, ldiv(T + off[T_XD2] + 2 * e));
-        iv X = ldiv(T + off[T_XI4] + 2 * e);
-        if (kkt_prune(q, X, D.dom[2 * j], D.dom[2 * j + 1])) return 1;
-      }
-      return 0;
+    default: {  // FAM_PRODCOS
+      long long e = eidx(D, C, code, j);
+      iv q = div(P.g, ldiv(T + off[T_CR] + 2 * e));
+      q = mul(mul(q, ldiv(T + off[T_SNA] + 2 * e)), mk(k[4 + 2 * j], k[4 + 2 * j + 1]));
+      q = add(q, ldiv(T + off[T_XD2] + 2 * e));
+      iv X = ldiv(T + off[T_XI4] + 2 * e);
+      return kkt_prune(q, X, D.dom[2 * j], D.dom[2 * j + 1]);
     }
   }
+}
+
+// 1 when the generalized KKT test rules the child out
+__device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
+  DerivPre P;
+  if (deriv_pre(D, T, C, code, &P)) return 0;
+  for (int j = 0; j < D.n; ++j)
+    if (deriv_coord(D, T, C, code, j, P)) return 1;
   return 0;
 }
 
