@@ -72,7 +72,9 @@ struct State {
   long long samples;          // children whose samples were evaluated
   long long ubc_count;        // UB candidates recorded this iteration
   long long m_children;       // children of the current parent
-  long long b_done;           // children of this iteration already processed
+  long long b_done;           // (unused)
+  long long cand_total;       // candidates queued this iteration
+  long long cand_done;        // candidates processed this iteration
   int has_who;
   int pad;
 };
@@ -91,6 +93,9 @@ struct Ctl {
   int n_big_q;                // big list length (appended during the children phase)
   unsigned int epoch;         // iteration tag of the ready-queue entries
   unsigned long long chunk_next;  // children phase: next chunk to hand out
+  unsigned long long cand_tail;   // candidate queue: entries written in pass 1
+  unsigned long long cand_head;   // candidate queue: entries claimed in pass 2
+  long long cand_claim;           // entries claimed per atomic in pass 2
 };
 
 struct KArgs {
@@ -103,6 +108,8 @@ struct KArgs {
   int* idsE;                  // [max_slots] big-pool instances (grid-wide path)
   long long* prefD;           // [max_slots + 1] pool tiles prefix of big instances
   unsigned long long* queue;  // [max_slots] ready queue entries: epoch << 32 | slot
+  unsigned long long* cands;  // [cand_cap][2] candidate queue: slot << 32 | code, lb bits
+  long long cand_cap;
   int max_slots;
   long long max_iters;        // iterations in this launch (<= 0: until idle)
   unsigned long long timeout_ns;
@@ -255,6 +262,8 @@ __device__ void build_lists(const KArgs& a) {
     a.ctl->nBig = 0;
     a.ctl->epoch = a.ctl->epoch + 1;
     a.ctl->chunk_next = 0;
+    a.ctl->cand_tail = 0;
+    a.ctl->cand_head = 0;
   }
 }
 
@@ -495,6 +504,8 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     st.count_before = st.count;
     st.ubc_count = 0;
     st.b_done = 0;
+    st.cand_total = 0;
+    st.cand_done = 0;
     st.removed_new = 0;
   }
   __syncwarp();
@@ -670,52 +681,54 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   return !__any_sync(0xffffffffu, pruned);
 }
 
-__device__ void phase_children(const KArgs& a) {
+// Term tables of a single-instance iteration go to shared memory.
+__device__ int stage_tables(const KArgs& a) {
+  extern __shared__ double s_tab[];
+  if (a.ctl->nA != 1) return -1;
+  const int si = a.idsA[0];
+  const Desc& D = a.desc[si];
+  if (D.tab_doubles * 8 > SMEM_TAB_BYTES) return -1;
+  const double2* src = (const double2*)D.tab;
+  double2* dst = (double2*)s_tab;
+  const long long n2 = (D.tab_doubles + 1) / 2;
+  for (long long t = threadIdx.x; t < n2; t += blockDim.x) dst[t] = src[t];
+  __syncthreads();
+  return si;
+}
+
+__device__ __forceinline__ void append_survivor(const KArgs& a, int s, unsigned long long code, double lb) {
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  long long pos = (long long)atomicAdd((unsigned long long*)&st.count, 1ULL);
+  if (pos < D.pool_cap) {
+    D.pool_lb[st.cur][pos] = lb;
+    D.pool_key[st.cur][pos] = ((unsigned long long)st.iter << 32) | code;
+  } else {
+    atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
+  }
+}
+
+// Pass 1: every child's lower bound (uniform cost, static interleave over warps);
+// children whose LB is not above the UB go to the candidate queue.
+__device__ void phase_bound(const KArgs& a) {
   bstamp(a, 2);
   extern __shared__ double s_tab[];
-  __shared__ long long s_base;
-  __shared__ int s_inst, s_cached;
+  const int si = stage_tables(a);
   const long long tot = a.ctl->totB;
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
-  const long long CH = blockDim.x;
-  if (threadIdx.x == 0) s_cached = -1;
+  const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long w = ((long long)(threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
   int hint = -1;
-  for (;;) {
-    // chunks are handed out dynamically: candidate children cluster in code space
-    if (threadIdx.x == 0) {
-      long long base = (long long)atomicAdd(&a.ctl->chunk_next, 1ULL) * CH;
-      s_base = base;
-      s_inst = -1;
-      if (base < tot) {
-        long long last = min(tot, base + CH) - 1;
-        int k0 = find_seg(a.prefB, nA, base, -1);
-        int s0 = a.idsA[k0];
-        if (a.prefB[k0 + 1] > last && a.desc[s0].tab_doubles * 8 <= SMEM_TAB_BYTES) s_inst = s0;
-      }
-    }
-    __syncthreads();
-    const long long base = s_base;
-    if (base >= tot) break;
-    const long long hi = min(tot, base + CH);
-    const int si = s_inst;
-    if (si >= 0 && si != s_cached) {
-      const Desc& D = a.desc[si];
-      const double2* src = (const double2*)D.tab;
-      double2* dst = (double2*)s_tab;
-      const long long n2 = (D.tab_doubles + 1) / 2;
-      for (long long t = threadIdx.x; t < n2; t += blockDim.x) dst[t] = src[t];
-      __syncthreads();
-      if (threadIdx.x == 0) s_cached = si;
-    }
-    long long it = base + threadIdx.x;
-    bool valid = it < hi;
+  for (long long base = w * 32; base < tot; base += W * 32) {
+    long long it = base + lane;
+    bool valid = it < tot;
     int k = valid ? find_seg(a.prefB, nA, it, hint) : -1;
     if (valid) hint = k;
     int s = valid ? a.idsA[k] : -1;
     double lb = 0.0;
-    bool cand = false;
     unsigned long long code = 0;
+    bool cand = false;
     if (valid) {
       const Desc& D = a.desc[s];
       const State& st = a.st[s];
@@ -725,60 +738,108 @@ __device__ void phase_children(const KArgs& a) {
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
       lb = child_lb(D, T, C, code);
-      cand = lb <= atomic_ub_read(&st.ub);
+      cand = lb <= ord_val(st.ub_start);
     }
-    bool keep = false;
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
-    while (cm) {
-      int b = __ffs(cm) - 1;
-      cm &= cm - 1;
-      int cs = __shfl_sync(0xffffffffu, s, b);
-      unsigned long long ccode = __shfl_sync(0xffffffffu, code, b);
-      double clb = shfl_d(lb, b);
-      const double* T = (cs == si) ? s_tab : a.desc[cs].tab;
-      bool kk = warp_candidate(a, cs, T, ccode, clb);
-      if (lane == b) keep = kk;
-    }
-    // survivors appended, aggregated per warp and instance
-    unsigned int active = __ballot_sync(0xffffffffu, keep);
-    while (active) {
-      int leader = __ffs(active) - 1;
-      int ls = __shfl_sync(0xffffffffu, s, leader);
-      unsigned int kmask = __ballot_sync(0xffffffffu, keep && s == ls);
-      long long basepos = 0;
-      if (lane == leader)
-        basepos = (long long)atomicAdd((unsigned long long*)&a.st[ls].count, (unsigned long long)__popc(kmask));
-      basepos = __shfl_sync(0xffffffffu, basepos, leader);
-      if (keep && s == ls) {
-        const Desc& D = a.desc[s];
-        State& st = a.st[s];
-        long long pos = basepos + __popc(kmask & ((1u << lane) - 1u));
-        if (pos < D.pool_cap) {
-          D.pool_lb[st.cur][pos] = lb;
-          D.pool_key[st.cur][pos] = ((unsigned long long)st.iter << 32) | code;
-        } else {
-          atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
-        }
+    if (!cm) continue;
+    unsigned long long qb = 0;
+    if (lane == 0) qb = atomicAdd(&a.ctl->cand_tail, (unsigned long long)__popc(cm));
+    qb = __shfl_sync(0xffffffffu, qb, 0);
+    if (qb + __popc(cm) <= (unsigned long long)a.cand_cap) {
+      if (cand) {
+        unsigned long long pos = qb + __popc(cm & ((1u << lane) - 1u));
+        a.cands[2 * pos] = ((unsigned long long)s << 32) | code;
+        a.cands[2 * pos + 1] = (unsigned long long)__double_as_longlong(lb);
       }
-      active &= ~kmask;
-    }
-    // report the chunk; the block completing an instance queues it
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int kk = find_seg(a.prefB, nA, base, -1);
-      for (; kk < nA && a.prefB[kk] < hi; ++kk) {
-        long long seg_lo = max(base, a.prefB[kk]), seg_hi = min(hi, a.prefB[kk + 1]);
-        long long n_here = seg_hi - seg_lo;
-        if (n_here <= 0) continue;
-        int sx = a.idsA[kk];
-        State& st = a.st[sx];
-        __threadfence();
-        unsigned long long old = atomicAdd((unsigned long long*)&st.b_done, (unsigned long long)n_here);
-        if ((long long)old + n_here == st.m_children) queue_push(a, sx);
+      // per-instance queued counts
+      unsigned int act = cm;
+      while (act) {
+        int leader = __ffs(act) - 1;
+        int ls = __shfl_sync(0xffffffffu, s, leader);
+        unsigned int m = __ballot_sync(0xffffffffu, cand && s == ls);
+        if (lane == leader) atomicAdd((unsigned long long*)&a.st[ls].cand_total, (unsigned long long)__popc(m));
+        act &= ~m;
       }
+    } else {
+      // queue full: process these candidates right here
+      bool keep = false;
+      while (cm) {
+        int b = __ffs(cm) - 1;
+        cm &= cm - 1;
+        int cs = __shfl_sync(0xffffffffu, s, b);
+        unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
+        double cl = shfl_d(lb, b);
+        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl);
+        if (lane == b) keep = kk;
+      }
+      if (keep) append_survivor(a, s, code, lb);
     }
   }
+  __syncthreads();
   bstamp(a, 3);
+}
+
+// instances without queued candidates are ready for their list update at once
+__device__ void prefill_ready(const KArgs& a) {
+  const int nA = a.ctl->nA;
+  for (int k = threadIdx.x; k < nA; k += blockDim.x) {
+    int s = a.idsA[k];
+    if (a.st[s].cand_total == 0) queue_push(a, s);
+  }
+  if (threadIdx.x == 0) {
+    long long tot = (long long)a.ctl->cand_tail;
+    if (tot > a.cand_cap) tot = a.cand_cap;
+    long long W = ((long long)gridDim.x * blockDim.x) >> 5;
+    long long c = tot / (4 * W);
+    a.ctl->cand_claim = c < 1 ? 1 : (c > 16 ? 16 : c);
+    a.ctl->cand_tail = (unsigned long long)tot;
+  }
+}
+
+// Pass 2: candidates claimed dynamically by warps; the warp finishing an
+// instance's last candidate queues it for its list update.
+__device__ void phase_candidates(const KArgs& a) {
+  extern __shared__ double s_tab[];
+  const int si = stage_tables(a);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long tot = a.ctl->cand_tail;
+  const unsigned long long K = (unsigned long long)a.ctl->cand_claim;
+  for (;;) {
+    unsigned long long h = 0;
+    if (lane == 0) h = atomicAdd(&a.ctl->cand_head, K);
+    h = __shfl_sync(0xffffffffu, h, 0);
+    if (h >= tot) break;
+    const unsigned long long e = min(tot, h + K);
+    int acc_s = -1;
+    long long acc_n = 0;
+    for (unsigned long long q = h; q < e; ++q) {
+      unsigned long long w0 = a.cands[2 * q];
+      double lb = __longlong_as_double((long long)a.cands[2 * q + 1]);
+      int s = (int)(w0 >> 32);
+      unsigned long long code = w0 & 0xffffffffULL;
+      bool keep = warp_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb);
+      if (keep && lane == 0) append_survivor(a, s, code, lb);
+      if (lane == 0) {
+        if (s != acc_s && acc_s >= 0) {
+          __threadfence();
+          State& st = a.st[acc_s];
+          unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)acc_n);
+          if ((long long)old + acc_n == st.cand_total) queue_push(a, acc_s);
+          acc_n = 0;
+        }
+        acc_s = s;
+        acc_n++;
+      }
+    }
+    if (lane == 0 && acc_s >= 0) {
+      __threadfence();
+      State& st = a.st[acc_s];
+      unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)acc_n);
+      if ((long long)old + acc_n == st.cand_total) queue_push(a, acc_s);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
   bstamp(a, 4);
   drain_queue(a);
   __syncthreads();
@@ -880,6 +941,10 @@ struct TailLists {
   const KArgs* a;
   __device__ void operator()() const { build_lists(*a); }
 };
+struct TailPrefill {
+  const KArgs* a;
+  __device__ void operator()() const { prefill_ready(*a); }
+};
 struct TailAfterChildren {
   const KArgs* a;
   __device__ void operator()() const {
@@ -896,6 +961,7 @@ __device__ __forceinline__ void stamp(const KArgs& a, long long it, int k) {
 __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   TailLists tl{&a};
   TailAfterChildren tc{&a};
+  TailPrefill tp{&a};
   // queue entries of earlier launches carry stale epochs
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_slots; i += gridDim.x * blockDim.x) a.queue[i] = 0ULL;
   if (!grid_barrier(a, tl)) return;
@@ -906,8 +972,9 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
     phase_tables(a);
     if (!grid_barrier(a, NoTail{})) return;
     stamp(a, it, 1);
-    phase_children(a);
-    // queue slots are reset before the next iteration reuses them
+    phase_bound(a);
+    if (!grid_barrier(a, tp)) return;
+    phase_candidates(a);
     if (!grid_barrier(a, tc)) return;
     stamp(a, it, 2);
     if (a.ctl->nBig > 0) {
@@ -1042,6 +1109,8 @@ struct gpugo_engine {
   Ctl* d_ctl = nullptr;
   int* d_ids = nullptr;          // idsA | idsE | init list
   unsigned long long* d_queue = nullptr;
+  unsigned long long* d_cands = nullptr;
+  long long cand_cap = 0;
   long long* d_pref = nullptr;   // prefA | prefB | prefD
   char* d_arena = nullptr;
   Arena arena;
@@ -1467,6 +1536,8 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaMemset(E->d_ctl, 0, sizeof(Ctl))))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_ids, sizeof(int) * 3 * E->max_slots)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_queue, sizeof(unsigned long long) * E->max_slots)))) break;
+    E->cand_cap = 1LL << 22;
+    if ((rc = cuda_err(cudaMalloc(&E->d_cands, 16 * (size_t)E->cand_cap)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
@@ -1491,7 +1562,7 @@ int gpugo_engine_destroy(gpugo_engine* E) {
   if (!E) return GPUGO_OK;
   if (E->stream) cudaStreamSynchronize(E->stream);
   cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
-  cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps); cudaFree(E->d_bstamps);
+  cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_cands); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps); cudaFree(E->d_bstamps);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->stream) cudaStreamDestroy(E->stream);
@@ -1596,6 +1667,8 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.prefB = E->d_pref + (E->max_slots + 1);
   a.prefD = E->d_pref + 2 * (E->max_slots + 1);
   a.queue = E->d_queue;
+  a.cands = E->d_cands;
+  a.cand_cap = E->cand_cap;
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
