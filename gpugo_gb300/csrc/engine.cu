@@ -370,7 +370,7 @@ __device__ void phase_tables(const KArgs& a) {
     int s = a.idsA[k];
     const Desc& D = a.desc[s];
     const State& st = a.st[s];
-    build_item(D, D.parents + 2LL * D.n * st.iter, st.cyc, it - a.prefA[k]);
+    build_item(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k]);
   }
   __syncthreads();
   bstamp(a, 1);
@@ -447,7 +447,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
         ccyc = D.pcyc[prow];
         const double* pb = D.parents + 2LL * n * prow;
         int gsz = group_size(n, D.group, ccyc);
-        iv x0 = child_iv(D, pb, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
+        iv x0 = child_iv(D, pb, D.pwid + (long long)n * prow, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
         double width = __dsub_rn(x0.hi, x0.lo);
         if (width < D.width_tol && ccyc == D.max_cyc) {
           decision = 1;
@@ -471,12 +471,15 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     const long long prow = (long long)(key >> 32);
     const unsigned long long code = key & 0xffffffffULL;
     const double* pb = D.parents + 2LL * n * prow;
+    const double* pw = D.pwid + (long long)n * prow;
     double* nb = D.parents + 2LL * n * (st.iter + 1);
+    double* nw = D.pwid + (long long)n * (st.iter + 1);
     const int gsz = group_size(n, D.group, ccyc);
     for (int i = lane; i < n; i += 32) {
-      iv x = child_iv(D, pb, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
+      iv x = child_iv(D, pb, pw, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
       nb[2 * i] = x.lo;
       nb[2 * i + 1] = x.hi;
+      nw[i] = part_width(D, x.lo, x.hi);
     }
   }
   __syncwarp();
@@ -1006,7 +1009,7 @@ __global__ void eval_init_kernel(Desc* desc) {
 __global__ void eval_tables_kernel(Desc* desc, int cyc) {
   const Desc& D = desc[0];
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < D.a_items; t += (long long)gridDim.x * blockDim.x)
-    build_item(D, D.parents, cyc, t);
+    build_item(D, D.parents, D.pwid, cyc, t);
 }
 
 __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long long* codes, long long m, double ub,
@@ -1176,7 +1179,7 @@ struct Layout {
   int64_t pool_cap, parent_cap, tiles_cap, ubc_cap, out_cap, trace_cap;
   int64_t bytes;
   // byte offsets
-  int64_t o_dom, o_coef, o_cst, o_tab, o_par, o_pcyc, o_plb0, o_plb1, o_pk0, o_pk1, o_tile, o_ubcv, o_ubci,
+  int64_t o_dom, o_coef, o_cst, o_tab, o_par, o_pw, o_pcyc, o_plb0, o_plb1, o_pk0, o_pk1, o_tile, o_ubcv, o_ubci,
       o_outk, o_outl, o_trub, o_trs, o_trp, o_trsel;
 };
 
@@ -1201,7 +1204,7 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
   switch (s->family) {
     case GPUGO_COSQUAD:
       put(T_LO, n * w); put(T_SHI, n * w * S); put(T_PRB, (n * w + 7) / 8);
-      L->a_items = n * w * (S + 1);
+      L->a_items = n * w * (S + 2);
       break;
     case GPUGO_CHAINED:
       put(T_LO, (n - 1) * w * w); put(T_SHI, (n - 1) * w * w * S); put(T_PRB, (n * w * w * w + 7) / 8);
@@ -1234,6 +1237,7 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
   L->o_cst = take(8 * L->cst);
   L->o_tab = take(8 * L->tab);
   L->o_par = take(8 * 2 * n * L->parent_cap);
+  L->o_pw = take(8 * n * L->parent_cap);
   L->o_pcyc = take(4 * L->parent_cap);
   L->o_plb0 = take(8 * L->pool_cap);
   L->o_plb1 = take(8 * L->pool_cap);
@@ -1268,6 +1272,7 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->cst = (double*)(base + L.o_cst);
   D->tab = (double*)(base + L.o_tab);
   D->parents = (double*)(base + L.o_par);
+  D->pwid = (double*)(base + L.o_pw);
   D->pcyc = (int*)(base + L.o_pcyc);
   D->pool_lb[0] = (double*)(base + L.o_plb0);
   D->pool_lb[1] = (double*)(base + L.o_plb1);

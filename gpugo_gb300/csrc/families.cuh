@@ -53,6 +53,7 @@ struct Desc {
   double* cst;                       // derived constants
   double* tab;                       // tables
   double* parents;                   // [parent_cap][2n]
+  double* pwid;                      // [parent_cap][n] (hi - lo) / wid of each parent coordinate
   int* pcyc;                         // [parent_cap]
   double* pool_lb[2];
   unsigned long long* pool_key[2];
@@ -91,15 +92,21 @@ __device__ __forceinline__ int ndig(const Desc& D, int c0, int gsz, int i) {
   return (k >= 0 && k < gsz) ? D.wid : 1;
 }
 
-// child interval of coordinate i for digit d (ackley50.py:583-586, :903-906)
-__device__ __forceinline__ iv child_iv(const Desc& D, const double* pbox, int c0, int gsz, int i, int d) {
+// child interval of coordinate i for digit d (ackley50.py:583-586, :903-906);
+// pw holds the parent's (hi - lo) / wid per coordinate
+__device__ __forceinline__ iv child_iv(const Desc& D, const double* pbox, const double* pw, int c0, int gsz, int i,
+                                       int d) {
   double lo = pbox[2 * i], hi = pbox[2 * i + 1];
   int k = i - c0;
   if (k >= 0 && k < gsz) {
-    double w = __ddiv_rn(__dsub_rn(hi, lo), (double)D.wid);
+    double w = pw[i];
     return mk(__dadd_rn(__dmul_rn(w, (double)d), lo), __dadd_rn(__dmul_rn(w, (double)(d + 1)), lo));
   }
   return mk(lo, hi);
+}
+
+__device__ __forceinline__ double part_width(const Desc& D, double lo, double hi) {
+  return __ddiv_rn(__dsub_rn(hi, lo), (double)D.wid);
 }
 
 // sample point j of an interval (ackley50.py:288-290)
@@ -109,8 +116,8 @@ __device__ __forceinline__ double sample_pt(iv x, int S, int j) {
 }
 
 __device__ __forceinline__ int kkt_prune(iv d, iv x, double dlo, double dhi) {
-  if (d.lo > 0 && x.lo != dlo) return 1;
-  if (d.hi < 0 && x.hi != dhi) return 1;
+  if (fpos(d.lo) && !feq(x.lo, dlo)) return 1;
+  if (fneg(d.hi) && !feq(x.hi, dhi)) return 1;
   return 0;
 }
 
@@ -122,6 +129,7 @@ __device__ __forceinline__ void stiv(double* p, iv v) { p[0] = v.lo; p[1] = v.hi
 // ---------------------------------------------------------------------------
 __device__ void init_consts(const Desc& D) {
   const int n = D.n;
+  for (int i = 0; i < n; ++i) D.pwid[i] = part_width(D, D.parents[2 * i], D.parents[2 * i + 1]);
   const double* c = D.coef;
   double* k = D.cst;
   switch (D.family) {
@@ -212,7 +220,7 @@ __device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv
   return d;
 }
 
-__device__ void build_item(const Desc& D, const double* pbox, int cyc, long long t) {
+__device__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
   const int n = D.n, w = D.wid, S = D.S;
   const int c0 = cyc - 1, gsz = group_size(n, D.group, cyc);
   const double* k = D.cst;
@@ -220,16 +228,17 @@ __device__ void build_item(const Desc& D, const double* pbox, int cyc, long long
   const long long* off = D.t_off;
   switch (D.family) {
     case FAM_COSQUAD: {
-      int j = (int)(t % (S + 1));
-      long long r = t / (S + 1);
+      int j = (int)(t % (S + 2));
+      long long r = t / (S + 2);
       int d = (int)(r % w), i = (int)(r / w);
       if (d >= ndig(D, c0, gsz, i)) return;
-      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[i], a = k[2 * n + i], b = k[3 * n + i];
       long long e = (long long)i * w + d;
       if (j == S) {
         iv term = minus(times(sqr(X), a), times(cos_iv(times(X, K)), b));
         T[off[T_LO] + e] = term.lo;
+      } else if (j == S + 1) {
         iv g = add(times(X, k[n + i]), mul(sin_iv(times(X, K)), mk(k[4 * n + 2 * i], k[4 * n + 2 * i + 1])));
         ((unsigned char*)(T + off[T_PRB]))[e] = (unsigned char)kkt_prune(g, X, D.dom[2 * i], D.dom[2 * i + 1]);
       } else {
@@ -250,8 +259,8 @@ __device__ void build_item(const Desc& D, const double* pbox, int cyc, long long
         int d0 = (int)(r % w);
         int i = (int)(r / w);
         if (d0 >= ndig(D, c0, gsz, i) || d1 >= ndig(D, c0, gsz, i + 1)) return;
-        iv X = child_iv(D, pbox, c0, gsz, i, d0);
-        iv Y = child_iv(D, pbox, c0, gsz, i + 1, d1);
+        iv X = child_iv(D, pbox, pw, c0, gsz, i, d0);
+        iv Y = child_iv(D, pbox, pw, c0, gsz, i + 1, d1);
         if (j < S) {
           double x = sample_pt(X, S, j), y = sample_pt(Y, S, j);
           X = mk(x, x); Y = mk(y, y);
@@ -271,9 +280,9 @@ __device__ void build_item(const Desc& D, const double* pbox, int cyc, long long
         int nm = (j > 0) ? ndig(D, c0, gsz, j - 1) : 1;
         int np = (j + 1 < n) ? ndig(D, c0, gsz, j + 1) : 1;
         if (dm >= nm || d >= ndig(D, c0, gsz, j) || dp >= np) return;
-        iv X = child_iv(D, pbox, c0, gsz, j, d);
-        iv Xm = (j > 0) ? child_iv(D, pbox, c0, gsz, j - 1, dm) : X;
-        iv Xp = (j + 1 < n) ? child_iv(D, pbox, c0, gsz, j + 1, dp) : X;
+        iv X = child_iv(D, pbox, pw, c0, gsz, j, d);
+        iv Xm = (j > 0) ? child_iv(D, pbox, pw, c0, gsz, j - 1, dm) : X;
+        iv Xp = (j + 1 < n) ? child_iv(D, pbox, pw, c0, gsz, j + 1, dp) : X;
         iv g = chained_grad(D, j, Xm, X, Xp);
         ((unsigned char*)(T + off[T_PRB]))[(long long)j * w3 + e] =
             (unsigned char)kkt_prune(g, X, D.dom[2 * j], D.dom[2 * j + 1]);
@@ -285,7 +294,7 @@ __device__ void build_item(const Desc& D, const double* pbox, int cyc, long long
       long long r = t / (S + 1);
       int d = (int)(r % w), i = (int)(r / w);
       if (d >= ndig(D, c0, gsz, i)) return;
-      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[8 + i];
       long long e = (long long)i * w + d;
       if (j == S) {
@@ -307,7 +316,7 @@ __device__ void build_item(const Desc& D, const double* pbox, int cyc, long long
       long long r = t / (S + 1);
       int d = (int)(r % w), i = (int)(r / w);
       if (d >= ndig(D, c0, gsz, i)) return;
-      iv X = child_iv(D, pbox, c0, gsz, i, d);
+      iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
       long long e = (long long)i * w + d;
       if (j == S) {
@@ -429,11 +438,11 @@ __device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx
 // (rastrigin50.py:289-297): minimum over (value, sample index).
 __device__ __forceinline__ bool samp_better(double v, int j, double bv, int bj) {
   // NaN at j = 0 sticks (best > x is false for every x); later NaNs never win
-  if (bj == 0 && bv != bv) return false;
-  if (j == 0 && v != v) return true;
-  if (v != v) return false;
-  if (bv != bv) return true;
-  return (v < bv) || (v == bv && j < bj);
+  if (bj == 0 && isnan_(bv)) return false;
+  if (j == 0 && isnan_(v)) return true;
+  if (isnan_(v)) return false;
+  if (isnan_(bv)) return true;
+  return flt(v, bv) || (feq(v, bv) && j < bj);
 }
 
 // smallest sampled upper bound; *jbest receives its sample index
@@ -443,7 +452,7 @@ __device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildC
   int jb = 0;
   for (int j = 0; j < D.S; ++j) {
     double fh = samp_one(D, T, C, code, j);
-    if (j == 0 || best > fh) { best = fh; jb = j; }
+    if (j == 0 || flt(fh, best)) { best = fh; jb = j; }
   }
   *jbest = jb;
   return best;

@@ -34,17 +34,38 @@ __device__ __forceinline__ double u2d(uint64_t u) { return __longlong_as_double(
 constexpr uint64_t ABS_MASK = 0x7fffffffffffffffULL;
 constexpr uint64_t INF_BITS = 0x7ff0000000000000ULL;
 
-// Python min(a, b) / max(a, b): keep the first unless the second is strictly better.
-__device__ __forceinline__ double pmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double pmax(double a, double b) { return (b > a) ? b : a; }
+// Comparisons run on the integer bit patterns (an FP64 compare costs as much as
+// an FP64 add on this part); each one returns exactly what the IEEE comparison
+// returns, NaN and signed-zero cases included.
+__device__ __forceinline__ bool isnan_(double x) { return (d2u(x) & ABS_MASK) > INF_BITS; }
+__device__ __forceinline__ uint64_t cmpkey(double x) {
+  uint64_t u = d2u(x);
+  if ((u & ABS_MASK) == 0) u = 0;  // -0 == +0
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+// IEEE a < b
+__device__ __forceinline__ bool flt(double a, double b) {
+  if (isnan_(a) || isnan_(b)) return false;
+  return cmpkey(a) < cmpkey(b);
+}
+// IEEE a == b
+__device__ __forceinline__ bool feq(double a, double b) {
+  if (isnan_(a) || isnan_(b)) return false;
+  return cmpkey(a) == cmpkey(b);
+}
+// IEEE a < 0 and a > 0
+__device__ __forceinline__ bool fneg(double a) { uint64_t u = d2u(a); return (u >> 63) && (u & ABS_MASK) && !isnan_(a); }
+__device__ __forceinline__ bool fpos(double a) { uint64_t u = d2u(a); return !(u >> 63) && (u & ABS_MASK) && !isnan_(a); }
 
-__device__ __forceinline__ bool isnan_(double x) { return x != x; }
+// Python min(a, b) / max(a, b): keep the first unless the second is strictly better.
+__device__ __forceinline__ double pmin(double a, double b) { return flt(b, a) ? b : a; }
+__device__ __forceinline__ double pmax(double a, double b) { return flt(a, b) ? b : a; }
 
 // Lower bound moved down by k ulps (IA.py:263-281).
 __device__ __forceinline__ double bump_lo(double v, int k) {
   if (isnan_(v)) return v;
   uint64_t m = d2u(v) & ABS_MASK;
-  if (v < 0) {
+  if (fneg(v)) {
     if (m + (uint64_t)k >= INF_BITS) return -__longlong_as_double(0x7ff0000000000000LL);
     return -u2d(m + (uint64_t)k);
   }
@@ -56,7 +77,7 @@ __device__ __forceinline__ double bump_lo(double v, int k) {
 __device__ __forceinline__ double bump_hi(double v, int k) {
   if (isnan_(v)) return v;
   uint64_t m = d2u(v) & ABS_MASK;
-  if (v < 0) {
+  if (fneg(v)) {
     if (m < (uint64_t)k) return u2d((uint64_t)k);
     return -u2d(m - (uint64_t)k);
   }
@@ -85,8 +106,8 @@ __device__ __forceinline__ double gg_exp(double x) {
   const double LN2_HI = 0x1.62e42fee00000p-1;
   const double LN2_LO = 0x1.a39ef35793c76p-33;
   if (isnan_(x)) return x;
-  if (x > 709.79) return u2d(INF_BITS);
-  if (x < -745.2) return 0.0;
+  if (flt(709.79, x)) return u2d(INF_BITS);
+  if (flt(x, -745.2)) return 0.0;
   double k = rint(__dmul_rn(x, INV_LN2));
   double rh = __fma_rn(-k, LN2_HI, x);
   double th = __dmul_rn(k, LN2_LO);
@@ -125,7 +146,7 @@ __device__ __forceinline__ int trig_reduce(double x, double& rh, double& rl) {
   const double C2 = 0x1.1a62633145c07p-54;
   const double C3 = -0x1.f1976b7ed8fbcp-110;
   const double TWO_OVER_PI = 0x1.45f306dc9c883p-1;
-  if (!(fabs(x) <= 0x1p22)) return -1;
+  if (isnan_(x) || (d2u(x) & ABS_MASK) > d2u(0x1p22)) return -1;
   double k = rint(__dmul_rn(x, TWO_OVER_PI));
   double p1h = __dmul_rn(k, C1), p1l = __fma_rn(k, C1, -p1h);
   double p2h = __dmul_rn(k, C2), p2l = __fma_rn(k, C2, -p2h);
@@ -207,16 +228,18 @@ __device__ __forceinline__ iv entire() { return mk(-u2d(INF_BITS), u2d(INF_BITS)
 
 __device__ __forceinline__ iv div(iv a, iv b) {
   const double INF = u2d(INF_BITS);
-  if (b.lo < 0 && b.hi > 0) return entire();
-  if (b.lo == 0) {
-    if (b.hi == 0) return entire();
-    if (a.lo >= 0) return mk(__ddiv_rd(a.lo, b.hi), INF);
-    if (a.hi <= 0) return mk(-INF, __ddiv_ru(a.hi, b.hi));
+  const bool blz = feq(b.lo, 0.0), bhz = feq(b.hi, 0.0);
+  const bool alo_ge0 = !isnan_(a.lo) && !fneg(a.lo), ahi_le0 = !isnan_(a.hi) && !fpos(a.hi);
+  if (fneg(b.lo) && fpos(b.hi)) return entire();
+  if (blz) {
+    if (bhz) return entire();
+    if (alo_ge0) return mk(__ddiv_rd(a.lo, b.hi), INF);
+    if (ahi_le0) return mk(-INF, __ddiv_ru(a.hi, b.hi));
     return entire();
   }
-  if (b.hi == 0) {
-    if (a.lo >= 0) return mk(-INF, __ddiv_ru(a.lo, b.lo));
-    if (a.hi <= 0) return mk(__ddiv_rd(a.hi, b.lo), INF);
+  if (bhz) {
+    if (alo_ge0) return mk(-INF, __ddiv_ru(a.lo, b.lo));
+    if (ahi_le0) return mk(__ddiv_rd(a.hi, b.lo), INF);
     return entire();
   }
   return mul(a, mk(__drcp_rd(b.hi), __drcp_ru(b.lo)));
@@ -225,20 +248,20 @@ __device__ __forceinline__ iv div(iv a, iv b) {
 // power(., 2): x*x rounded to nearest, widened by 5 ulp
 __device__ __forceinline__ iv sqr(iv a) {
   double pl = __dmul_rn(a.lo, a.lo), ph = __dmul_rn(a.hi, a.hi);
-  if (a.lo < 0 && a.hi > 0) return mk(0.0, bump_hi(pmax(pl, ph), 5));
+  if (fneg(a.lo) && fpos(a.hi)) return mk(0.0, bump_hi(pmax(pl, ph), 5));
   return mk(bump_lo(pmin(pl, ph), 5), bump_hi(pmax(pl, ph), 5));
 }
 
 // power(., 1/2): correctly rounded sqrt, widened by 5 ulp; negative endpoints clamp to 0
 __device__ __forceinline__ iv sqrt_iv(iv a) {
-  double l = a.lo < 0 ? 0.0 : a.lo;
-  double h = a.hi < 0 ? 0.0 : a.hi;
+  double l = fneg(a.lo) ? 0.0 : a.lo;
+  double h = fneg(a.hi) ? 0.0 : a.hi;
   double pl = __dsqrt_rn(l), ph = __dsqrt_rn(h);
   return mk(bump_lo(pmin(pl, ph), 5), bump_hi(pmax(pl, ph), 5));
 }
 
 __device__ __forceinline__ iv times(iv a, double v) {
-  if (v < 0) return mk(__dmul_rd(a.hi, v), __dmul_ru(a.lo, v));
+  if (fneg(v)) return mk(__dmul_rd(a.hi, v), __dmul_ru(a.lo, v));
   return mk(__dmul_rd(a.lo, v), __dmul_ru(a.hi, v));
 }
 
@@ -246,11 +269,31 @@ __device__ __forceinline__ iv plus(iv a, double v) { return mk(__dadd_rd(a.lo, v
 
 __device__ __forceinline__ long long floordiv4(long long t) { return (t >= 0) ? t / 4 : -((-t + 3) / 4); }
 
+// floor(x / P) exactly for P > 0 and |x| <= 2^22 (IA.py:430-436 use Python's floor
+// division): the product with 1/P is within 2^-30 of x/P, so its floor is off by
+// at most one, and the sign of the exact remainder x - t P (one rounding of an
+// fma never changes a sign) settles it.
+__device__ __forceinline__ long long floor_div(double x, double P, double invP) {
+  double t = floor(__dmul_rn(x, invP));
+  double r0 = __fma_rn(-t, P, x);
+  if (fneg(r0)) {
+    t = __dsub_rn(t, 1.0);
+  } else {
+    double t1 = __dadd_rn(t, 1.0);
+    double r1 = __fma_rn(-t1, P, x);
+    if (!fneg(r1)) t = t1;
+  }
+  return (long long)t;
+}
+
 __device__ __forceinline__ void quarter_idx(iv a, long long& t1, long long& t2) {
-  const double P_UP = 0x1.921fb54442d1ap+0;  // 1.570796326794897 (above pi/2)
-  const double P_DN = 0x1.921fb54442d16p+0;  // 1.5707963267948961 (below pi/2)
-  t1 = (long long)floor(__ddiv_rd(a.lo, a.lo >= 0 ? P_UP : P_DN));
-  t2 = (long long)floor(__ddiv_rd(a.hi, a.hi >= 0 ? P_DN : P_UP));
+  const double P_UP = 0x1.921fb54442d1ap+0;   // 1.570796326794897 (above pi/2)
+  const double P_DN = 0x1.921fb54442d16p+0;   // 1.5707963267948961 (below pi/2)
+  const double I_UP = 0x1.45f306dc9c881p-1;   // RN(1/P_UP)
+  const double I_DN = 0x1.45f306dc9c884p-1;   // RN(1/P_DN)
+  const bool l0 = !fneg(a.lo), h0 = !fneg(a.hi);
+  t1 = floor_div(a.lo, l0 ? P_UP : P_DN, l0 ? I_UP : I_DN);
+  t2 = floor_div(a.hi, h0 ? P_DN : P_UP, h0 ? I_DN : I_UP);
 }
 
 __device__ __forceinline__ iv sin_iv(iv a) {
@@ -258,8 +301,8 @@ __device__ __forceinline__ iv sin_iv(iv a) {
   if (gg_sin(a.lo, s1) || gg_sin(a.hi, s2)) return mk(-1.0, 1.0);
   double lo = bump_lo(pmin(s1, s2), 5);
   double hi = bump_hi(pmax(s1, s2), 5);
-  if (lo < -1) lo = -1;
-  if (hi > 1) hi = 1;
+  if (flt(lo, -1.0)) lo = -1;
+  if (flt(1.0, hi)) hi = 1;
   long long t1, t2;
   quarter_idx(a, t1, t2);
   if (floordiv4(t1 + 1) != floordiv4(t2 + 1)) lo = -1;
@@ -272,8 +315,8 @@ __device__ __forceinline__ iv cos_iv(iv a) {
   if (gg_cos(a.lo, c1) || gg_cos(a.hi, c2)) return mk(-1.0, 1.0);
   double lo = bump_lo(pmin(c1, c2), 5);
   double hi = bump_hi(pmax(c1, c2), 5);
-  if (lo < -1) lo = -1;
-  if (hi > 1) hi = 1;
+  if (flt(lo, -1.0)) lo = -1;
+  if (flt(1.0, hi)) hi = 1;
   long long t1, t2;
   quarter_idx(a, t1, t2);
   if (floordiv4(t1 + 2) != floordiv4(t2 + 2)) lo = -1;
