@@ -16,6 +16,7 @@ ERRORS = {
     -4: "box pool capacity exceeded", -5: "parent table capacity exceeded",
     -6: "a bounded device wait expired", -7: "no free slot or pool memory",
     -8: "unknown ticket", -9: "no CUDA device",
+    -10: "request exceeds the fixed scratch of gpugo_eval_children_static",
 }
 CERTIFIED, FINISHED, ITER_LIMIT = 1, 2, 3
 ERR_BUSY = -7
@@ -69,7 +70,7 @@ class Done(ctypes.Structure):
 EXPORTS = [
     "gpugo_solve", "gpugo_eval_children", "gpugo_engine_create", "gpugo_engine_destroy", "gpugo_submit",
     "gpugo_run", "gpugo_poll", "gpugo_engine_free_bytes", "gpugo_instance_bytes", "gpugo_strerror",
-    "gpugo_device_info", "gpugo_engine_stats", "gpugo_fp64_peak",
+    "gpugo_device_info", "gpugo_engine_stats", "gpugo_fp64_peak", "gpugo_eval_children_static",
 ]
 
 _lib = None
@@ -102,6 +103,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                               ctypes.POINTER(Trace)]
     L.gpugo_eval_children.argtypes = [ctypes.POINTER(Spec), _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.c_int64, ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_int32)]
+    L.gpugo_eval_children_static.argtypes = L.gpugo_eval_children.argtypes
     L.gpugo_engine_create.argtypes = [ctypes.POINTER(EngineCfg), ctypes.POINTER(vp)]
     L.gpugo_engine_destroy.argtypes = [vp]
     L.gpugo_submit.argtypes = [vp, ctypes.POINTER(Spec), _dp, _dp, ctypes.c_int64, _dp, ctypes.POINTER(Trace), _i64p]

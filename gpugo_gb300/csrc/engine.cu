@@ -1445,6 +1445,7 @@ const char* gpugo_strerror(int code) {
     case GPUGO_ERR_BUSY: return "no free slot or pool memory";
     case GPUGO_ERR_NOT_FOUND: return "unknown ticket";
     case GPUGO_ERR_NO_DEVICE: return "no CUDA device";
+    case GPUGO_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch of gpugo_eval_children_static";
     case GPUGO_CERTIFIED: return "certified";
     case GPUGO_FINISHED: return "finished";
     case GPUGO_ITER_LIMIT: return "iteration limit";
@@ -1744,6 +1745,93 @@ int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_d
     h = HostSlot();
   }
   if (n_done_out) *n_done_out = k;
+  return GPUGO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// no-allocation variant of gpugo_eval_children
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+// The only working memory of gpugo_eval_children_static.  In host code this name
+// is a stand-in, not a device address: the address is looked up once per device.
+static __device__ __align__(256) unsigned char g_static_scratch[GPUGO_STATIC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_static_mu;
+constexpr int MAX_DEVICES = 64;
+void* g_static_ptr[MAX_DEVICES] = {};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+}  // namespace
+
+extern "C" {
+
+int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes,
+                               int64_t m, double ub, double* lb_out, double* samp_out, int32_t* flag_out) {
+  int rc = validate(spec);
+  if (rc) return rc;
+  if (!parent_box || (m > 0 && (!codes || !lb_out || !samp_out || !flag_out)) || m < 0 || cyc < 1 || cyc > spec->n)
+    return GPUGO_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
+  const int64_t M = children_host(spec, cyc);
+  for (int64_t t = 0; t < m; ++t) if ((int64_t)codes[t] >= M) return GPUGO_ERR_INVALID;
+  gpugo_spec s2 = *spec;
+  s2.pool_cap = 1;
+  s2.parent_cap = 1;
+  Layout L;
+  layout(&s2, 1, 0, &L);
+  // scratch layout: descriptor | instance region | codes | lb | samp | flag
+  const size_t o_desc = 0;
+  const size_t o_inst = align256(sizeof(Desc));
+  const size_t o_codes = o_inst + align256((size_t)L.bytes);
+  const size_t o_lb = o_codes + align256(8 * (size_t)m);
+  const size_t o_samp = o_lb + align256(8 * (size_t)m);
+  const size_t o_flag = o_samp + align256(8 * (size_t)m);
+  const size_t total = o_flag + align256(4 * (size_t)m);
+  if (total > GPUGO_STATIC_SCRATCH_BYTES) return GPUGO_ERR_SCRATCH_LIMIT;
+
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) return GPUGO_ERR_INVALID;
+  if (!g_static_ptr[dev]) {
+    // set-up, once per device, with that device current
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) return cuda_err(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
+    g_static_ptr[dev] = p;
+  }
+  char* base = (char*)g_static_ptr[dev];
+  Desc* d_desc = (Desc*)(base + o_desc);
+  unsigned long long* d_codes = (unsigned long long*)(base + o_codes);
+  double* d_lb = (double*)(base + o_lb);
+  double* d_samp = (double*)(base + o_samp);
+  int* d_flag = (int*)(base + o_flag);
+  Desc D;
+  fill_desc(&s2, L, base + o_inst, &D);
+  CK(cudaMemcpy((void*)D.dom, spec->domain, 8 * 2 * spec->n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((void*)D.coef, spec->coef, 8 * spec->ncoef, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(D.parents, parent_box, 8 * 2 * spec->n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_desc, &D, sizeof(Desc), cudaMemcpyHostToDevice));
+  if (m > 0) CK(cudaMemcpy(d_codes, codes, 8 * m, cudaMemcpyHostToDevice));
+  eval_init_kernel<<<1, 32>>>(d_desc);
+  CK(cudaGetLastError());
+  const int blocks = (int)std::min<int64_t>((L.a_items + 255) / 256, 4096);
+  eval_tables_kernel<<<std::max(blocks, 1), 256>>>(d_desc, cyc);
+  CK(cudaGetLastError());
+  if (m > 0) {
+    const int b2 = (int)std::min<int64_t>((m + 255) / 256, 4096);
+    eval_children_kernel<<<b2, 256>>>(d_desc, cyc, d_codes, m, ub, d_lb, d_samp, d_flag);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(0));
+  if (m > 0) {
+    CK(cudaMemcpy(lb_out, d_lb, 8 * m, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(samp_out, d_samp, 8 * m, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(flag_out, d_flag, 4 * m, cudaMemcpyDeviceToHost));
+  }
   return GPUGO_OK;
 }
 

@@ -35,6 +35,7 @@ extern "C" {
 #define GPUGO_ERR_BUSY            -7   /* no free slot or pool memory: retry after a run */
 #define GPUGO_ERR_NOT_FOUND       -8   /* unknown ticket */
 #define GPUGO_ERR_NO_DEVICE       -9   /* no CUDA device */
+#define GPUGO_ERR_SCRATCH_LIMIT  -10   /* request larger than the fixed scratch of gpugo_eval_children_static */
 
 /* per-instance outcome (gpugo_result.status) */
 #define GPUGO_CERTIFIED   1   /* UB - LB <= gap_tol (gap mode) */
@@ -121,6 +122,35 @@ int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, do
 int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_t cyc,
                         const uint64_t* codes, int64_t m, double ub,
                         double* lb_out, double* samp_out, int32_t* flag_out);
+
+/*
+ * gpugo_eval_children_static: the same pass as gpugo_eval_children, for callers
+ * that must not allocate device memory.  No counterpart in the reference.
+ *
+ * Some hosts own all of the GPU's memory themselves: an application that reserves
+ * the device heap at start-up and hands out pieces of it, a plugin running inside
+ * such a process, or a real-time loop that cannot afford cudaMalloc/cudaFree
+ * (both may synchronise the whole device and may fail late under memory
+ * pressure).  This entry point calls no allocator: its working memory (problem
+ * descriptor, derived constants, term tables, child codes and result staging) is
+ * one fixed array of GPUGO_STATIC_SCRATCH_BYTES in the library's own device
+ * memory, loaded with the library on every GPU that uses it and kept until the
+ * process exits.  Inputs and outputs are host buffers, as for gpugo_eval_children.
+ *
+ * Limit: a request whose term tables plus 28 bytes per child code exceed the
+ * scratch returns GPUGO_ERR_SCRATCH_LIMIT (the 8-variable chained instance with
+ * wid = 4 fits about 290 000 child codes per call).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current; make
+ * it before any stream capture.  The array is shared by all calls and keeps the
+ * last call's contents; nothing in it has to start at zero because every value a
+ * call reads is written earlier in the same call.  Calls are serialised by a host
+ * lock inside the library; two calls running on the GPU at the same time (for
+ * example from two loaded copies of the library) would race on the array.
+ */
+#define GPUGO_STATIC_SCRATCH_BYTES (8u << 20)
+int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box, int32_t cyc,
+                               const uint64_t* codes, int64_t m, double ub,
+                               double* lb_out, double* samp_out, int32_t* flag_out);
 
 /* ---------------------------------------------------------------------------
  * Engines: many solves share one persistent kernel (batching and serving).
