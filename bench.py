@@ -283,6 +283,73 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_batched(args):
+    """Config 4: a mixed batch solved by one engine vs the same problems solved
+    one per launch (gpugo_solve in a loop); results must be identical."""
+    import gpugo_gb300 as G
+    from gpugo_gb300 import problems as P
+    probs = P.config4(count=args.count)
+    for p in probs[:8]:
+        G.solve(p, box_cap=4)                      # warm-up
+    t0 = time.perf_counter()
+    plain = [G.solve(p, box_cap=4) for p in probs]
+    t_plain = time.perf_counter() - t0
+    dev_plain = sum(r.device_ms for r in plain) * 1e-3
+    with G.Engine(max_slots=args.count, arena_bytes=args.arena_gb << 30) as eng:
+        eng.solve_all(probs[:8], box_cap=4)        # warm-up
+        st0 = eng.stats()
+        t0 = time.perf_counter()
+        res = eng.solve_all(probs, box_cap=4)
+        t_b = time.perf_counter() - t0
+        st1 = eng.stats()
+    same = all((a.lb, a.ub, a.iterations, a.status) == (b.lb, b.ub, b.iterations, b.status)
+               for a, b in zip(plain, res))
+    boxes = sum(r.boxes_bounded for r in res)
+    return {"metric": "boxes/s", "value": boxes / t_b, "unit": "boxes/s", "n_gpus": 1, "dtype": "f64",
+            "higher_is_better": True, "data": "synthetic (config 4 generator, MASTER_SEED+4)",
+            "config": {"workload": f"cfg4-batch{args.count}: families F1-F4, n log-uniform 2..64, UB-LB<=1e-6",
+                       "certified": sum(r.certified for r in res), "boxes": boxes,
+                       "max_iterations": max(r.iterations for r in res)},
+            "batched_wall_s": t_b, "batched_device_s": (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
+            "batched_launches": st1["kernel_launches"] - st0["kernel_launches"],
+            "plain_wall_s": t_plain, "plain_device_s": dev_plain, "plain_launches": 2 * len(probs),
+            "speedup_vs_plain": t_plain / t_b, "identical_to_plain": same}
+
+
+def run_serving(args):
+    """Config 5: Poisson stream of requests, continuous batching, p50/p99."""
+    from gpugo_gb300 import problems as P
+    from gpugo_gb300.serve import serve
+    stream = P.config5(count=args.count, rate=args.rate)
+    rep = serve(stream, max_slots=min(args.count, 2048), arena_bytes=args.arena_gb << 30,
+                slice_iters=args.slice)
+    sm = rep.summary()
+    return {"metric": "time-to-certified p50/p99 (ms) and boxes/s", "value": sm["boxes_per_s"], "unit": "boxes/s",
+            "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"], "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic (config 5 generator, MASTER_SEED+5)",
+            "config": {"workload": f"cfg5-serve{args.count}: Poisson {args.rate}/s, F1-F4, n log-uniform 2..128, "
+                                   f"tol 1e-6 or 1e-4, pool arena {args.arena_gb} GiB",
+                       "slice_iters": args.slice},
+            **{k: v for k, v in sm.items() if k not in ("p50_ms", "p99_ms")}}
+
+
+def run_single(args):
+    import gpugo_gb300 as G
+    from gpugo_gb300 import problems as P
+    p = {"cfg1": P.config1, "cfg3": lambda: P.config3(split=(3, 8))}[args.workload]()
+    for _ in range(args.warmup):
+        G.solve(p, box_cap=4)
+    dev, boxes = 0.0, 0
+    for _ in range(args.steps):
+        r = G.solve(p, box_cap=4)
+        dev += r.device_ms
+        boxes += r.boxes_bounded
+    return {"metric": "boxes/s", "value": boxes / (dev * 1e-3), "unit": "boxes/s", "n_gpus": 1, "dtype": "f64",
+            "steps": args.steps, "ms_per_step": dev / args.steps,
+            "config": {"workload": p.tag, "n": p.n, "split": [p.wid, p.group], "iterations": r.iterations,
+                       "boxes_per_solve": r.boxes_bounded, "enclosure": [r.lb, r.ub], "certified": r.certified}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -290,9 +357,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpugo", choices=["gpugo", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"],
+                    help="cfg2 is the benchmark line; the others print their own records")
+    ap.add_argument("--count", type=int, default=1024)
+    ap.add_argument("--rate", type=float, default=20000.0)
+    ap.add_argument("--slice", type=int, default=16)
+    ap.add_argument("--arena-gb", type=int, default=80)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
+    if args.workload != "cfg2" and args.impl == "gpugo":
+        fn = {"cfg1": run_single, "cfg3": run_single, "cfg4": run_batched, "cfg5": run_serving}[args.workload]
+        print(json.dumps(fn(args)))
+        return
     if args.impl == "reference":
         out = run_reference(args)
         if out is not None:

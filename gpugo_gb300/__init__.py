@@ -202,6 +202,14 @@ class Engine:
             out.append((t, _result(p, arr[i].result, boxes, lbs, xhat, arrs)))
         return out
 
+    def stats(self) -> dict:
+        """Engine counters: device time of the runs, kernel launches, iterations, copies."""
+        st = _lib.Stats()
+        _lib.check(self._L.gpugo_engine_stats(self._h, ctypes.byref(st)), "gpugo_engine_stats")
+        return {"last_run_ms": st.last_run_ms, "total_run_ms": st.total_run_ms,
+                "kernel_launches": st.kernel_launches, "iterations": st.iterations,
+                "h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes}
+
     def free_bytes(self) -> int:
         out = ctypes.c_int64()
         _lib.check(self._L.gpugo_engine_free_bytes(self._h, ctypes.byref(out)), "gpugo_engine_free_bytes")

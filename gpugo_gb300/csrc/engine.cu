@@ -1223,8 +1223,8 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
   }
   L->tab = o;
   const int64_t M = max_children(s);
-  L->pool_cap = s->pool_cap > 0 ? s->pool_cap : std::max<int64_t>(1 << 18, std::min<int64_t>(16 * M, 1 << 26));
-  L->parent_cap = s->parent_cap > 0 ? s->parent_cap : 8192;
+  L->pool_cap = s->pool_cap > 0 ? s->pool_cap : std::max<int64_t>(1 << 19, std::min<int64_t>(16 * M, 1 << 26));
+  L->parent_cap = s->parent_cap > 0 ? s->parent_cap : 2048;
   if (s->max_iter > 0) L->parent_cap = std::min<int64_t>(L->parent_cap, s->max_iter + 1);
   L->tiles_cap = (L->pool_cap + TD - 1) / TD;
   L->ubc_cap = 4096;

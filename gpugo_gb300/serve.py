@@ -1,0 +1,114 @@
+"""Continuous-batching request loop over one GPU.
+
+Solve requests arrive over time (a Poisson stream in the benchmark).  A request
+is admitted into the resident engine as soon as a slot and enough box-pool memory
+are free (``Engine.submit`` refuses otherwise); every resident solve keeps its
+list and UB on the device and advances inside the same persistent kernel; the
+kernel returns every ``slice_iters`` iterations so that finished solves are
+collected and waiting requests join the running batch.
+
+The reference has no serving mode: each script solves one problem
+(GPUGO_1.1/1-Ackley/ackley50.py:950-1396).
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import Engine, SolveResult, _lib
+from .problems import Problem
+
+
+@dataclass
+class RequestRecord:
+    index: int
+    arrival: float                 # seconds after the start of the run
+    admitted: float = -1.0
+    finished: float = -1.0
+    result: SolveResult | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+@dataclass
+class ServeReport:
+    records: list[RequestRecord]
+    wall_s: float
+    device_s: float
+    launches: int
+    engine_iterations: int
+    boxes: int = 0
+    certified: int = 0
+    p50_ms: float = 0.0
+    p99_ms: float = 0.0
+    extra: dict = field(default_factory=dict)
+
+    def summary(self) -> dict:
+        return {"requests": len(self.records), "certified": self.certified, "wall_s": self.wall_s,
+                "device_s": self.device_s, "boxes": self.boxes, "boxes_per_s": self.boxes / self.wall_s,
+                "p50_ms": self.p50_ms, "p99_ms": self.p99_ms, "kernel_launches": self.launches,
+                "engine_iterations": self.engine_iterations, **self.extra}
+
+
+def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_bytes: int = 80 << 30,
+          slice_iters: int = 16, box_cap: int = 4, engine: Engine | None = None,
+          clock=time.perf_counter) -> ServeReport:
+    """Run ``stream`` (pairs of arrival time in seconds and problem, sorted by
+    arrival) through one engine; returns per-request latencies and results."""
+    own = engine is None
+    eng = engine or Engine(max_slots=max_slots, arena_bytes=arena_bytes)
+    records = [RequestRecord(i, float(t)) for i, (t, _) in enumerate(stream)]
+    pending: deque[int] = deque()
+    nxt = 0
+    tickets: dict[int, int] = {}
+    st0 = eng.stats()
+    t0 = clock()
+    done = 0
+    while done < len(records):
+        now = clock() - t0
+        while nxt < len(records) and stream[nxt][0] <= now:
+            pending.append(nxt)
+            nxt += 1
+        # admit in arrival order while slots and pool memory last
+        while pending:
+            i = pending[0]
+            t = eng.submit(stream[i][1], box_cap=box_cap)
+            if t is None:
+                if not tickets:
+                    raise _lib.GpugoError(-7, f"request {i} does not fit an empty engine")
+                break
+            pending.popleft()
+            tickets[t] = i
+            records[i].admitted = clock() - t0
+        if not tickets:
+            # idle until the next arrival
+            if nxt < len(records):
+                wait = stream[nxt][0] - (clock() - t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.001))
+            continue
+        eng.run(slice_iters)
+        fin = clock() - t0
+        for t, r in eng.poll():
+            i = tickets.pop(t)
+            records[i].finished = fin
+            records[i].result = r
+            done += 1
+    wall = clock() - t0
+    st1 = eng.stats()
+    if own:
+        eng.close()
+    lat = np.array([r.latency for r in records]) * 1e3
+    rep = ServeReport(records, wall, (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
+                      int(st1["kernel_launches"] - st0["kernel_launches"]),
+                      int(st1["iterations"] - st0["iterations"]))
+    rep.boxes = sum(r.result.boxes_bounded for r in records)
+    rep.certified = sum(r.result.certified for r in records)
+    rep.p50_ms = float(np.percentile(lat, 50))
+    rep.p99_ms = float(np.percentile(lat, 99))
+    return rep

@@ -1,0 +1,69 @@
+"""Host logic of the serving loop against a fake engine (no GPU): arrival
+ordering, admission only while slots are free, collection, latency accounting."""
+from types import SimpleNamespace
+
+from gpugo_gb300 import problems as P
+from gpugo_gb300.serve import serve
+
+
+class FakeEngine:
+    """A solve needs `iters` runs of one slice; at most `slots` are resident."""
+
+    def __init__(self, slots, iters):
+        self.slots, self.iters = slots, iters
+        self.resident = {}
+        self.next = 1
+        self.runs = 0
+        self.max_resident = 0
+        self.admit_order = []
+
+    def submit(self, p, box_cap=4):
+        if len(self.resident) >= self.slots:
+            return None
+        t = self.next
+        self.next += 1
+        self.resident[t] = [self.iters, p]
+        self.admit_order.append(p.tag)
+        self.max_resident = max(self.max_resident, len(self.resident))
+        return t
+
+    def run(self, k):
+        self.runs += 1
+        for v in self.resident.values():
+            v[0] -= 1
+        return sum(v[0] > 0 for v in self.resident.values())
+
+    def poll(self):
+        out = []
+        for t in [t for t, v in self.resident.items() if v[0] <= 0]:
+            p = self.resident.pop(t)[1]
+            out.append((t, SimpleNamespace(boxes_bounded=10, certified=True, tag=p.tag)))
+        return out
+
+    def stats(self):
+        return {"total_run_ms": float(self.runs), "kernel_launches": self.runs, "iterations": self.runs}
+
+    def close(self):
+        pass
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        self.t += 0.001
+        return self.t
+
+
+def test_admission_respects_slots_and_arrival_order():
+    stream = [(0.0005 * i, P.instance(P.COSQUAD, 2, i, tag=f"q{i}")) for i in range(20)]
+    eng = FakeEngine(slots=3, iters=2)
+    rep = serve(stream, engine=eng, clock=FakeClock())
+    assert eng.max_resident == 3
+    assert eng.admit_order == [f"q{i}" for i in range(20)]
+    assert rep.certified == 20 and rep.boxes == 200
+    for r in rep.records:
+        assert r.admitted >= r.arrival and r.finished > r.admitted
+        assert r.result.tag == f"q{r.index}"
+    assert rep.p99_ms >= rep.p50_ms > 0
