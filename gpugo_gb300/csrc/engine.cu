@@ -50,6 +50,10 @@ enum { ST_FREE = 0, ST_EXPAND = 1, ST_REPOP = 2, ST_DONE = 3 };
 // after the instance's children are done; larger pools take the grid-wide path.
 constexpr long long POOL_BLOCK_MAX = 1LL << 12;
 
+// Candidate queue entry: slot << 32 | child code, LB bits, six intermediates of the
+// value code list reused by the derivative test.
+constexpr int CAND_WORDS = 8;
+
 // Shared memory per block holding one instance's term tables during phase B.
 constexpr int SMEM_TAB_BYTES = 96 * 1024;
 
@@ -632,7 +636,8 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 // One candidate child (its LB is not above the running UB) processed by the whole
 // warp: its sample points spread over the lanes, then its KKT coordinates.
 // Returns true when the child survives.  Every lane returns the same value.
-__device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb) {
+__device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
+                               const double* aux = nullptr) {
   const int lane = threadIdx.x & 31;
   const Desc& D = a.desc[s];
   State& st = a.st[s];
@@ -673,7 +678,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   DerivPre P;
   int skip = 0;
   if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS) {
-    if (lane == 0) skip = deriv_pre(D, T, C, code, &P);
+    if (lane == 0) skip = aux ? deriv_pre_aux(D, T, C, code, aux, &P) : deriv_pre(D, T, C, code, &P);
     skip = __shfl_sync(0xffffffffu, skip, 0);
     P.g.lo = shfl_d(P.g.lo, 0); P.g.hi = shfl_d(P.g.hi, 0);
     P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
@@ -682,6 +687,45 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   if (!skip)
     for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, code, j, P);
   return !__any_sync(0xffffffffu, pruned);
+}
+
+// One candidate processed by one thread (long queues): the samples run one after
+// the other and every sample value below the running UB lowers it (the minimum
+// over all of them is the same value the per-child minimum would give).
+// returns bit 0: the child survives, bit 1: its samples were evaluated
+__device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
+                                const double* aux) {
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  ChildCtx C;
+  C.c0 = st.cyc - 1;
+  C.gsz = group_size(D.n, D.group, st.cyc);
+  double ub = atomic_ub_read(&st.ub);
+  if (flt(ub, lb)) return 0;
+  const double ub0 = ord_val(st.ub_start);
+  for (int j = 0; j < D.S; ++j) {
+    double v = samp_one(D, T, C, code, j);
+    if (feq(v, 0.0)) v = 0.0;
+    if (flt(v, ub0)) {
+      long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+      if (slot < D.ubc_cap) {
+        D.ubc_val[slot] = v;
+        D.ubc_id[slot] = (code << 8) | (unsigned long long)j;
+      }
+    }
+    if (flt(v, ub)) {
+      atomicMin(&st.ub, ord_key(v));
+      ub = v;
+    }
+  }
+  ub = atomic_ub_read(&st.ub);
+  if (flt(ub, lb)) return 2;
+  DerivPre P;
+  if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS)
+    if (deriv_pre_aux(D, T, C, code, aux, &P)) return 3;
+  for (int j = 0; j < D.n; ++j)
+    if (deriv_coord(D, T, C, code, j, P)) return 2;
+  return 3;
 }
 
 // Term tables of a single-instance iteration go to shared memory.
@@ -730,6 +774,7 @@ __device__ void phase_bound(const KArgs& a) {
     if (valid) hint = k;
     int s = valid ? a.idsA[k] : -1;
     double lb = 0.0;
+    double aux[6] = {0, 0, 0, 0, 0, 0};
     unsigned long long code = 0;
     bool cand = false;
     if (valid) {
@@ -740,8 +785,8 @@ __device__ void phase_bound(const KArgs& a) {
       ChildCtx C;
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
-      lb = child_lb(D, T, C, code);
-      cand = lb <= ord_val(st.ub_start);
+      lb = child_lb(D, T, C, code, aux);
+      cand = !flt(ord_val(st.ub_start), lb);
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
     if (!cm) continue;
@@ -751,8 +796,11 @@ __device__ void phase_bound(const KArgs& a) {
     if (qb + __popc(cm) <= (unsigned long long)a.cand_cap) {
       if (cand) {
         unsigned long long pos = qb + __popc(cm & ((1u << lane) - 1u));
-        a.cands[2 * pos] = ((unsigned long long)s << 32) | code;
-        a.cands[2 * pos + 1] = (unsigned long long)__double_as_longlong(lb);
+        unsigned long long* e = a.cands + CAND_WORDS * pos;
+        e[0] = ((unsigned long long)s << 32) | code;
+        e[1] = (unsigned long long)__double_as_longlong(lb);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) e[2 + q] = (unsigned long long)__double_as_longlong(aux[q]);
       }
       // per-instance queued counts
       unsigned int act = cm;
@@ -772,7 +820,10 @@ __device__ void phase_bound(const KArgs& a) {
         int cs = __shfl_sync(0xffffffffu, s, b);
         unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
         double cl = shfl_d(lb, b);
-        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl);
+        double ca[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) ca[q] = shfl_d(aux[q], b);
+        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca);
         if (lane == b) keep = kk;
       }
       if (keep) append_survivor(a, s, code, lb);
@@ -793,14 +844,25 @@ __device__ void prefill_ready(const KArgs& a) {
     long long tot = (long long)a.ctl->cand_tail;
     if (tot > a.cand_cap) tot = a.cand_cap;
     long long W = ((long long)gridDim.x * blockDim.x) >> 5;
-    long long c = tot / (4 * W);
-    a.ctl->cand_claim = c < 1 ? 1 : (c > 16 ? 16 : c);
+    long long c = tot / (2 * W);
+    // a warp per candidate while there are fewer candidates than warps x 32;
+    // beyond that each lane takes its own candidate, 32 or 64 per claim
+    a.ctl->cand_claim = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 8 ? 8 : c));
     a.ctl->cand_tail = (unsigned long long)tot;
   }
 }
 
 // Pass 2: candidates claimed dynamically by warps; the warp finishing an
-// instance's last candidate queues it for its list update.
+// instance's last candidate queues it for its list update.  Short queues give a
+// whole warp to each candidate (samples and KKT coordinates across the lanes);
+// long queues give each lane its own candidate.
+__device__ __forceinline__ void count_done(const KArgs& a, int s, long long n) {
+  __threadfence();
+  State& st = a.st[s];
+  unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)n);
+  if ((long long)old + n == st.cand_total) queue_push(a, s);
+}
+
 __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ double s_tab[];
   const int si = stage_tables(a);
@@ -813,33 +875,64 @@ __device__ void phase_candidates(const KArgs& a) {
     h = __shfl_sync(0xffffffffu, h, 0);
     if (h >= tot) break;
     const unsigned long long e = min(tot, h + K);
+    if (K >= 32) {
+      // one candidate per lane
+      for (unsigned long long q0 = h; q0 < e; q0 += 32) {
+        unsigned long long q = q0 + lane;
+        bool valid = q < e;
+        int s = -1;
+        unsigned long long code = 0;
+        double lb = 0.0;
+        bool keep = false, sampled = false;
+        if (valid) {
+          const unsigned long long* en = a.cands + CAND_WORDS * q;
+          s = (int)(en[0] >> 32);
+          code = en[0] & 0xffffffffULL;
+          lb = __longlong_as_double((long long)en[1]);
+          double aux[6];
+#pragma unroll
+          for (int t = 0; t < 6; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
+          int r = thread_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
+          keep = r & 1;
+          sampled = r & 2;
+          if (keep) append_survivor(a, s, code, lb);
+        }
+        // per-instance counts (samples, done), aggregated over the warp
+        unsigned int act = __ballot_sync(0xffffffffu, valid);
+        while (act) {
+          int leader = __ffs(act) - 1;
+          int ls = __shfl_sync(0xffffffffu, s, leader);
+          unsigned int m = __ballot_sync(0xffffffffu, valid && s == ls);
+          unsigned int sm = __ballot_sync(0xffffffffu, valid && s == ls && sampled);
+          if (lane == leader) {
+            if (sm) atomicAdd((unsigned long long*)&a.st[ls].samples, (unsigned long long)__popc(sm));
+            count_done(a, ls, __popc(m));
+          }
+          act &= ~m;
+        }
+      }
+      continue;
+    }
     int acc_s = -1;
     long long acc_n = 0;
     for (unsigned long long q = h; q < e; ++q) {
-      unsigned long long w0 = a.cands[2 * q];
-      double lb = __longlong_as_double((long long)a.cands[2 * q + 1]);
+      const unsigned long long* en = a.cands + CAND_WORDS * q;
+      unsigned long long w0 = en[0];
+      double lb = __longlong_as_double((long long)en[1]);
+      double aux[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
       int s = (int)(w0 >> 32);
       unsigned long long code = w0 & 0xffffffffULL;
-      bool keep = warp_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb);
+      bool keep = warp_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
       if (keep && lane == 0) append_survivor(a, s, code, lb);
       if (lane == 0) {
-        if (s != acc_s && acc_s >= 0) {
-          __threadfence();
-          State& st = a.st[acc_s];
-          unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)acc_n);
-          if ((long long)old + acc_n == st.cand_total) queue_push(a, acc_s);
-          acc_n = 0;
-        }
+        if (s != acc_s && acc_s >= 0) { count_done(a, acc_s, acc_n); acc_n = 0; }
         acc_s = s;
         acc_n++;
       }
     }
-    if (lane == 0 && acc_s >= 0) {
-      __threadfence();
-      State& st = a.st[acc_s];
-      unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)acc_n);
-      if ((long long)old + acc_n == st.cand_total) queue_push(a, acc_s);
-    }
+    if (lane == 0 && acc_s >= 0) count_done(a, acc_s, acc_n);
     __syncwarp();
   }
   __syncthreads();
@@ -1542,8 +1635,8 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaMemset(E->d_ctl, 0, sizeof(Ctl))))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_ids, sizeof(int) * 3 * E->max_slots)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_queue, sizeof(unsigned long long) * E->max_slots)))) break;
-    E->cand_cap = 1LL << 22;
-    if ((rc = cuda_err(cudaMalloc(&E->d_cands, 16 * (size_t)E->cand_cap)))) break;
+    E->cand_cap = std::min<long long>(1LL << 24, std::max<long long>(1LL << 20, 8192LL * E->max_slots));
+    if ((rc = cuda_err(cudaMalloc(&E->d_cands, 8 * CAND_WORDS * (size_t)E->cand_cap)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);

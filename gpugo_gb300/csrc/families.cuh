@@ -348,7 +348,10 @@ __device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned lo
   return (long long)i * D.wid + digit(D, C.c0, C.gsz, code, i);
 }
 
-__device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
+// aux (may be null) receives the intermediates the derivative test reuses:
+// expsqrt E = exp(-B r), r, u (six doubles); prodcos the cosine product (two).
+__device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                        double* aux = nullptr) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
   const long long* off = D.t_off;
@@ -375,9 +378,11 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
       for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
       for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
       iv inv_n = mk(k[2], k[3]);
-      iv t = sqrt_iv(mul(s, inv_n));
-      t = times(exp_iv(times(t, -k[1])), -k[0]);
+      iv r = sqrt_iv(mul(s, inv_n));
+      iv E = exp_iv(times(r, -k[1]));
+      iv t = times(E, -k[0]);
       iv u = exp_iv(mul(c, inv_n));
+      if (aux) { aux[0] = E.lo; aux[1] = E.hi; aux[2] = r.lo; aux[3] = r.hi; aux[4] = u.lo; aux[5] = u.hi; }
       return add(minus(t, u), mk(k[4], k[5])).lo;
     }
     case FAM_PRODCOS: {
@@ -385,6 +390,7 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
       for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
       for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ4] + 2 * eidx(D, C, code, i)));
       s = plus(mul(s, mk(k[0], k[1])), 1.0);
+      if (aux) { aux[0] = pr.lo; aux[1] = pr.hi; }
       return add(s, pr).lo;
     }
   }
@@ -489,6 +495,30 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
     iv pr = mk(1.0, 1.0);
     for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
     P->g = pr;
+  }
+  return 0;
+}
+
+// The same scalars from the value pass's intermediates.  expsqrt: the value code
+// list computes r = sqrt(mean x^2), E = exp(-B r) and u = exp(mean cos) exactly as
+// the derivative code list does.  prodcos: the value product starts from [-1,-1]
+// and the derivative product from [1,1]; interval multiplication commutes with
+// negation bit for bit, so P is the negated value product.
+__device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                             const double* aux, DerivPre* P) {
+  const int n = D.n;
+  const double* k = D.cst;
+  if (D.family == FAM_EXPSQRT) {
+    const unsigned char* zb = (const unsigned char*)(T + D.t_off[T_ZB]);
+    int origin = 1;
+    for (int i = 0; i < n; ++i)
+      if (!zb[eidx(D, C, code, i)]) { origin = 0; break; }
+    if (origin) return 1;
+    iv E = mk(aux[0], aux[1]), r = mk(aux[2], aux[3]);
+    P->g = mul(div(E, r), mk(k[6], k[7]));
+    P->u = mk(aux[4], aux[5]);
+  } else if (D.family == FAM_PRODCOS) {
+    P->g = mk(-aux[1], -aux[0]);
   }
   return 0;
 }
