@@ -77,6 +77,7 @@ struct State {
   long long ubc_count;        // UB candidates recorded this iteration
   long long m_children;       // children of the current parent
   long long b_done;           // (unused)
+  unsigned long long seed_key;  // high half of the smallest candidate LB key << 32 | its child code
   long long cand_total;       // candidates queued this iteration
   long long cand_done;        // candidates processed this iteration
   int has_who;
@@ -100,6 +101,8 @@ struct Ctl {
   unsigned long long cand_tail;   // candidate queue: entries written in pass 1
   unsigned long long cand_head;   // candidate queue: entries claimed in pass 2
   long long cand_claim;           // entries claimed per atomic in pass 2
+  int seed_on;                    // run the seed pass this iteration
+  int pad2;
 };
 
 struct KArgs {
@@ -363,11 +366,14 @@ __device__ void phase_tables(const KArgs& a) {
   bstamp(a, 0);
   const long long tot = a.ctl->totA;
   const int nA = a.ctl->nA;
-  const long long G = gridDim.x;
+  const int lane = threadIdx.x & 31;
+  // 32 consecutive items per warp (same instance, mostly the same coordinate and
+  // digit), warps dealt round-robin over the blocks
+  const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long w = ((long long)(threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
   int hint = -1;
-  for (long long r = 0;; ++r) {
-    long long it = (r * blockDim.x + threadIdx.x) * G + blockIdx.x;
-    if ((r * blockDim.x) * G >= tot) break;
+  for (long long base = w * 32; base < tot; base += W * 32) {
+    long long it = base + lane;
     if (it >= tot) continue;
     int k = find_seg(a.prefA, nA, it, hint);
     hint = k;
@@ -513,6 +519,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     st.b_done = 0;
     st.cand_total = 0;
     st.cand_done = 0;
+    st.seed_key = ~0ULL;
     st.removed_new = 0;
   }
   __syncwarp();
@@ -790,6 +797,22 @@ __device__ void phase_bound(const KArgs& a) {
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
     if (!cm) continue;
+    {
+      // the lowest-LB candidate of each instance seeds the UB before pass 2
+      unsigned long long sk = cand ? (((ord_key(lb) >> 32) << 32) | code) : ~0ULL;
+      unsigned int act = cm;
+      while (act) {
+        int leader = __ffs(act) - 1;
+        int ls = __shfl_sync(0xffffffffu, s, leader);
+        unsigned long long v = (cand && s == ls) ? sk : ~0ULL;
+        for (int o = 16; o > 0; o >>= 1) {
+          unsigned long long y = __shfl_xor_sync(0xffffffffu, v, o);
+          v = y < v ? y : v;
+        }
+        if (lane == leader) atomicMin(&a.st[ls].seed_key, v);
+        act &= ~__ballot_sync(0xffffffffu, cand && s == ls);
+      }
+    }
     unsigned long long qb = 0;
     if (lane == 0) qb = atomicAdd(&a.ctl->cand_tail, (unsigned long long)__popc(cm));
     qb = __shfl_sync(0xffffffffu, qb, 0);
@@ -848,7 +871,51 @@ __device__ void prefill_ready(const KArgs& a) {
     // a warp per candidate while there are fewer candidates than warps x 32;
     // beyond that each lane takes its own candidate, 32 or 64 per claim
     a.ctl->cand_claim = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 8 ? 8 : c));
+    a.ctl->seed_on = (tot > 4 * W) ? 1 : 0;
     a.ctl->cand_tail = (unsigned long long)tot;
+  }
+}
+
+// Seed pass (long candidate queues): one warp per instance evaluates the samples
+// of its lowest-LB candidate and lowers the UB with them.  The child is processed
+// again in pass 2; the UB stays the minimum over the same set of sample values.
+__device__ void phase_seed(const KArgs& a) {
+  extern __shared__ double s_tab[];
+  const int si = stage_tables(a);
+  const int nA = a.ctl->nA;
+  const int lane = threadIdx.x & 31;
+  const int gw = ((threadIdx.x >> 5) * gridDim.x) + blockIdx.x;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int k = gw; k < nA; k += nwarps) {
+    const int s = a.idsA[k];
+    const Desc& D = a.desc[s];
+    State& st = a.st[s];
+    const unsigned long long sk = st.seed_key;
+    if (sk == ~0ULL) continue;
+    const unsigned long long code = sk & 0xffffffffULL;
+    const double* T = (s == si) ? s_tab : D.tab;
+    ChildCtx C;
+    C.c0 = st.cyc - 1;
+    C.gsz = group_size(D.n, D.group, st.cyc);
+    double bv = 0.0;
+    int bj = J_NONE;
+    for (int j = lane; j < D.S; j += 32) {
+      double v = samp_one(D, T, C, code, j);
+      if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+      if (samp_less(ov, oj, bv, bj)) { bv = ov; bj = oj; }
+    }
+    if (lane == 0 && bj != J_NONE) {
+      double sm = feq(bv, 0.0) ? 0.0 : bv;
+      if (flt(sm, ord_val(st.ub_start))) {
+        long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+        if (slot < D.ubc_cap) { D.ubc_val[slot] = sm; D.ubc_id[slot] = (code << 8) | (unsigned long long)bj; }
+      }
+      atomicMin(&st.ub, ord_key(sm));
+    }
   }
 }
 
@@ -1070,6 +1137,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
     stamp(a, it, 1);
     phase_bound(a);
     if (!grid_barrier(a, tp)) return;
+    if (a.ctl->seed_on) {
+      phase_seed(a);
+      if (!grid_barrier(a, NoTail{})) return;
+    }
     phase_candidates(a);
     if (!grid_barrier(a, tc)) return;
     stamp(a, it, 2);
@@ -1730,6 +1801,7 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
     if (ub0 == 0.0) ub0 = 0.0;
     s0.ub = ord_key_host(ub0);
     s0.ub_start = s0.ub;
+    s0.seed_key = ~0ULL;
     s0.out_lb_min = INFINITY;
     s0.m_children = children_host(spec, 1);
     if ((rc = cuda_err(cudaMemcpyAsync(E->d_state + slot, &s0, sizeof(State), cudaMemcpyHostToDevice, st)))) break;
