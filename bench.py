@@ -309,6 +309,7 @@ def run_batched(args):
             "higher_is_better": True, "data": "synthetic (config 4 generator, MASTER_SEED+4)",
             "config": {"workload": f"cfg4-batch{args.count}: families F1-F4, n log-uniform 2..64, UB-LB<=1e-6",
                        "certified": sum(r.certified for r in res), "boxes": boxes,
+                       "samples_evaluated": sum(r.samples_evaluated for r in res),
                        "max_iterations": max(r.iterations for r in res)},
             "batched_wall_s": t_b, "batched_device_s": (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
             "batched_launches": st1["kernel_launches"] - st0["kernel_launches"],

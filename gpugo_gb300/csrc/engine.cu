@@ -751,6 +751,7 @@ __device__ int stage_tables(const KArgs& a) {
 }
 
 __device__ __forceinline__ void append_survivor(const KArgs& a, int s, unsigned long long code, double lb) {
+  if (feq(lb, 0.0)) lb = 0.0;  // list keys order -0 before +0; the LB comparison does not
   const Desc& D = a.desc[s];
   State& st = a.st[s];
   long long pos = (long long)atomicAdd((unsigned long long*)&st.count, 1ULL);

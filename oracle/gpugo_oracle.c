@@ -1072,7 +1072,7 @@ OC_API int oc_solve(const oc_spec* sp, int mode, oc_result* res, double* boxes_o
         for (uint64_t code = 0; code < M; ++code) {
             if (!ckeep[code]) continue;
             if (L == lcap) { lcap *= 2; list = (entry*)realloc(list, sizeof(entry) * lcap); }
-            entry e = { clb[code], (uint32_t)cur, (uint32_t)code };
+            entry e = { clb[code] == 0.0 ? 0.0 : clb[code], (uint32_t)cur, (uint32_t)code };
             list[L++] = e;
             ns++;
         }
