@@ -110,6 +110,15 @@ def test_solve_trace_parity(oracle_lib, name, make):
     assert rg.lb - 1e-12 <= fx <= rg.ub + 1e-12
 
 
+def test_solve_large_list_parity(oracle_lib):
+    """Lists of tens of thousands of entries take the grid-wide compaction and
+    argmin path instead of the block-level one; the trace must not change."""
+    p = P.instance(P.COSQUAD, 32, 20, 1e-6)
+    p.max_iter = 3000
+    rg, ro = _compare_solves(p, oracle_lib, box_cap=64)
+    assert rg.status == G.CERTIFIED and max(ro.trace["pool"]) > 4096
+
+
 def test_solve_width_mode_parity(oracle_lib):
     p = P.instance(P.COSQUAD, 4, 99, tol=0.0, split=(4, 2))
     p.stop_mode = P.STOP_WIDTH
