@@ -795,6 +795,7 @@ __device__ void phase_bound(const KArgs& a) {
       C.gsz = group_size(D.n, D.group, st.cyc);
       lb = child_lb(D, T, C, code, aux);
       cand = !flt(ord_val(st.ub_start), lb);
+      if (cand && D.family == FAM_EXPSQRT) expsqrt_aux(D, T, C, code, aux);
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
     if (!cm) continue;

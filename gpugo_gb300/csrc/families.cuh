@@ -344,6 +344,49 @@ struct ChildCtx {
   int c0, gsz;
 };
 
+// One side of the interval operations with a positive interval constant [kl, kh]
+// (IA.py:117-152 with the sign of the constant known): the lower bound of a*k
+// depends on a's lower bound only, the upper bound on a's upper bound only.
+__device__ __forceinline__ double mulk_lo(double al, double kl, double kh) {
+  return fneg(al) ? __dmul_rd(al, kh) : __dmul_rd(al, kl);
+}
+__device__ __forceinline__ double mulk_hi(double ah, double kl, double kh) {
+  return fneg(ah) ? __dmul_ru(ah, kl) : __dmul_ru(ah, kh);
+}
+// one side of power(., 1/2) and exp (IA.py:209-304, :532-570)
+__device__ __forceinline__ double sqrt_lo(double l) { return bump_lo(__dsqrt_rn(fneg(l) ? 0.0 : l), 5); }
+__device__ __forceinline__ double sqrt_hi(double h) { return bump_hi(__dsqrt_rn(fneg(h) ? 0.0 : h), 5); }
+__device__ __forceinline__ double exp_lo(double x) {
+  double l = gg_exp(x);
+  if (isnan_(l)) return l;
+  uint64_t m = d2u(l);
+  return (m < 2) ? 0.0 : u2d(m - 2);
+}
+__device__ __forceinline__ double exp_hi(double x) {
+  double h = gg_exp(x);
+  if (isnan_(h)) return h;
+  uint64_t m = d2u(h);
+  return (m + 2 >= INF_BITS) ? u2d(INF_BITS) : u2d(m + 2);
+}
+
+// expsqrt f = -A exp(-B sqrt(mean x^2)) - exp(mean cos) + A + e (ackley50.py:166-212):
+// f's lower bound from the lower bound of the sum of squares and the upper bound of
+// the cosine sum; its upper bound from the opposite sides.
+__device__ __forceinline__ double expsqrt_lo(const double* k, double s_lo, double c_hi) {
+  double r_lo = sqrt_lo(mulk_lo(s_lo, k[2], k[3]));
+  double E_hi = exp_hi(__dmul_ru(r_lo, -k[1]));        // times(r, -B).hi
+  double t_lo = __dmul_rd(E_hi, -k[0]);                // times(E, -A).lo
+  double u_hi = exp_hi(mulk_hi(c_hi, k[2], k[3]));
+  return __dadd_rd(__dadd_rd(t_lo, -u_hi), k[4]);
+}
+__device__ __forceinline__ double expsqrt_hi(const double* k, double s_hi, double c_lo) {
+  double r_hi = sqrt_hi(mulk_hi(s_hi, k[2], k[3]));
+  double E_lo = exp_lo(__dmul_rd(r_hi, -k[1]));        // times(r, -B).lo
+  double t_hi = __dmul_ru(E_lo, -k[0]);                // times(E, -A).hi
+  double u_lo = exp_lo(mulk_lo(c_lo, k[2], k[3]));
+  return __dadd_ru(__dadd_ru(t_hi, -u_lo), k[5]);
+}
+
 __device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned long long code, int i) {
   return (long long)i * D.wid + digit(D, C.c0, C.gsz, code, i);
 }
@@ -374,24 +417,18 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
       return f;
     }
     case FAM_EXPSQRT: {
-      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
-      for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
-      iv inv_n = mk(k[2], k[3]);
-      iv r = sqrt_iv(mul(s, inv_n));
-      iv E = exp_iv(times(r, -k[1]));
-      iv t = times(E, -k[0]);
-      iv u = exp_iv(mul(c, inv_n));
-      if (aux) { aux[0] = E.lo; aux[1] = E.hi; aux[2] = r.lo; aux[3] = r.hi; aux[4] = u.lo; aux[5] = u.hi; }
-      return add(minus(t, u), mk(k[4], k[5])).lo;
+      double s_lo = 0.0, c_hi = 0.0;
+      for (int i = 0; i < n; ++i) s_lo = __dadd_rd(s_lo, T[off[T_SQ] + 2 * eidx(D, C, code, i)]);
+      for (int i = 0; i < n; ++i) c_hi = __dadd_ru(c_hi, T[off[T_CS] + 2 * eidx(D, C, code, i) + 1]);
+      return expsqrt_lo(k, s_lo, c_hi);
     }
     case FAM_PRODCOS: {
-      iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
+      iv pr = mk(-1.0, -1.0);
+      double s_lo = 0.0;
       for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
-      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ4] + 2 * eidx(D, C, code, i)));
-      s = plus(mul(s, mk(k[0], k[1])), 1.0);
+      for (int i = 0; i < n; ++i) s_lo = __dadd_rd(s_lo, T[off[T_SQ4] + 2 * eidx(D, C, code, i)]);
       if (aux) { aux[0] = pr.lo; aux[1] = pr.hi; }
-      return add(s, pr).lo;
+      return __dadd_rd(__dadd_rd(mulk_lo(s_lo, k[0], k[1]), 1.0), pr.lo);
     }
   }
   return 0.0;
@@ -421,21 +458,17 @@ __device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx
       return f;
     }
     case FAM_EXPSQRT: {
-      iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQS] + 2 * (eidx(D, C, code, i) * S + j)));
-      for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CSS] + 2 * (eidx(D, C, code, i) * S + j)));
-      iv inv_n = mk(k[2], k[3]);
-      iv t = sqrt_iv(mul(s, inv_n));
-      t = times(exp_iv(times(t, -k[1])), -k[0]);
-      iv u = exp_iv(mul(c, inv_n));
-      return add(minus(t, u), mk(k[4], k[5])).hi;
+      double s_hi = 0.0, c_lo = 0.0;
+      for (int i = 0; i < n; ++i) s_hi = __dadd_ru(s_hi, T[off[T_SQS] + 2 * (eidx(D, C, code, i) * S + j) + 1]);
+      for (int i = 0; i < n; ++i) c_lo = __dadd_rd(c_lo, T[off[T_CSS] + 2 * (eidx(D, C, code, i) * S + j)]);
+      return expsqrt_hi(k, s_hi, c_lo);
     }
     default: {  // FAM_PRODCOS
-      iv pr = mk(-1.0, -1.0), s = mk(0.0, 0.0);
+      iv pr = mk(-1.0, -1.0);
+      double s_hi = 0.0;
       for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CRS] + 2 * (eidx(D, C, code, i) * S + j)));
-      for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQS4] + 2 * (eidx(D, C, code, i) * S + j)));
-      s = plus(mul(s, mk(k[0], k[1])), 1.0);
-      return add(s, pr).hi;
+      for (int i = 0; i < n; ++i) s_hi = __dadd_ru(s_hi, T[off[T_SQS4] + 2 * (eidx(D, C, code, i) * S + j) + 1]);
+      return __dadd_ru(__dadd_ru(mulk_hi(s_hi, k[0], k[1]), 1.0), pr.hi);
     }
   }
 }
@@ -497,6 +530,23 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
     P->g = pr;
   }
   return 0;
+}
+
+// expsqrt intermediates for a candidate: E = exp(-B r), r, u as full intervals
+// (the value pass computes one side of each only).
+__device__ __noinline__ void expsqrt_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+                                         double* aux) {
+  const int n = D.n;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
+  for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
+  for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
+  iv inv_n = mk(k[2], k[3]);
+  iv r = sqrt_iv(mul(s, inv_n));
+  iv E = exp_iv(times(r, -k[1]));
+  iv u = exp_iv(mul(c, inv_n));
+  aux[0] = E.lo; aux[1] = E.hi; aux[2] = r.lo; aux[3] = r.hi; aux[4] = u.lo; aux[5] = u.hi;
 }
 
 // The same scalars from the value pass's intermediates.  expsqrt: the value code
