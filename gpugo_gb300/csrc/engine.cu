@@ -934,6 +934,7 @@ __device__ __forceinline__ void count_done(const KArgs& a, int s, long long n) {
 
 __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ double s_tab[];
+  __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
   const int si = stage_tables(a);
   const int lane = threadIdx.x & 31;
   const unsigned long long tot = a.ctl->cand_tail;
@@ -945,28 +946,55 @@ __device__ void phase_candidates(const KArgs& a) {
     if (h >= tot) break;
     const unsigned long long e = min(tot, h + K);
     if (K >= 32) {
-      // one candidate per lane
+      // One candidate per lane.  The claim is filtered first (LB against the
+      // current UB) and the survivors are packed densely, so that no lane idles
+      // through another lane's sample chains.
+      unsigned int* surv = s_surv[threadIdx.x >> 5];
+      int nsurv = 0;
       for (unsigned long long q0 = h; q0 < e; q0 += 32) {
         unsigned long long q = q0 + lane;
         bool valid = q < e;
+        bool live = false;
         int s = -1;
-        unsigned long long code = 0;
-        double lb = 0.0;
-        bool keep = false, sampled = false;
         if (valid) {
           const unsigned long long* en = a.cands + CAND_WORDS * q;
           s = (int)(en[0] >> 32);
-          code = en[0] & 0xffffffffULL;
-          lb = __longlong_as_double((long long)en[1]);
+          double lb = __longlong_as_double((long long)en[1]);
+          live = !flt(atomic_ub_read(&a.st[s].ub), lb);
+        }
+        unsigned int lm = __ballot_sync(0xffffffffu, live);
+        if (live) surv[nsurv + __popc(lm & ((1u << lane) - 1u))] = (unsigned int)(q - h);
+        nsurv += __popc(lm);
+        // candidates ruled out here are done
+        unsigned int act = __ballot_sync(0xffffffffu, valid && !live);
+        while (act) {
+          int leader = __ffs(act) - 1;
+          int ls = __shfl_sync(0xffffffffu, s, leader);
+          unsigned int m = __ballot_sync(0xffffffffu, valid && !live && s == ls);
+          if (lane == leader) count_done(a, ls, __popc(m));
+          act &= ~m;
+        }
+      }
+      __syncwarp();
+      for (int r0 = 0; r0 < nsurv; r0 += 32) {
+        int idx = r0 + lane;
+        bool valid = idx < nsurv;
+        int s = -1;
+        bool keep = false, sampled = false;
+        if (valid) {
+          const unsigned long long q = h + surv[idx];
+          const unsigned long long* en = a.cands + CAND_WORDS * q;
+          s = (int)(en[0] >> 32);
+          unsigned long long code = en[0] & 0xffffffffULL;
+          double lb = __longlong_as_double((long long)en[1]);
           double aux[6];
 #pragma unroll
           for (int t = 0; t < 6; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
-          int r = thread_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
-          keep = r & 1;
-          sampled = r & 2;
+          int rr = thread_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
+          keep = rr & 1;
+          sampled = rr & 2;
           if (keep) append_survivor(a, s, code, lb);
         }
-        // per-instance counts (samples, done), aggregated over the warp
         unsigned int act = __ballot_sync(0xffffffffu, valid);
         while (act) {
           int leader = __ffs(act) - 1;
@@ -980,6 +1008,7 @@ __device__ void phase_candidates(const KArgs& a) {
           act &= ~m;
         }
       }
+      __syncwarp();
       continue;
     }
     int acc_s = -1;
