@@ -669,14 +669,14 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   if (sm == 0.0) sm = 0.0;  // -0 -> +0
   if (lane == 0) {
     atomicAdd((unsigned long long*)&st.samples, 1ULL);
-    if (sm < ord_val(st.ub_start)) {
+    if (flt(sm, ub)) {
       long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
       if (slot < D.ubc_cap) {
         D.ubc_val[slot] = sm;
         D.ubc_id[slot] = (code << 8) | (unsigned long long)bj;
       }
+      atomicMin(&st.ub, ord_key(sm));
     }
-    if (sm < ub) atomicMin(&st.ub, ord_key(sm));
   }
   __syncwarp();
   ub = atomic_ub_read(&st.ub);
@@ -709,18 +709,17 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   C.gsz = group_size(D.n, D.group, st.cyc);
   double ub = atomic_ub_read(&st.ub);
   if (flt(ub, lb)) return 0;
-  const double ub0 = ord_val(st.ub_start);
+  // a sample is recorded (for the minimiser point) only when it lowers this
+  // lane's view of the UB: the first sample to reach the final UB always does
   for (int j = 0; j < D.S; ++j) {
     double v = samp_one(D, T, C, code, j);
     if (feq(v, 0.0)) v = 0.0;
-    if (flt(v, ub0)) {
+    if (flt(v, ub)) {
       long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
       if (slot < D.ubc_cap) {
         D.ubc_val[slot] = v;
         D.ubc_id[slot] = (code << 8) | (unsigned long long)j;
       }
-    }
-    if (flt(v, ub)) {
       atomicMin(&st.ub, ord_key(v));
       ub = v;
     }
@@ -912,11 +911,11 @@ __device__ void phase_seed(const KArgs& a) {
     }
     if (lane == 0 && bj != J_NONE) {
       double sm = feq(bv, 0.0) ? 0.0 : bv;
-      if (flt(sm, ord_val(st.ub_start))) {
+      if (flt(sm, atomic_ub_read(&st.ub))) {
         long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
         if (slot < D.ubc_cap) { D.ubc_val[slot] = sm; D.ubc_id[slot] = (code << 8) | (unsigned long long)bj; }
+        atomicMin(&st.ub, ord_key(sm));
       }
-      atomicMin(&st.ub, ord_key(sm));
     }
   }
 }
