@@ -1148,7 +1148,14 @@ struct TailAfterChildren {
 };
 
 __device__ __forceinline__ void stamp(const KArgs& a, long long it, int k) {
-  if (a.stamps && blockIdx.x == 0 && threadIdx.x == 0 && (it * 5 + k) < a.stamp_cap) a.stamps[it * 5 + k] = gtimer();
+  if (a.stamps && blockIdx.x == 0 && threadIdx.x == 0 && (it * 8 + k) < a.stamp_cap) {
+    a.stamps[it * 8 + k] = gtimer();
+    if (k == 2) {
+      a.stamps[it * 8 + 5] = a.ctl->cand_tail;
+      a.stamps[it * 8 + 6] = (unsigned long long)a.ctl->nA;
+      a.stamps[it * 8 + 7] = (unsigned long long)a.ctl->totB;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
@@ -1743,7 +1750,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
     if (const char* sp = getenv("GPUGO_PHASE_STAMPS")) {
       E->stamp_path = sp;
-      E->stamp_cap = 5 * 65536;
+      E->stamp_cap = 8 * 65536;
       if ((rc = cuda_err(cudaMalloc(&E->d_stamps, 8 * E->stamp_cap)))) break;
       E->bstamp_iters = 64;
       if ((rc = cuda_err(cudaMalloc(&E->d_bstamps, 8 * 6 * (size_t)E->bstamp_iters * E->blocks)))) break;
@@ -1894,12 +1901,12 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   E->iterations += c.iters;
   E->d2h += (int64_t)(sizeof(Ctl) + sizeof(State) * E->max_slots);
   if (E->d_stamps && c.iters > 0) {
-    long long k = std::min<long long>(5 * c.iters, E->stamp_cap);
+    long long k = std::min<long long>(8 * c.iters, E->stamp_cap);
     std::vector<unsigned long long> ts(k);
     CK(cudaMemcpy(ts.data(), E->d_stamps, 8 * k, cudaMemcpyDeviceToHost));
     if (FILE* f = fopen(E->stamp_path, "a")) {
       fprintf(f, "run blocks=%d threads=%d iters=%lld\n", E->blocks, E->threads, (long long)c.iters);
-      for (long long i = 0; i < k; ++i) fprintf(f, "%llu%c", ts[i], (i % 5 == 4) ? '\n' : ' ');
+      for (long long i = 0; i < k; ++i) fprintf(f, "%llu%c", ts[i], (i % 8 == 7) ? '\n' : ' ');
       fclose(f);
     }
     long long ki = std::min<long long>(c.iters, E->bstamp_iters);
