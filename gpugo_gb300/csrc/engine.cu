@@ -457,7 +457,8 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
         ccyc = D.pcyc[prow];
         const double* pb = D.parents + 2LL * n * prow;
         int gsz = group_size(n, D.group, ccyc);
-        iv x0 = child_iv(D, pb, D.pwid + (long long)n * prow, ccyc - 1, gsz, 0, digit(D, ccyc - 1, gsz, code, 0));
+        iv x0 = child_iv(D, pb, D.pwid + (long long)n * prow, ccyc - 1, gsz, 0,
+                         digit(D, ccyc - 1, gsz, pack_code(D, gsz, code), 0));
         double width = __dsub_rn(x0.hi, x0.lo);
         if (width < D.width_tol && ccyc == D.max_cyc) {
           decision = 1;
@@ -485,8 +486,9 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     double* nb = D.parents + 2LL * n * (st.iter + 1);
     double* nw = D.pwid + (long long)n * (st.iter + 1);
     const int gsz = group_size(n, D.group, ccyc);
+    const unsigned long long pc = pack_code(D, gsz, code);
     for (int i = lane; i < n; i += 32) {
-      iv x = child_iv(D, pb, pw, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, code, i));
+      iv x = child_iv(D, pb, pw, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, pc, i));
       nb[2 * i] = x.lo;
       nb[2 * i + 1] = x.hi;
       nw[i] = part_width(D, x.lo, x.hi);
@@ -653,10 +655,11 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   C.gsz = group_size(D.n, D.group, st.cyc);
   double ub = atomic_ub_read(&st.ub);
   if (lb > ub) return false;
+  const unsigned long long pc = pack_code(D, C.gsz, code);
   double bv = 0.0;
   int bj = J_NONE;
   for (int j = lane; j < D.S; j += 32) {
-    double v = samp_one(D, T, C, code, j);
+    double v = samp_one(D, T, C, pc, j);
     if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
   }
 #pragma unroll
@@ -685,14 +688,14 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   DerivPre P;
   int skip = 0;
   if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS) {
-    if (lane == 0) skip = aux ? deriv_pre_aux(D, T, C, code, aux, &P) : deriv_pre(D, T, C, code, &P);
+    if (lane == 0) skip = aux ? deriv_pre_aux(D, T, C, pc, aux, &P) : deriv_pre(D, T, C, pc, &P);
     skip = __shfl_sync(0xffffffffu, skip, 0);
     P.g.lo = shfl_d(P.g.lo, 0); P.g.hi = shfl_d(P.g.hi, 0);
     P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
   }
   int pruned = 0;
   if (!skip)
-    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, code, j, P);
+    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
   return !__any_sync(0xffffffffu, pruned);
 }
 
@@ -709,10 +712,12 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   C.gsz = group_size(D.n, D.group, st.cyc);
   double ub = atomic_ub_read(&st.ub);
   if (flt(ub, lb)) return 0;
-  // a sample is recorded (for the minimiser point) only when it lowers this
-  // lane's view of the UB: the first sample to reach the final UB always does
-  for (int j = 0; j < D.S; ++j) {
-    double v = samp_one(D, T, C, code, j);
+  const unsigned long long pc = pack_code(D, C.gsz, code);
+  // Samples are evaluated four (then two, then one) at a time and considered in
+  // index order.  A sample is recorded (for the minimiser point) only when it
+  // lowers this lane's view of the UB: the first sample to reach the final UB
+  // always does.
+  auto consider = [&](double v, int j) {
     if (feq(v, 0.0)) v = 0.0;
     if (flt(v, ub)) {
       long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
@@ -723,14 +728,33 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
       atomicMin(&st.ub, ord_key(v));
       ub = v;
     }
+  };
+  int j = 0;
+  for (; j + 4 <= D.S; j += 4) {
+    double v[4];
+    samp_multi<4>(D, T, C, pc, j, v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) consider(v[q], j + q);
+  }
+  if (j + 2 <= D.S) {
+    double v[2];
+    samp_multi<2>(D, T, C, pc, j, v);
+    consider(v[0], j);
+    consider(v[1], j + 1);
+    j += 2;
+  }
+  if (j < D.S) {
+    double v[1];
+    samp_multi<1>(D, T, C, pc, j, v);
+    consider(v[0], j);
   }
   ub = atomic_ub_read(&st.ub);
   if (flt(ub, lb)) return 2;
   DerivPre P;
   if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS)
-    if (deriv_pre_aux(D, T, C, code, aux, &P)) return 3;
-  for (int j = 0; j < D.n; ++j)
-    if (deriv_coord(D, T, C, code, j, P)) return 2;
+    if (deriv_pre_aux(D, T, C, pc, aux, &P)) return 3;
+  for (int jj = 0; jj < D.n; ++jj)
+    if (deriv_coord(D, T, C, pc, jj, P)) return 2;
   return 3;
 }
 
@@ -792,9 +816,10 @@ __device__ void phase_bound(const KArgs& a) {
       ChildCtx C;
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
-      lb = child_lb(D, T, C, code, aux);
+      const unsigned long long pc = pack_code(D, C.gsz, code);
+      lb = child_lb(D, T, C, pc, aux);
       cand = !flt(ord_val(st.ub_start), lb);
-      if (cand && D.family == FAM_EXPSQRT) expsqrt_aux(D, T, C, code, aux);
+      if (cand && D.family == FAM_EXPSQRT) expsqrt_aux(D, T, C, pc, aux);
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
     if (!cm) continue;
@@ -898,10 +923,11 @@ __device__ void phase_seed(const KArgs& a) {
     ChildCtx C;
     C.c0 = st.cyc - 1;
     C.gsz = group_size(D.n, D.group, st.cyc);
+    const unsigned long long pc = pack_code(D, C.gsz, code);
     double bv = 0.0;
     int bj = J_NONE;
     for (int j = lane; j < D.S; j += 32) {
-      double v = samp_one(D, T, C, code, j);
+      double v = samp_one(D, T, C, pc, j);
       if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1220,13 +1246,13 @@ __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long lo
   C.c0 = cyc - 1;
   C.gsz = group_size(D.n, D.group, cyc);
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x) {
-    unsigned long long code = codes[t];
-    double lb = child_lb(D, D.tab, C, code);
+    const unsigned long long pc = pack_code(D, C.gsz, codes[t]);
+    double lb = child_lb(D, D.tab, C, pc);
     int jb;
-    double sm = child_samp(D, D.tab, C, code, &jb);
+    double sm = child_samp(D, D.tab, C, pc, &jb);
     lb_out[t] = lb;
     samp_out[t] = sm;
-    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, D.tab, C, code);
+    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, D.tab, C, pc);
   }
 }
 
@@ -1359,6 +1385,9 @@ int validate(const gpugo_spec* s) {
   int g = std::min(s->group, s->n);
   double m = std::pow((double)s->wid, (double)g);
   if (m > 4294967296.0) return GPUGO_ERR_INVALID;
+  int dbits = 0;
+  while ((1LL << dbits) < s->wid) ++dbits;
+  if ((int64_t)dbits * g > 64) return GPUGO_ERR_INVALID;  // packed child codes (never with m <= 2^32)
   for (int i = 0; i < s->n; ++i)
     if (!(s->domain[2 * i] < s->domain[2 * i + 1])) return GPUGO_ERR_INVALID;
   int64_t need = 0;
@@ -1462,6 +1491,15 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->stop_mode = s->stop_mode;
   D->max_cyc = 1 + s->group * ((s->n - 1) / s->group);
   D->wlog = ilog2_exact(s->wid);
+  if (D->wlog >= 0) {
+    D->dbits = D->wlog;
+    D->wmag = 0;
+  } else {
+    int b = 0;
+    while ((1LL << b) < s->wid) ++b;
+    D->dbits = b;
+    D->wmag = (~0ULL) / (unsigned long long)s->wid + 1ULL;
+  }
   D->width_tol = s->width_tol; D->gap_tol = s->gap_tol;
   D->max_iter = s->max_iter;
   D->pool_cap = L.pool_cap; D->parent_cap = L.parent_cap; D->out_cap = L.out_cap; D->trace_cap = L.trace_cap;

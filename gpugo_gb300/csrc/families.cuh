@@ -42,6 +42,8 @@ struct CstLayout {
 
 struct Desc {
   int family, n, wid, group, S, stop_mode, max_cyc, wlog;
+  int dbits;                         // bits of one digit field of a packed child code
+  unsigned long long wmag;           // floor(2^64 / wid) + 1 (wid not a power of two)
   double width_tol, gap_tol;
   long long max_iter;
   long long pool_cap, parent_cap, out_cap, trace_cap, tiles_cap, ubc_cap;
@@ -76,13 +78,31 @@ __device__ __forceinline__ int group_size(int n, int group, int cyc) {
   return g < group ? g : group;
 }
 
-// digit of coordinate i (0-based) in child code; 0 for coordinates outside the split group
-__device__ __forceinline__ int digit(const Desc& D, int c0, int gsz, unsigned long long code, int i) {
+// A child code is a mixed-radix number: the digit of coordinate c0 + k is digit k
+// in base wid, least significant first (ackley50.py:544-577).  Kernels repack a
+// code once into fixed dbits-wide fields, after which every digit lookup is a
+// shift and a mask.  Division by wid is a multiply-high (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994): with
+// M = floor(2^64 / wid) + 1 = (2^64 + e) / wid, 0 < e < wid, the product
+// r M / 2^64 exceeds r / wid by less than r / 2^64 < 2^-32 < 1 / wid for every
+// r < 2^32, so its integer part is floor(r / wid).  Codes of a power-of-two wid
+// are packed already.
+__device__ __forceinline__ unsigned long long pack_code(const Desc& D, int gsz, unsigned long long code) {
+  if (D.wlog >= 0) return code;
+  unsigned long long p = 0, r = code;
+  for (int k = 0; k < gsz; ++k) {
+    unsigned long long q = __umul64hi(r, D.wmag);
+    p |= (r - q * (unsigned long long)D.wid) << (k * D.dbits);
+    r = q;
+  }
+  return p;
+}
+
+// digit of coordinate i (0-based) in a packed child code; 0 outside the split group
+__device__ __forceinline__ int digit(const Desc& D, int c0, int gsz, unsigned long long pc, int i) {
   int k = i - c0;
   if (k < 0 || k >= gsz) return 0;
-  if (D.wlog >= 0) return (int)((code >> (k * D.wlog)) & (unsigned long long)(D.wid - 1));
-  for (int t = 0; t < k; ++t) code /= (unsigned long long)D.wid;
-  return (int)(code % (unsigned long long)D.wid);
+  return (int)((pc >> (k * D.dbits)) & ((1ULL << D.dbits) - 1ULL));
 }
 
 // number of digit values of coordinate i this iteration
@@ -387,13 +407,16 @@ __device__ __forceinline__ double expsqrt_hi(const double* k, double s_hi, doubl
   return __dadd_ru(__dadd_ru(t_hi, -u_lo), k[5]);
 }
 
-__device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned long long code, int i) {
-  return (long long)i * D.wid + digit(D, C.c0, C.gsz, code, i);
+// Per-child functions take packed child codes (pack_code).
+__device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned long long pc, int i) {
+  return (long long)i * D.wid + digit(D, C.c0, C.gsz, pc, i);
 }
 
 // aux (may be null) receives the intermediates the derivative test reuses:
 // expsqrt E = exp(-B r), r, u (six doubles); prodcos the cosine product (two).
-__device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+// Two independent reductions over the coordinates share one loop; each keeps
+// the reference's left-to-right order.
+__device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                         double* aux = nullptr) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
@@ -402,15 +425,15 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
     case FAM_COSQUAD: {
       double s = 0.0;
       const double* tl = T + off[T_LO];
-      for (int i = 0; i < n; ++i) s = __dadd_rd(s, tl[eidx(D, C, code, i)]);
+      for (int i = 0; i < n; ++i) s = __dadd_rd(s, tl[eidx(D, C, pc, i)]);
       return __dadd_rd(s, k[6 * n]);
     }
     case FAM_CHAINED: {
       double f = 0.0;
       const double* tl = T + off[T_LO];
-      int dcur = digit(D, C.c0, C.gsz, code, 0);
+      int dcur = digit(D, C.c0, C.gsz, pc, 0);
       for (int i = 0; i < n - 1; ++i) {
-        int dn = digit(D, C.c0, C.gsz, code, i + 1);
+        int dn = digit(D, C.c0, C.gsz, pc, i + 1);
         f = __dadd_rd(f, tl[(long long)i * w * w + dcur * w + dn]);
         dcur = dn;
       }
@@ -418,15 +441,21 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
     }
     case FAM_EXPSQRT: {
       double s_lo = 0.0, c_hi = 0.0;
-      for (int i = 0; i < n; ++i) s_lo = __dadd_rd(s_lo, T[off[T_SQ] + 2 * eidx(D, C, code, i)]);
-      for (int i = 0; i < n; ++i) c_hi = __dadd_ru(c_hi, T[off[T_CS] + 2 * eidx(D, C, code, i) + 1]);
+      for (int i = 0; i < n; ++i) {
+        const long long e = eidx(D, C, pc, i);
+        s_lo = __dadd_rd(s_lo, T[off[T_SQ] + 2 * e]);
+        c_hi = __dadd_ru(c_hi, T[off[T_CS] + 2 * e + 1]);
+      }
       return expsqrt_lo(k, s_lo, c_hi);
     }
     case FAM_PRODCOS: {
       iv pr = mk(-1.0, -1.0);
       double s_lo = 0.0;
-      for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
-      for (int i = 0; i < n; ++i) s_lo = __dadd_rd(s_lo, T[off[T_SQ4] + 2 * eidx(D, C, code, i)]);
+      for (int i = 0; i < n; ++i) {
+        const long long e = eidx(D, C, pc, i);
+        pr = mul(pr, ldiv(T + off[T_CR] + 2 * e));
+        s_lo = __dadd_rd(s_lo, T[off[T_SQ4] + 2 * e]);
+      }
       if (aux) { aux[0] = pr.lo; aux[1] = pr.hi; }
       return __dadd_rd(__dadd_rd(mulk_lo(s_lo, k[0], k[1]), 1.0), pr.lo);
     }
@@ -434,43 +463,92 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
   return 0.0;
 }
 
-// upper bound of f at sample point j of the child (one pass of the sample code list)
-__device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long code, int j) {
+// Upper bounds of f at sample points j0 .. j0+M-1 of the child: M passes of the
+// sample code list run side by side in one loop over the coordinates, each in
+// the reference's order, so each value equals that of its own pass.
+template <int M>
+__device__ __forceinline__ void samp_multi(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
+                                           double* v) {
   const int n = D.n, w = D.wid, S = D.S;
   const double* k = D.cst;
   const long long* off = D.t_off;
   switch (D.family) {
     case FAM_COSQUAD: {
-      double s = 0.0;
-      const double* th = T + off[T_SHI];
-      for (int i = 0; i < n; ++i) s = __dadd_ru(s, th[eidx(D, C, code, i) * S + j]);
-      return __dadd_ru(s, k[6 * n + 1]);
+      double s[M];
+#pragma unroll
+      for (int q = 0; q < M; ++q) s[q] = 0.0;
+      const double* th = T + off[T_SHI] + j0;
+      for (int i = 0; i < n; ++i) {
+        const double* t = th + eidx(D, C, pc, i) * S;
+#pragma unroll
+        for (int q = 0; q < M; ++q) s[q] = __dadd_ru(s[q], t[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < M; ++q) v[q] = __dadd_ru(s[q], k[6 * n + 1]);
+      return;
     }
     case FAM_CHAINED: {
-      double f = 0.0;
-      const double* th = T + off[T_SHI];
-      int dcur = digit(D, C.c0, C.gsz, code, 0);
+      double f[M];
+#pragma unroll
+      for (int q = 0; q < M; ++q) f[q] = 0.0;
+      const double* th = T + off[T_SHI] + j0;
+      int dcur = digit(D, C.c0, C.gsz, pc, 0);
       for (int i = 0; i < n - 1; ++i) {
-        int dn = digit(D, C.c0, C.gsz, code, i + 1);
-        f = __dadd_ru(f, th[((long long)i * w * w + dcur * w + dn) * S + j]);
+        int dn = digit(D, C.c0, C.gsz, pc, i + 1);
+        const double* t = th + ((long long)i * w * w + dcur * w + dn) * S;
+#pragma unroll
+        for (int q = 0; q < M; ++q) f[q] = __dadd_ru(f[q], t[q]);
         dcur = dn;
       }
-      return f;
+#pragma unroll
+      for (int q = 0; q < M; ++q) v[q] = f[q];
+      return;
     }
     case FAM_EXPSQRT: {
-      double s_hi = 0.0, c_lo = 0.0;
-      for (int i = 0; i < n; ++i) s_hi = __dadd_ru(s_hi, T[off[T_SQS] + 2 * (eidx(D, C, code, i) * S + j) + 1]);
-      for (int i = 0; i < n; ++i) c_lo = __dadd_rd(c_lo, T[off[T_CSS] + 2 * (eidx(D, C, code, i) * S + j)]);
-      return expsqrt_hi(k, s_hi, c_lo);
+      double s_hi[M], c_lo[M];
+#pragma unroll
+      for (int q = 0; q < M; ++q) { s_hi[q] = 0.0; c_lo[q] = 0.0; }
+      const double* ts = T + off[T_SQS] + 2 * j0 + 1;
+      const double* tc = T + off[T_CSS] + 2 * j0;
+      for (int i = 0; i < n; ++i) {
+        const long long e2 = 2 * eidx(D, C, pc, i) * S;
+#pragma unroll
+        for (int q = 0; q < M; ++q) {
+          s_hi[q] = __dadd_ru(s_hi[q], ts[e2 + 2 * q]);
+          c_lo[q] = __dadd_rd(c_lo[q], tc[e2 + 2 * q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < M; ++q) v[q] = expsqrt_hi(k, s_hi[q], c_lo[q]);
+      return;
     }
     default: {  // FAM_PRODCOS
-      iv pr = mk(-1.0, -1.0);
-      double s_hi = 0.0;
-      for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CRS] + 2 * (eidx(D, C, code, i) * S + j)));
-      for (int i = 0; i < n; ++i) s_hi = __dadd_ru(s_hi, T[off[T_SQS4] + 2 * (eidx(D, C, code, i) * S + j) + 1]);
-      return __dadd_ru(__dadd_ru(mulk_hi(s_hi, k[0], k[1]), 1.0), pr.hi);
+      iv pr[M];
+      double s_hi[M];
+#pragma unroll
+      for (int q = 0; q < M; ++q) { pr[q] = mk(-1.0, -1.0); s_hi[q] = 0.0; }
+      const double* tr = T + off[T_CRS] + 2 * j0;
+      const double* ts = T + off[T_SQS4] + 2 * j0 + 1;
+      for (int i = 0; i < n; ++i) {
+        const long long e2 = 2 * eidx(D, C, pc, i) * S;
+#pragma unroll
+        for (int q = 0; q < M; ++q) {
+          pr[q] = mul(pr[q], ldiv(tr + e2 + 2 * q));
+          s_hi[q] = __dadd_ru(s_hi[q], ts[e2 + 2 * q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < M; ++q) v[q] = __dadd_ru(__dadd_ru(mulk_hi(s_hi[q], k[0], k[1]), 1.0), pr[q].hi);
+      return;
     }
   }
+}
+
+// upper bound of f at sample point j of the child (one pass of the sample code list)
+__device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j) {
+  double v;
+  samp_multi<1>(D, T, C, pc, j, &v);
+  return v;
 }
 
 // The sample code list keeps the first sample with the smallest upper bound
@@ -485,12 +563,12 @@ __device__ __forceinline__ bool samp_better(double v, int j, double bv, int bj) 
 }
 
 // smallest sampled upper bound; *jbest receives its sample index
-__device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+__device__ __noinline__ double child_samp(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                           int* jbest) {
   double best = 0.0;
   int jb = 0;
   for (int j = 0; j < D.S; ++j) {
-    double fh = samp_one(D, T, C, code, j);
+    double fh = samp_one(D, T, C, pc, j);
     if (j == 0 || flt(fh, best)) { best = fh; jb = j; }
   }
   *jbest = jb;
@@ -505,7 +583,7 @@ struct DerivPre {
   iv g, u;
 };
 
-__device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+__device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                       DerivPre* P) {
   const int n = D.n;
   const double* k = D.cst;
@@ -514,19 +592,22 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
     const unsigned char* zb = (const unsigned char*)(T + off[T_ZB]);
     int origin = 1;
     for (int i = 0; i < n; ++i)
-      if (!zb[eidx(D, C, code, i)]) { origin = 0; break; }
+      if (!zb[eidx(D, C, pc, i)]) { origin = 0; break; }
     if (origin) return 1;
     iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-    for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
+    for (int i = 0; i < n; ++i) {
+      const long long e = eidx(D, C, pc, i);
+      s = add(s, ldiv(T + off[T_SQ] + 2 * e));
+      c = add(c, ldiv(T + off[T_CS] + 2 * e));
+    }
     iv inv_n = mk(k[2], k[3]);
     iv r = sqrt_iv(mul(s, inv_n));
     iv g = exp_iv(times(r, -k[1]));
     P->g = mul(div(g, r), mk(k[6], k[7]));
-    for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
     P->u = exp_iv(mul(c, inv_n));
   } else if (D.family == FAM_PRODCOS) {
     iv pr = mk(1.0, 1.0);
-    for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, code, i)));
+    for (int i = 0; i < n; ++i) pr = mul(pr, ldiv(T + off[T_CR] + 2 * eidx(D, C, pc, i)));
     P->g = pr;
   }
   return 0;
@@ -534,14 +615,17 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
 
 // expsqrt intermediates for a candidate: E = exp(-B r), r, u as full intervals
 // (the value pass computes one side of each only).
-__device__ __noinline__ void expsqrt_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+__device__ __noinline__ void expsqrt_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                          double* aux) {
   const int n = D.n;
   const double* k = D.cst;
   const long long* off = D.t_off;
   iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-  for (int i = 0; i < n; ++i) s = add(s, ldiv(T + off[T_SQ] + 2 * eidx(D, C, code, i)));
-  for (int i = 0; i < n; ++i) c = add(c, ldiv(T + off[T_CS] + 2 * eidx(D, C, code, i)));
+  for (int i = 0; i < n; ++i) {
+    const long long e = eidx(D, C, pc, i);
+    s = add(s, ldiv(T + off[T_SQ] + 2 * e));
+    c = add(c, ldiv(T + off[T_CS] + 2 * e));
+  }
   iv inv_n = mk(k[2], k[3]);
   iv r = sqrt_iv(mul(s, inv_n));
   iv E = exp_iv(times(r, -k[1]));
@@ -554,7 +638,7 @@ __device__ __noinline__ void expsqrt_aux(const Desc& D, const double* T, ChildCt
 // the derivative code list does.  prodcos: the value product starts from [-1,-1]
 // and the derivative product from [1,1]; interval multiplication commutes with
 // negation bit for bit, so P is the negated value product.
-__device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+__device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                              const double* aux, DerivPre* P) {
   const int n = D.n;
   const double* k = D.cst;
@@ -562,7 +646,7 @@ __device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, Chi
     const unsigned char* zb = (const unsigned char*)(T + D.t_off[T_ZB]);
     int origin = 1;
     for (int i = 0; i < n; ++i)
-      if (!zb[eidx(D, C, code, i)]) { origin = 0; break; }
+      if (!zb[eidx(D, C, pc, i)]) { origin = 0; break; }
     if (origin) return 1;
     iv E = mk(aux[0], aux[1]), r = mk(aux[2], aux[3]);
     P->g = mul(div(E, r), mk(k[6], k[7]));
@@ -574,23 +658,23 @@ __device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, Chi
 }
 
 // generalized KKT test of coordinate j (rastrigin50.py:365-370); 1 = rule out
-__device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, ChildCtx C, unsigned long long code,
+__device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                            int j, const DerivPre& P) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
   const long long* off = D.t_off;
   switch (D.family) {
     case FAM_COSQUAD:
-      return ((const unsigned char*)(T + off[T_PRB]))[eidx(D, C, code, j)];
+      return ((const unsigned char*)(T + off[T_PRB]))[eidx(D, C, pc, j)];
     case FAM_CHAINED: {
       const long long w2 = (long long)w * w, w3 = w2 * w;
-      int dm = (j > 0) ? digit(D, C.c0, C.gsz, code, j - 1) : 0;
-      int d = digit(D, C.c0, C.gsz, code, j);
-      int dp = (j + 1 < n) ? digit(D, C.c0, C.gsz, code, j + 1) : 0;
+      int dm = (j > 0) ? digit(D, C.c0, C.gsz, pc, j - 1) : 0;
+      int d = digit(D, C.c0, C.gsz, pc, j);
+      int dp = (j + 1 < n) ? digit(D, C.c0, C.gsz, pc, j + 1) : 0;
       return ((const unsigned char*)(T + off[T_PRB]))[(long long)j * w3 + (long long)dm * w2 + (long long)d * w + dp];
     }
     case FAM_EXPSQRT: {
-      long long e = eidx(D, C, code, j);
+      long long e = eidx(D, C, pc, j);
       iv X = ldiv(T + off[T_XI] + 2 * e);
       iv dd = mul(P.g, X);
       iv h = mul(mul(ldiv(T + off[T_SN] + 2 * e), P.u), mk(k[8 + n + 2 * j], k[8 + n + 2 * j + 1]));
@@ -598,7 +682,7 @@ __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, Child
       return kkt_prune(dd, X, D.dom[2 * j], D.dom[2 * j + 1]);
     }
     default: {  // FAM_PRODCOS
-      long long e = eidx(D, C, code, j);
+      long long e = eidx(D, C, pc, j);
       iv q = div(P.g, ldiv(T + off[T_CR] + 2 * e));
       q = mul(mul(q, ldiv(T + off[T_SNA] + 2 * e)), mk(k[4 + 2 * j], k[4 + 2 * j + 1]));
       q = add(q, ldiv(T + off[T_XD2] + 2 * e));
@@ -609,11 +693,11 @@ __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, Child
 }
 
 // 1 when the generalized KKT test rules the child out
-__device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long code) {
+__device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long pc) {
   DerivPre P;
-  if (deriv_pre(D, T, C, code, &P)) return 0;
+  if (deriv_pre(D, T, C, pc, &P)) return 0;
   for (int j = 0; j < D.n; ++j)
-    if (deriv_coord(D, T, C, code, j, P)) return 1;
+    if (deriv_coord(D, T, C, pc, j, P)) return 1;
   return 0;
 }
 
