@@ -19,6 +19,7 @@ ERRORS = {
     -10: "request exceeds the fixed scratch of gpugo_eval_children_static",
 }
 CERTIFIED, FINISHED, ITER_LIMIT = 1, 2, 3
+CAND_AUTO, CAND_WARP, CAND_LANE = 0, 1, 2
 ERR_BUSY = -7
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -58,7 +59,7 @@ class Trace(ctypes.Structure):
 class EngineCfg(ctypes.Structure):
     _fields_ = [
         ("max_slots", ctypes.c_int32), ("threads", ctypes.c_int32), ("arena_bytes", ctypes.c_int64),
-        ("wait_timeout_s", ctypes.c_double), ("blocks_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("wait_timeout_s", ctypes.c_double), ("blocks_per_sm", ctypes.c_int32), ("cand_mode", ctypes.c_int32),
     ]
 
 

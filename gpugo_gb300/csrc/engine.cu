@@ -52,7 +52,7 @@ constexpr long long POOL_BLOCK_MAX = 1LL << 12;
 
 // Candidate queue entry: slot << 32 | child code, LB bits, six intermediates of the
 // value code list reused by the derivative test.
-constexpr int CAND_WORDS = 8;
+constexpr int CAND_WORDS = 4;   // key, LB, two words of value-pass intermediates
 
 // Shared memory per block holding one instance's term tables during phase B.
 constexpr int SMEM_TAB_BYTES = 96 * 1024;
@@ -115,8 +115,9 @@ struct KArgs {
   int* idsE;                  // [max_slots] big-pool instances (grid-wide path)
   long long* prefD;           // [max_slots + 1] pool tiles prefix of big instances
   unsigned long long* queue;  // [max_slots] ready queue entries: epoch << 32 | slot
-  unsigned long long* cands;  // [cand_cap][2] candidate queue: slot << 32 | code, lb bits
+  unsigned long long* cands;  // [cand_cap][CAND_WORDS] candidate queue: slot << 32 | code, lb bits, aux
   long long cand_cap;
+  int cand_mode;              // GPUGO_CAND_AUTO / _WARP / _LANE
   int max_slots;
   long long max_iters;        // iterations in this launch (<= 0: until idle)
   unsigned long long timeout_ns;
@@ -659,7 +660,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   double bv = 0.0;
   int bj = J_NONE;
   for (int j = lane; j < D.S; j += 32) {
-    double v = samp_one(D, T, C, pc, j);
+    double v = samp_one(D, T, C, pc, j, ub);
     if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
   }
 #pragma unroll
@@ -686,9 +687,14 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   ub = shfl_d(ub, 0);
   if (lb > ub) return false;
   DerivPre P;
+  P.g = mk(0.0, 0.0);
+  P.u = P.g;
   int skip = 0;
   if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS) {
-    if (lane == 0) skip = aux ? deriv_pre_aux(D, T, C, pc, aux, &P) : deriv_pre(D, T, C, pc, &P);
+    if (lane == 0) {
+      if (aux && D.family == FAM_PRODCOS) deriv_pre_aux(aux, &P);
+      else skip = deriv_pre(D, T, C, pc, &P);
+    }
     skip = __shfl_sync(0xffffffffu, skip, 0);
     P.g.lo = shfl_d(P.g.lo, 0); P.g.hi = shfl_d(P.g.hi, 0);
     P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
@@ -732,27 +738,30 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   int j = 0;
   for (; j + 4 <= D.S; j += 4) {
     double v[4];
-    samp_multi<4>(D, T, C, pc, j, v);
+    samp_multi<4>(D, T, C, pc, j, v, ub);
 #pragma unroll
     for (int q = 0; q < 4; ++q) consider(v[q], j + q);
   }
   if (j + 2 <= D.S) {
     double v[2];
-    samp_multi<2>(D, T, C, pc, j, v);
+    samp_multi<2>(D, T, C, pc, j, v, ub);
     consider(v[0], j);
     consider(v[1], j + 1);
     j += 2;
   }
   if (j < D.S) {
     double v[1];
-    samp_multi<1>(D, T, C, pc, j, v);
+    samp_multi<1>(D, T, C, pc, j, v, ub);
     consider(v[0], j);
   }
   ub = atomic_ub_read(&st.ub);
   if (flt(ub, lb)) return 2;
   DerivPre P;
-  if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS)
-    if (deriv_pre_aux(D, T, C, pc, aux, &P)) return 3;
+  if (D.family == FAM_EXPSQRT) {
+    if (deriv_pre(D, T, C, pc, &P)) return 3;
+  } else if (D.family == FAM_PRODCOS) {
+    deriv_pre_aux(aux, &P);
+  }
   for (int jj = 0; jj < D.n; ++jj)
     if (deriv_coord(D, T, C, pc, jj, P)) return 2;
   return 3;
@@ -805,7 +814,7 @@ __device__ void phase_bound(const KArgs& a) {
     if (valid) hint = k;
     int s = valid ? a.idsA[k] : -1;
     double lb = 0.0;
-    double aux[6] = {0, 0, 0, 0, 0, 0};
+    double aux[2] = {0, 0};
     unsigned long long code = 0;
     bool cand = false;
     if (valid) {
@@ -817,9 +826,8 @@ __device__ void phase_bound(const KArgs& a) {
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
       const unsigned long long pc = pack_code(D, C.gsz, code);
-      lb = child_lb(D, T, C, pc, aux);
+      lb = child_lb(D, T, C, pc, aux, ord_val(st.ub_start));
       cand = !flt(ord_val(st.ub_start), lb);
-      if (cand && D.family == FAM_EXPSQRT) expsqrt_aux(D, T, C, pc, aux);
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
     if (!cm) continue;
@@ -849,7 +857,7 @@ __device__ void phase_bound(const KArgs& a) {
         e[0] = ((unsigned long long)s << 32) | code;
         e[1] = (unsigned long long)__double_as_longlong(lb);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) e[2 + q] = (unsigned long long)__double_as_longlong(aux[q]);
+        for (int q = 0; q < 2; ++q) e[2 + q] = (unsigned long long)__double_as_longlong(aux[q]);
       }
       // per-instance queued counts
       unsigned int act = cm;
@@ -869,9 +877,9 @@ __device__ void phase_bound(const KArgs& a) {
         int cs = __shfl_sync(0xffffffffu, s, b);
         unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
         double cl = shfl_d(lb, b);
-        double ca[6];
+        double ca[2];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) ca[q] = shfl_d(aux[q], b);
+        for (int q = 0; q < 2; ++q) ca[q] = shfl_d(aux[q], b);
         bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca);
         if (lane == b) keep = kk;
       }
@@ -896,7 +904,10 @@ __device__ void prefill_ready(const KArgs& a) {
     long long c = tot / (2 * W);
     // a warp per candidate while there are fewer candidates than warps x 32;
     // beyond that each lane takes its own candidate, 32 or 64 per claim
-    a.ctl->cand_claim = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 8 ? 8 : c));
+    long long k = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 8 ? 8 : c));
+    if (a.cand_mode == GPUGO_CAND_WARP && k >= 32) k = 8;
+    if (a.cand_mode == GPUGO_CAND_LANE && k < 32) k = 32;
+    a.ctl->cand_claim = k;
     a.ctl->seed_on = (tot > 4 * W) ? 1 : 0;
     a.ctl->cand_tail = (unsigned long long)tot;
   }
@@ -924,10 +935,11 @@ __device__ void phase_seed(const KArgs& a) {
     C.c0 = st.cyc - 1;
     C.gsz = group_size(D.n, D.group, st.cyc);
     const unsigned long long pc = pack_code(D, C.gsz, code);
+    const double cut = atomic_ub_read(&st.ub);
     double bv = 0.0;
     int bj = J_NONE;
     for (int j = lane; j < D.S; j += 32) {
-      double v = samp_one(D, T, C, pc, j);
+      double v = samp_one(D, T, C, pc, j, cut);
       if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1012,9 +1024,9 @@ __device__ void phase_candidates(const KArgs& a) {
           s = (int)(en[0] >> 32);
           unsigned long long code = en[0] & 0xffffffffULL;
           double lb = __longlong_as_double((long long)en[1]);
-          double aux[6];
+          double aux[2];
 #pragma unroll
-          for (int t = 0; t < 6; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
+          for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
           int rr = thread_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
           keep = rr & 1;
           sampled = rr & 2;
@@ -1042,9 +1054,9 @@ __device__ void phase_candidates(const KArgs& a) {
       const unsigned long long* en = a.cands + CAND_WORDS * q;
       unsigned long long w0 = en[0];
       double lb = __longlong_as_double((long long)en[1]);
-      double aux[6];
+      double aux[2];
 #pragma unroll
-      for (int t = 0; t < 6; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
+      for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
       int s = (int)(w0 >> 32);
       unsigned long long code = w0 & 0xffffffffULL;
       bool keep = warp_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
@@ -1332,6 +1344,7 @@ struct Arena {
 struct gpugo_engine {
   int dev = 0, nsm = 0, threads = 256, blocks = 0;
   int max_slots = 0;
+  int cand_mode = 0;
   double timeout_s = 60.0;
   cudaStream_t stream = nullptr;
   Desc* d_desc = nullptr;
@@ -1752,6 +1765,7 @@ int gpugo_instance_bytes(const gpugo_spec* spec, int64_t* bytes_out) {
 
 int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
   if (!cfg || !out || cfg->max_slots < 1 || cfg->max_slots > 8192 || cfg->arena_bytes <= 0) return GPUGO_ERR_INVALID;
+  if (cfg->cand_mode < GPUGO_CAND_AUTO || cfg->cand_mode > GPUGO_CAND_LANE) return GPUGO_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
   gpugo_engine* E = new (std::nothrow) gpugo_engine();
@@ -1760,6 +1774,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
   E->threads = cfg->threads > 0 ? cfg->threads : 256;
   if (E->threads != 256 && E->threads != 512) { delete E; return GPUGO_ERR_INVALID; }
   E->timeout_s = cfg->wait_timeout_s > 0 ? cfg->wait_timeout_s : 60.0;
+  E->cand_mode = cfg->cand_mode;
   int rc = GPUGO_OK;
   do {
     if ((rc = cuda_err(cudaGetDevice(&E->dev)))) break;
@@ -1915,6 +1930,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.queue = E->d_queue;
   a.cands = E->d_cands;
   a.cand_cap = E->cand_cap;
+  a.cand_mode = E->cand_mode;
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);

@@ -407,17 +407,53 @@ __device__ __forceinline__ double expsqrt_hi(const double* k, double s_hi, doubl
   return __dadd_ru(__dadd_ru(t_hi, -u_lo), k[5]);
 }
 
+// Screening bounds.  exp_upper(x) is an upper bound of exp(x) widened by 2^-13:
+// y = RN32(x log2 e) is within 2^-18 of x log2 e for |x| < 80, ex2.approx.f32 is
+// within 2^-21 of 2^y, so e = 2^y >= exp(x) (1 - 2^-18) and RU(e (1 + 2^-12)) >=
+// exp(x) (1 + 2^-13).  Our exp is within two units in the last place, so exp_hi and
+// exp_lo (our exp moved outward by two units) never exceed it.  Replacing the
+// exponentials of expsqrt_lo / expsqrt_hi by exp_upper, with every other operation
+// unchanged and directed the same way (A > 0, and every step is monotone in the
+// replaced value), gives a value that is never above the exact bound.  Such a value
+// already above the UB settles a comparison without the exact exponentials.
+__device__ __forceinline__ bool exp_upper(double x, double* out) {
+  if (!(flt(-80.0, x) && flt(x, 80.0))) return false;   // also NaN
+  const float y = __double2float_rn(__dmul_rn(x, 0x1.71547652b82fep+0));
+  float e;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(y));
+  *out = __dmul_ru((double)e, 1.0 + 0x1p-12);
+  return true;
+}
+// lower bound of expsqrt_lo(k, s_lo, c_hi); false when it cannot bound
+__device__ __forceinline__ bool expsqrt_lo_bound(const double* k, double s_lo, double c_hi, double* out) {
+  double r_lo = sqrt_lo(mulk_lo(s_lo, k[2], k[3]));
+  double E, U;
+  if (!exp_upper(__dmul_ru(r_lo, -k[1]), &E) || !exp_upper(mulk_hi(c_hi, k[2], k[3]), &U)) return false;
+  *out = __dadd_rd(__dadd_rd(__dmul_rd(E, -k[0]), -U), k[4]);
+  return true;
+}
+// lower bound of expsqrt_hi(k, s_hi, c_lo); false when it cannot bound
+__device__ __forceinline__ bool expsqrt_hi_bound(const double* k, double s_hi, double c_lo, double* out) {
+  double r_hi = sqrt_hi(mulk_hi(s_hi, k[2], k[3]));
+  double E, U;
+  if (!exp_upper(__dmul_rd(r_hi, -k[1]), &E) || !exp_upper(mulk_lo(c_lo, k[2], k[3]), &U)) return false;
+  *out = __dadd_ru(__dadd_ru(__dmul_ru(E, -k[0]), -U), k[5]);
+  return true;
+}
+
 // Per-child functions take packed child codes (pack_code).
 __device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned long long pc, int i) {
   return (long long)i * D.wid + digit(D, C.c0, C.gsz, pc, i);
 }
 
-// aux (may be null) receives the intermediates the derivative test reuses:
-// expsqrt E = exp(-B r), r, u (six doubles); prodcos the cosine product (two).
+// aux (may be null) receives the product-cosine value product (two doubles),
+// which the derivative test reuses.  With a finite cut the function may return,
+// instead of the LB, a lower bound of it that is already above cut (the caller
+// only compares it with cut).
 // Two independent reductions over the coordinates share one loop; each keeps
 // the reference's left-to-right order.
 __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
-                                        double* aux = nullptr) {
+                                        double* aux = nullptr, double cut = INF_D) {
   const int n = D.n, w = D.wid;
   const double* k = D.cst;
   const long long* off = D.t_off;
@@ -446,6 +482,8 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
         s_lo = __dadd_rd(s_lo, T[off[T_SQ] + 2 * e]);
         c_hi = __dadd_ru(c_hi, T[off[T_CS] + 2 * e + 1]);
       }
+      double b;
+      if (expsqrt_lo_bound(k, s_lo, c_hi, &b) && flt(cut, b)) return b;
       return expsqrt_lo(k, s_lo, c_hi);
     }
     case FAM_PRODCOS: {
@@ -465,10 +503,12 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
 
 // Upper bounds of f at sample points j0 .. j0+M-1 of the child: M passes of the
 // sample code list run side by side in one loop over the coordinates, each in
-// the reference's order, so each value equals that of its own pass.
+// the reference's order, so each value equals that of its own pass.  With a
+// finite cut a value may be replaced by a lower bound of it that is not below cut
+// (callers only look for values below cut).
 template <int M>
 __device__ __forceinline__ void samp_multi(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
-                                           double* v) {
+                                           double* v, double cut = INF_D) {
   const int n = D.n, w = D.wid, S = D.S;
   const double* k = D.cst;
   const long long* off = D.t_off;
@@ -519,7 +559,10 @@ __device__ __forceinline__ void samp_multi(const Desc& D, const double* T, Child
         }
       }
 #pragma unroll
-      for (int q = 0; q < M; ++q) v[q] = expsqrt_hi(k, s_hi[q], c_lo[q]);
+      for (int q = 0; q < M; ++q) {
+        double b;
+        v[q] = (expsqrt_hi_bound(k, s_hi[q], c_lo[q], &b) && !flt(b, cut)) ? b : expsqrt_hi(k, s_hi[q], c_lo[q]);
+      }
       return;
     }
     default: {  // FAM_PRODCOS
@@ -545,9 +588,10 @@ __device__ __forceinline__ void samp_multi(const Desc& D, const double* T, Child
 }
 
 // upper bound of f at sample point j of the child (one pass of the sample code list)
-__device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j) {
+__device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j,
+                                        double cut = INF_D) {
   double v;
-  samp_multi<1>(D, T, C, pc, j, &v);
+  samp_multi<1>(D, T, C, pc, j, &v, cut);
   return v;
 }
 
@@ -613,49 +657,11 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
   return 0;
 }
 
-// expsqrt intermediates for a candidate: E = exp(-B r), r, u as full intervals
-// (the value pass computes one side of each only).
-__device__ __noinline__ void expsqrt_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
-                                         double* aux) {
-  const int n = D.n;
-  const double* k = D.cst;
-  const long long* off = D.t_off;
-  iv s = mk(0.0, 0.0), c = mk(0.0, 0.0);
-  for (int i = 0; i < n; ++i) {
-    const long long e = eidx(D, C, pc, i);
-    s = add(s, ldiv(T + off[T_SQ] + 2 * e));
-    c = add(c, ldiv(T + off[T_CS] + 2 * e));
-  }
-  iv inv_n = mk(k[2], k[3]);
-  iv r = sqrt_iv(mul(s, inv_n));
-  iv E = exp_iv(times(r, -k[1]));
-  iv u = exp_iv(mul(c, inv_n));
-  aux[0] = E.lo; aux[1] = E.hi; aux[2] = r.lo; aux[3] = r.hi; aux[4] = u.lo; aux[5] = u.hi;
-}
-
-// The same scalars from the value pass's intermediates.  expsqrt: the value code
-// list computes r = sqrt(mean x^2), E = exp(-B r) and u = exp(mean cos) exactly as
-// the derivative code list does.  prodcos: the value product starts from [-1,-1]
-// and the derivative product from [1,1]; interval multiplication commutes with
-// negation bit for bit, so P is the negated value product.
-__device__ __forceinline__ int deriv_pre_aux(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
-                                             const double* aux, DerivPre* P) {
-  const int n = D.n;
-  const double* k = D.cst;
-  if (D.family == FAM_EXPSQRT) {
-    const unsigned char* zb = (const unsigned char*)(T + D.t_off[T_ZB]);
-    int origin = 1;
-    for (int i = 0; i < n; ++i)
-      if (!zb[eidx(D, C, pc, i)]) { origin = 0; break; }
-    if (origin) return 1;
-    iv E = mk(aux[0], aux[1]), r = mk(aux[2], aux[3]);
-    P->g = mul(div(E, r), mk(k[6], k[7]));
-    P->u = mk(aux[4], aux[5]);
-  } else if (D.family == FAM_PRODCOS) {
-    P->g = mk(-aux[1], -aux[0]);
-  }
-  return 0;
-}
+// The product-cosine derivative scalar from the value pass: the value product
+// starts from [-1,-1] and the derivative product from [1,1]; interval
+// multiplication commutes with negation bit for bit, so P is the negated value
+// product (griewank50.py:383-396).
+__device__ __forceinline__ void deriv_pre_aux(const double* aux, DerivPre* P) { P->g = mk(-aux[1], -aux[0]); }
 
 // generalized KKT test of coordinate j (rastrigin50.py:365-370); 1 = rule out
 __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,

@@ -33,6 +33,7 @@ __device__ __forceinline__ double u2d(uint64_t u) { return __longlong_as_double(
 
 constexpr uint64_t ABS_MASK = 0x7fffffffffffffffULL;
 constexpr uint64_t INF_BITS = 0x7ff0000000000000ULL;
+constexpr double INF_D = __builtin_huge_val();
 
 // Comparisons run on the integer bit patterns (an FP64 compare costs as much as
 // an FP64 add on this part); each one returns exactly what the IEEE comparison
@@ -232,15 +233,21 @@ __device__ __forceinline__ iv mul4(iv a, iv b) {
 // extreme products are fixed by the signs, so only those are formed (a quarter of
 // the FP64 work).  The value returned equals the full form's; only the sign of a
 // zero result can differ, which no comparison here distinguishes.
+// The four sign cases, tried in the order (a>=0, b>=0), (a<=0, b<=0), (a>=0, b<=0),
+// (a<=0, b>=0), take the lower bound from (a.lo or a.hi) x (b.lo or b.hi) and the
+// upper bound from the other two endpoints; the operands are selected without
+// branches so that lanes with different sign cases stay converged.
 __device__ __forceinline__ iv mul(iv a, iv b) {
   if (!(finite_(a.lo) && finite_(a.hi) && finite_(b.lo) && finite_(b.hi))) return mul4(a, b);
   const bool a_nn = !fneg(a.lo), a_np = !fpos(a.hi);   // a >= 0, a <= 0
   const bool b_nn = !fneg(b.lo), b_np = !fpos(b.hi);
-  if (a_nn && b_nn) return mk(__dmul_rd(a.lo, b.lo), __dmul_ru(a.hi, b.hi));
-  if (a_np && b_np) return mk(__dmul_rd(a.hi, b.hi), __dmul_ru(a.lo, b.lo));
-  if (a_nn && b_np) return mk(__dmul_rd(a.hi, b.lo), __dmul_ru(a.lo, b.hi));
-  if (a_np && b_nn) return mk(__dmul_rd(a.lo, b.hi), __dmul_ru(a.hi, b.lo));
-  return mul4(a, b);
+  const bool c1 = a_nn && b_nn, c2 = a_np && b_np, c3 = a_nn && b_np, c4 = a_np && b_nn;
+  if (!(c1 || c2 || c3 || c4)) return mul4(a, b);
+  const bool lo_a = c1 || (!c2 && !c3 && c4);   // lower bound takes a.lo (cases 1, 4)
+  const bool lo_b = c1 || (!c2 && c3);          // lower bound takes b.lo (cases 1, 3)
+  const double x1 = lo_a ? a.lo : a.hi, x2 = lo_a ? a.hi : a.lo;
+  const double y1 = lo_b ? b.lo : b.hi, y2 = lo_b ? b.hi : b.lo;
+  return mk(__dmul_rd(x1, y1), __dmul_ru(x2, y2));
 }
 
 __device__ __forceinline__ iv entire() { return mk(-u2d(INF_BITS), u2d(INF_BITS)); }

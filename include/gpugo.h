@@ -163,8 +163,15 @@ typedef struct gpugo_engine_cfg {
     int64_t arena_bytes;        /* device memory for pools, tables and parent tables */
     double  wait_timeout_s;     /* bound of every device-side wait (0: 60 s) */
     int32_t blocks_per_sm;      /* 0: occupancy maximum */
-    int32_t reserved;
+    int32_t cand_mode;          /* candidate scheduling, GPUGO_CAND_* (results are the same in every mode) */
 } gpugo_engine_cfg;
+
+/* Candidate children (LB not above the UB) are sampled and KKT-tested either by
+   a whole warp each (sample points and coordinates across the lanes: short
+   queues) or by one lane each (long queues).  AUTO picks by queue length. */
+#define GPUGO_CAND_AUTO 0
+#define GPUGO_CAND_WARP 1
+#define GPUGO_CAND_LANE 2
 
 typedef struct gpugo_done {
     int64_t ticket;

@@ -150,6 +150,43 @@ def test_engine_batch_matches_single(oracle_lib):
         assert _same(a.boxes, b.boxes)
 
 
+WIDE = [
+    ("cosquad40", lambda: P.instance(P.COSQUAD, 40, 21, 1e-6)),
+    ("chained30", lambda: P.instance(P.CHAINED, 30, 22, 1e-6)),
+    ("expsqrt20", lambda: P.instance(P.EXPSQRT, 20, 18, 1e-6)),
+    ("expsqrt32", lambda: P.instance(P.EXPSQRT, 32, 17, 1e-4)),
+    ("prodcos24", lambda: P.instance(P.PRODCOS, 24, 19, 1e-6)),
+]
+
+
+@pytest.mark.parametrize("name,make", WIDE, ids=[c[0] for c in WIDE])
+def test_solve_trace_parity_wide(oracle_lib, name, make):
+    """Split groups that cycle through the coordinates (n > group)."""
+    p = make()
+    p.max_iter = 3000
+    rg, ro = _compare_solves(p, oracle_lib, box_cap=64)
+    assert rg.status == G.CERTIFIED
+
+
+@pytest.mark.parametrize("mode", [G._lib.CAND_WARP, G._lib.CAND_LANE], ids=["warp", "lane"])
+def test_engine_batch_matches_oracle(oracle_lib, mode):
+    """A batch in each candidate scheduling mode against the oracle, trace for trace."""
+    probs = [make() for _, make in WIDE + CFGS]
+    for p in probs:
+        p.max_iter = 3000
+    ros = [oracle_lib.solve(p, box_cap=16, trace_cap=100000) for p in probs]
+    with G.Engine(max_slots=len(probs), arena_bytes=4 << 30, cand_mode=mode) as eng:
+        tickets = [eng.submit(p, box_cap=16, trace_cap=100000) for p in probs]
+        eng.run(0)
+        done = dict(eng.poll())
+    for t, p, ro in zip(tickets, probs, ros):
+        rg = done[t]
+        assert (rg.iterations, rg.lb, rg.ub, rg.pool_size) == (ro.iterations, ro.lb, ro.ub, ro.pool_size), p.tag
+        for k in ("ub", "n_surv", "pool", "sel"):
+            assert _same(rg.trace[k], ro.trace[k]), (p.tag, k)
+        assert _same(rg.box_lbs, ro.box_lbs), p.tag
+
+
 def test_pool_overflow_reports_error():
     """Host-side fault injection: a pool too small for the survivors."""
     p = P.config2()
