@@ -123,7 +123,7 @@ struct KArgs {
   unsigned long long timeout_ns;
   unsigned long long* stamps; // optional: %globaltimer at each barrier release
   long long stamp_cap;
-  unsigned long long* bstamps; // optional: per block, per iteration: 6 timestamps inside phases A and B
+  unsigned long long* bstamps; // optional: per block, per iteration: BSTAMP_W values inside phases A and B
   long long bstamp_iters;
   long long cur_it;            // iteration index for bstamps (set by the kernel loop)
 };
@@ -134,10 +134,14 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-__device__ __forceinline__ void bstamp(const KArgs& a, int k) {
+// per block and iteration: 0/1 table phase start/end, 2/3 pass 1 start/end,
+// 4 pass 2 claims end, 5 list updates end, 6 pass 2 claims start, 7 candidates claimed
+constexpr int BSTAMP_W = 8;
+__device__ __forceinline__ void bstamp_val(const KArgs& a, int k, unsigned long long v) {
   if (a.bstamps && threadIdx.x == 0 && a.cur_it < a.bstamp_iters)
-    a.bstamps[(a.cur_it * gridDim.x + blockIdx.x) * 6 + k] = gtimer();
+    a.bstamps[(a.cur_it * gridDim.x + blockIdx.x) * BSTAMP_W + k] = v;
 }
+__device__ __forceinline__ void bstamp(const KArgs& a, int k) { bstamp_val(a, k, gtimer()); }
 
 __device__ __forceinline__ double atomic_ub_read(const unsigned long long* p) {
   return ord_val(*(volatile const unsigned long long*)p);
@@ -646,8 +650,9 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 // One candidate child (its LB is not above the running UB) processed by the whole
 // warp: its sample points spread over the lanes, then its KKT coordinates.
 // Returns true when the child survives.  Every lane returns the same value.
+// pfx (may be null): the instance's shared sample prefixes.
 __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
-                               const double* aux = nullptr) {
+                               const double* aux, const double* pfx) {
   const int lane = threadIdx.x & 31;
   const Desc& D = a.desc[s];
   State& st = a.st[s];
@@ -660,7 +665,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   double bv = 0.0;
   int bj = J_NONE;
   for (int j = lane; j < D.S; j += 32) {
-    double v = samp_one(D, T, C, pc, j, ub);
+    double v = samp_one(D, T, C, pc, j, ub, pfx);
     if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
   }
 #pragma unroll
@@ -710,7 +715,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
 // over all of them is the same value the per-child minimum would give).
 // returns bit 0: the child survives, bit 1: its samples were evaluated
 __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
-                                const double* aux) {
+                                const double* aux, const double* pfx) {
   const Desc& D = a.desc[s];
   State& st = a.st[s];
   ChildCtx C;
@@ -738,20 +743,20 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   int j = 0;
   for (; j + 4 <= D.S; j += 4) {
     double v[4];
-    samp_multi<4>(D, T, C, pc, j, v, ub);
+    samp_multi<4>(D, T, C, pc, j, v, ub, pfx);
 #pragma unroll
     for (int q = 0; q < 4; ++q) consider(v[q], j + q);
   }
   if (j + 2 <= D.S) {
     double v[2];
-    samp_multi<2>(D, T, C, pc, j, v, ub);
+    samp_multi<2>(D, T, C, pc, j, v, ub, pfx);
     consider(v[0], j);
     consider(v[1], j + 1);
     j += 2;
   }
   if (j < D.S) {
     double v[1];
-    samp_multi<1>(D, T, C, pc, j, v, ub);
+    samp_multi<1>(D, T, C, pc, j, v, ub, pfx);
     consider(v[0], j);
   }
   ub = atomic_ub_read(&st.ub);
@@ -880,7 +885,7 @@ __device__ void phase_bound(const KArgs& a) {
         double ca[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) ca[q] = shfl_d(aux[q], b);
-        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca);
+        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
         if (lane == b) keep = kk;
       }
       if (keep) append_survivor(a, s, code, lb);
@@ -916,6 +921,8 @@ __device__ void prefill_ready(const KArgs& a) {
 // Seed pass (long candidate queues): one warp per instance evaluates the samples
 // of its lowest-LB candidate and lowers the UB with them.  The child is processed
 // again in pass 2; the UB stays the minimum over the same set of sample values.
+// The same warp stores the instance's shared sample prefixes (samp_prefix), which
+// pass 2 then starts every candidate's sample passes from.
 __device__ void phase_seed(const KArgs& a) {
   extern __shared__ double s_tab[];
   const int si = stage_tables(a);
@@ -936,10 +943,13 @@ __device__ void phase_seed(const KArgs& a) {
     C.gsz = group_size(D.n, D.group, st.cyc);
     const unsigned long long pc = pack_code(D, C.gsz, code);
     const double cut = atomic_ub_read(&st.ub);
+    const int sh = samp_shared(D, C);
     double bv = 0.0;
     int bj = J_NONE;
     for (int j = lane; j < D.S; j += 32) {
-      double v = samp_one(D, T, C, pc, j, cut);
+      SAcc r = (sh > 0) ? samp_prefix(D, T, C, j, D.tab + D.t_off[T_PFX]) : sacc_init(D);
+      samp_run<1>(D, T, C, pc, j, sh, samp_terms(D), &r);
+      double v = samp_value(D, r, cut);
       if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -972,16 +982,22 @@ __device__ __forceinline__ void count_done(const KArgs& a, int s, long long n) {
 __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ double s_tab[];
   __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
+  __shared__ unsigned long long s_claimed;
   const int si = stage_tables(a);
+  if (threadIdx.x == 0) s_claimed = 0;
+  __syncthreads();
+  bstamp(a, 6);
   const int lane = threadIdx.x & 31;
   const unsigned long long tot = a.ctl->cand_tail;
   const unsigned long long K = (unsigned long long)a.ctl->cand_claim;
+  const bool pfx_on = a.ctl->seed_on != 0;   // the seed pass stored the shared sample prefixes
   for (;;) {
     unsigned long long h = 0;
     if (lane == 0) h = atomicAdd(&a.ctl->cand_head, K);
     h = __shfl_sync(0xffffffffu, h, 0);
     if (h >= tot) break;
     const unsigned long long e = min(tot, h + K);
+    if (a.bstamps && lane == 0) atomicAdd(&s_claimed, e - h);
     if (K >= 32) {
       // One candidate per lane.  The claim is filtered first (LB against the
       // current UB) and the survivors are packed densely, so that no lane idles
@@ -1027,7 +1043,8 @@ __device__ void phase_candidates(const KArgs& a) {
           double aux[2];
 #pragma unroll
           for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
-          int rr = thread_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
+          const double* T = (s == si) ? s_tab : a.desc[s].tab;
+          int rr = thread_candidate(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
           keep = rr & 1;
           sampled = rr & 2;
           if (keep) append_survivor(a, s, code, lb);
@@ -1059,7 +1076,8 @@ __device__ void phase_candidates(const KArgs& a) {
       for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
       int s = (int)(w0 >> 32);
       unsigned long long code = w0 & 0xffffffffULL;
-      bool keep = warp_candidate(a, s, (s == si) ? s_tab : a.desc[s].tab, code, lb, aux);
+      const double* T = (s == si) ? s_tab : a.desc[s].tab;
+      bool keep = warp_candidate(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
       if (keep && lane == 0) append_survivor(a, s, code, lb);
       if (lane == 0) {
         if (s != acc_s && acc_s >= 0) { count_done(a, acc_s, acc_n); acc_n = 0; }
@@ -1072,6 +1090,7 @@ __device__ void phase_candidates(const KArgs& a) {
   }
   __syncthreads();
   bstamp(a, 4);
+  bstamp_val(a, 7, s_claimed);
   drain_queue(a);
   __syncthreads();
   bstamp(a, 5);
@@ -1460,10 +1479,11 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
       break;
     default:
       put(T_CR, 2 * n * w); put(T_SQ4, 2 * n * w); put(T_SNA, 2 * n * w); put(T_XD2, 2 * n * w);
-      put(T_XI4, 2 * n * w); put(T_CRS, 2 * n * w * S); put(T_SQS4, 2 * n * w * S);
+      put(T_XI4, 2 * n * w); put(T_CRS, 2 * n * w * S); put(T_SQS4, 2 * n * w * S); put(T_RCP4, 2 * n * w);
       L->a_items = n * w * (S + 1);
       break;
   }
+  put(T_PFX, 3 * S);
   L->tab = o;
   const int64_t M = max_children(s);
   L->pool_cap = s->pool_cap > 0 ? s->pool_cap : std::max<int64_t>(1 << 19, std::min<int64_t>(16 * M, 1 << 26));
@@ -1806,7 +1826,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
       E->stamp_cap = 8 * 65536;
       if ((rc = cuda_err(cudaMalloc(&E->d_stamps, 8 * E->stamp_cap)))) break;
       E->bstamp_iters = 64;
-      if ((rc = cuda_err(cudaMalloc(&E->d_bstamps, 8 * 6 * (size_t)E->bstamp_iters * E->blocks)))) break;
+      if ((rc = cuda_err(cudaMalloc(&E->d_bstamps, 8 * BSTAMP_W * (size_t)E->bstamp_iters * E->blocks)))) break;
     }
     if ((rc = cuda_err(cudaEventCreate(&E->ev0)))) break;
     if ((rc = cuda_err(cudaEventCreate(&E->ev1)))) break;
@@ -1964,12 +1984,12 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
       fclose(f);
     }
     long long ki = std::min<long long>(c.iters, E->bstamp_iters);
-    std::vector<unsigned long long> bs(6 * ki * E->blocks);
+    std::vector<unsigned long long> bs(BSTAMP_W * ki * E->blocks);
     CK(cudaMemcpy(bs.data(), E->d_bstamps, 8 * bs.size(), cudaMemcpyDeviceToHost));
     std::string bp = std::string(E->stamp_path) + ".blocks";
     if (FILE* f = fopen(bp.c_str(), "a")) {
-      fprintf(f, "run blocks=%d iters=%lld\n", E->blocks, ki);
-      for (size_t i = 0; i < bs.size(); ++i) fprintf(f, "%llu%c", bs[i], (i % 6 == 5) ? '\n' : ' ');
+      fprintf(f, "run blocks=%d iters=%lld width=%d\n", E->blocks, ki, BSTAMP_W);
+      for (size_t i = 0; i < bs.size(); ++i) fprintf(f, "%llu%c", bs[i], (i % BSTAMP_W == BSTAMP_W - 1) ? '\n' : ' ');
       fclose(f);
     }
   }

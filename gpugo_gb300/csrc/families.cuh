@@ -28,8 +28,9 @@ constexpr double E_HI = 0x1.5bf0a8b14576ap+1;     // next double, above e
 enum {
   T_LO = 0, T_SHI, T_PRB,                               // cosquad / chained
   T_SQ = 0, T_CS, T_XI, T_SN, T_ZB, T_SQS, T_CSS,       // expsqrt
-  T_CR = 0, T_SQ4, T_SNA, T_XD2, T_XI4, T_CRS, T_SQS4,  // prodcos
-  T_NOFF = 8
+  T_CR = 0, T_SQ4, T_SNA, T_XD2, T_XI4, T_CRS, T_SQS4, T_RCP4,  // prodcos
+  T_PFX = 8,                                            // shared sample prefixes (all families)
+  T_NOFF = 9
 };
 
 // Derived-constant offsets (doubles) within an instance's constant region.
@@ -341,7 +342,9 @@ __device__ void build_item(const Desc& D, const double* pbox, const double* pw, 
       long long e = (long long)i * w + d;
       if (j == S) {
         iv a = mul(X, RSQ);
-        stiv(T + off[T_CR] + 2 * e, cos_iv(a));
+        iv cr = cos_iv(a);
+        stiv(T + off[T_CR] + 2 * e, cr);
+        stiv(T + off[T_RCP4] + 2 * e, div_recip(cr));
         stiv(T + off[T_SQ4] + 2 * e, sqr(X));
         stiv(T + off[T_SNA] + 2 * e, sin_iv(a));
         stiv(T + off[T_XD2] + 2 * e, mul(X, mk(k[2], k[3])));
@@ -501,97 +504,147 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
   return 0.0;
 }
 
-// Upper bounds of f at sample points j0 .. j0+M-1 of the child: M passes of the
-// sample code list run side by side in one loop over the coordinates, each in
-// the reference's order, so each value equals that of its own pass.  With a
-// finite cut a value may be replaced by a lower bound of it that is not below cut
-// (callers only look for values below cut).
+// Running values of one pass of the sample code list: cosquad / chained the sum
+// (a); expsqrt the sum of squares (a, upper side) and of cosines (b, lower side);
+// prodcos the cosine product [a, b] and the sum of squares (c, upper side).
+struct SAcc {
+  double a, b, c;
+};
+
+__device__ __forceinline__ SAcc sacc_init(const Desc& D) {
+  SAcc r;
+  r.a = r.b = (D.family == FAM_PRODCOS) ? -1.0 : 0.0;
+  r.c = 0.0;
+  return r;
+}
+
+// number of terms of the sample reduction, and how many of them (those of
+// coordinates before the split group, whose digit is 0 in every child) are the
+// same for all children of the parent
+__device__ __forceinline__ int samp_terms(const Desc& D) { return D.family == FAM_CHAINED ? D.n - 1 : D.n; }
+__device__ __forceinline__ int samp_shared(const Desc& D, ChildCtx C) {
+  return D.family == FAM_CHAINED ? (C.c0 > 0 ? C.c0 - 1 : 0) : C.c0;
+}
+
+// Terms ib .. ie-1 of the sample passes j0 .. j0+M-1, added to acc in the
+// reference's order (M passes side by side in one loop over the coordinates).
 template <int M>
-__device__ __forceinline__ void samp_multi(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
-                                           double* v, double cut = INF_D) {
-  const int n = D.n, w = D.wid, S = D.S;
-  const double* k = D.cst;
+__device__ __forceinline__ void samp_run(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
+                                         int ib, int ie, SAcc* acc) {
+  const int w = D.wid, S = D.S;
   const long long* off = D.t_off;
   switch (D.family) {
     case FAM_COSQUAD: {
-      double s[M];
-#pragma unroll
-      for (int q = 0; q < M; ++q) s[q] = 0.0;
       const double* th = T + off[T_SHI] + j0;
-      for (int i = 0; i < n; ++i) {
+      for (int i = ib; i < ie; ++i) {
         const double* t = th + eidx(D, C, pc, i) * S;
 #pragma unroll
-        for (int q = 0; q < M; ++q) s[q] = __dadd_ru(s[q], t[q]);
+        for (int q = 0; q < M; ++q) acc[q].a = __dadd_ru(acc[q].a, t[q]);
       }
-#pragma unroll
-      for (int q = 0; q < M; ++q) v[q] = __dadd_ru(s[q], k[6 * n + 1]);
       return;
     }
     case FAM_CHAINED: {
-      double f[M];
-#pragma unroll
-      for (int q = 0; q < M; ++q) f[q] = 0.0;
       const double* th = T + off[T_SHI] + j0;
-      int dcur = digit(D, C.c0, C.gsz, pc, 0);
-      for (int i = 0; i < n - 1; ++i) {
+      int dcur = digit(D, C.c0, C.gsz, pc, ib);
+      for (int i = ib; i < ie; ++i) {
         int dn = digit(D, C.c0, C.gsz, pc, i + 1);
         const double* t = th + ((long long)i * w * w + dcur * w + dn) * S;
 #pragma unroll
-        for (int q = 0; q < M; ++q) f[q] = __dadd_ru(f[q], t[q]);
+        for (int q = 0; q < M; ++q) acc[q].a = __dadd_ru(acc[q].a, t[q]);
         dcur = dn;
       }
-#pragma unroll
-      for (int q = 0; q < M; ++q) v[q] = f[q];
       return;
     }
     case FAM_EXPSQRT: {
-      double s_hi[M], c_lo[M];
-#pragma unroll
-      for (int q = 0; q < M; ++q) { s_hi[q] = 0.0; c_lo[q] = 0.0; }
       const double* ts = T + off[T_SQS] + 2 * j0 + 1;
       const double* tc = T + off[T_CSS] + 2 * j0;
-      for (int i = 0; i < n; ++i) {
+      for (int i = ib; i < ie; ++i) {
         const long long e2 = 2 * eidx(D, C, pc, i) * S;
 #pragma unroll
         for (int q = 0; q < M; ++q) {
-          s_hi[q] = __dadd_ru(s_hi[q], ts[e2 + 2 * q]);
-          c_lo[q] = __dadd_rd(c_lo[q], tc[e2 + 2 * q]);
+          acc[q].a = __dadd_ru(acc[q].a, ts[e2 + 2 * q]);
+          acc[q].b = __dadd_rd(acc[q].b, tc[e2 + 2 * q]);
         }
-      }
-#pragma unroll
-      for (int q = 0; q < M; ++q) {
-        double b;
-        v[q] = (expsqrt_hi_bound(k, s_hi[q], c_lo[q], &b) && !flt(b, cut)) ? b : expsqrt_hi(k, s_hi[q], c_lo[q]);
       }
       return;
     }
     default: {  // FAM_PRODCOS
-      iv pr[M];
-      double s_hi[M];
-#pragma unroll
-      for (int q = 0; q < M; ++q) { pr[q] = mk(-1.0, -1.0); s_hi[q] = 0.0; }
       const double* tr = T + off[T_CRS] + 2 * j0;
       const double* ts = T + off[T_SQS4] + 2 * j0 + 1;
-      for (int i = 0; i < n; ++i) {
+      for (int i = ib; i < ie; ++i) {
         const long long e2 = 2 * eidx(D, C, pc, i) * S;
 #pragma unroll
         for (int q = 0; q < M; ++q) {
-          pr[q] = mul(pr[q], ldiv(tr + e2 + 2 * q));
-          s_hi[q] = __dadd_ru(s_hi[q], ts[e2 + 2 * q]);
+          iv pr = mul(mk(acc[q].a, acc[q].b), ldiv(tr + e2 + 2 * q));
+          acc[q].a = pr.lo;
+          acc[q].b = pr.hi;
+          acc[q].c = __dadd_ru(acc[q].c, ts[e2 + 2 * q]);
         }
       }
-#pragma unroll
-      for (int q = 0; q < M; ++q) v[q] = __dadd_ru(__dadd_ru(mulk_hi(s_hi[q], k[0], k[1]), 1.0), pr[q].hi);
       return;
     }
   }
 }
 
+// The value of a finished sample pass.  With a finite cut the value may be
+// replaced by a lower bound of it that is not below cut (callers only look for
+// values below cut).
+__device__ __forceinline__ double samp_value(const Desc& D, const SAcc& r, double cut) {
+  const double* k = D.cst;
+  switch (D.family) {
+    case FAM_COSQUAD: return __dadd_ru(r.a, k[6 * D.n + 1]);
+    case FAM_CHAINED: return r.a;
+    case FAM_EXPSQRT: {
+      double b;
+      if (expsqrt_hi_bound(k, r.a, r.b, &b) && !flt(b, cut)) return b;
+      return expsqrt_hi(k, r.a, r.b);
+    }
+    default: return __dadd_ru(__dadd_ru(mulk_hi(r.c, k[0], k[1]), 1.0), r.b);
+  }
+}
+
+// Upper bounds of f at sample points j0 .. j0+M-1 of the child.  pfx (may be
+// null) holds the running values after the shared terms (samp_shared) for every
+// sample index: pfx[j], pfx[S + j], pfx[2S + j] = a, b, c.
+template <int M>
+__device__ __forceinline__ void samp_multi(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
+                                           double* v, double cut = INF_D, const double* pfx = nullptr) {
+  SAcc acc[M];
+  int ib = 0;
+  const int sh = samp_shared(D, C);
+  if (pfx && sh > 0) {
+    ib = sh;
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+      acc[q].a = pfx[j0 + q];
+      acc[q].b = pfx[D.S + j0 + q];
+      acc[q].c = pfx[2 * D.S + j0 + q];
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < M; ++q) acc[q] = sacc_init(D);
+  }
+  samp_run<M>(D, T, C, pc, j0, ib, samp_terms(D), acc);
+#pragma unroll
+  for (int q = 0; q < M; ++q) v[q] = samp_value(D, acc[q], cut);
+}
+
+// Running values of sample pass j after the shared terms, stored in pfx
+// (samp_multi's layout); returns them.
+__device__ __forceinline__ SAcc samp_prefix(const Desc& D, const double* T, ChildCtx C, int j, double* pfx) {
+  SAcc r = sacc_init(D);
+  samp_run<1>(D, T, C, 0ULL, j, 0, samp_shared(D, C), &r);
+  pfx[j] = r.a;
+  pfx[D.S + j] = r.b;
+  pfx[2 * D.S + j] = r.c;
+  return r;
+}
+
 // upper bound of f at sample point j of the child (one pass of the sample code list)
 __device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j,
-                                        double cut = INF_D) {
+                                        double cut = INF_D, const double* pfx = nullptr) {
   double v;
-  samp_multi<1>(D, T, C, pc, j, &v, cut);
+  samp_multi<1>(D, T, C, pc, j, &v, cut, pfx);
   return v;
 }
 
@@ -689,7 +742,8 @@ __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, Child
     }
     default: {  // FAM_PRODCOS
       long long e = eidx(D, C, pc, j);
-      iv q = div(P.g, ldiv(T + off[T_CR] + 2 * e));
+      iv R = ldiv(T + off[T_RCP4] + 2 * e);
+      iv q = isnan_(R.lo) ? div(P.g, ldiv(T + off[T_CR] + 2 * e)) : mul(P.g, R);
       q = mul(mul(q, ldiv(T + off[T_SNA] + 2 * e)), mk(k[4 + 2 * j], k[4 + 2 * j + 1]));
       q = add(q, ldiv(T + off[T_XD2] + 2 * e));
       iv X = ldiv(T + off[T_XI4] + 2 * e);

@@ -229,24 +229,45 @@ __device__ __forceinline__ iv mul4(iv a, iv b) {
   return mk(l, h);
 }
 
-// Same result with the sign of each operand known: with four finite endpoints the
-// extreme products are fixed by the signs, so only those are formed (a quarter of
-// the FP64 work).  The value returned equals the full form's; only the sign of a
-// zero result can differ, which no comparison here distinguishes.
-// The four sign cases, tried in the order (a>=0, b>=0), (a<=0, b<=0), (a>=0, b<=0),
-// (a<=0, b>=0), take the lower bound from (a.lo or a.hi) x (b.lo or b.hi) and the
-// upper bound from the other two endpoints; the operands are selected without
+// Same result from the signs of the operands: with four finite endpoints the
+// extreme products are fixed by the signs, so only those are formed.  With
+// a >= 0 or a <= 0 (and the same for b) the order of the four cases below is the
+// order of the sign tests; an operand that contains zero in its interior takes
+// the other operand's larger-magnitude endpoint for both bounds, and two such
+// operands compare the two candidate products of each bound.  Directed rounding
+// is monotone, so the rounded extreme product is the extreme rounded product:
+// the value returned equals mul4's; only the sign of a zero result can differ,
+// which no comparison here distinguishes.  Operands are selected without
 // branches so that lanes with different sign cases stay converged.
 __device__ __forceinline__ iv mul(iv a, iv b) {
   if (!(finite_(a.lo) && finite_(a.hi) && finite_(b.lo) && finite_(b.hi))) return mul4(a, b);
   const bool a_nn = !fneg(a.lo), a_np = !fpos(a.hi);   // a >= 0, a <= 0
   const bool b_nn = !fneg(b.lo), b_np = !fpos(b.hi);
-  const bool c1 = a_nn && b_nn, c2 = a_np && b_np, c3 = a_nn && b_np, c4 = a_np && b_nn;
-  if (!(c1 || c2 || c3 || c4)) return mul4(a, b);
-  const bool lo_a = c1 || (!c2 && !c3 && c4);   // lower bound takes a.lo (cases 1, 4)
-  const bool lo_b = c1 || (!c2 && c3);          // lower bound takes b.lo (cases 1, 3)
-  const double x1 = lo_a ? a.lo : a.hi, x2 = lo_a ? a.hi : a.lo;
-  const double y1 = lo_b ? b.lo : b.hi, y2 = lo_b ? b.hi : b.lo;
+  const bool a_s = !a_nn && !a_np, b_s = !b_nn && !b_np; // zero in the interior
+  if (a_s && b_s) {
+    // lo = min(a.lo b.hi, a.hi b.lo), hi = max(a.lo b.lo, a.hi b.hi)
+    const double l1 = __dmul_rd(a.lo, b.hi), l2 = __dmul_rd(a.hi, b.lo);
+    const double h1 = __dmul_ru(a.lo, b.lo), h2 = __dmul_ru(a.hi, b.hi);
+    return mk(pmin(l1, l2), pmax(h1, h2));
+  }
+  double x1, y1, x2, y2;   // lo = x1 * y1 (down), hi = x2 * y2 (up)
+  if (!a_s && !b_s) {
+    const bool c1 = a_nn && b_nn, c2 = a_np && b_np, c3 = a_nn && b_np;
+    const bool lo_a = c1 || (!c2 && !c3);         // a.lo for (a>=0, b>=0) and (a<=0, b>=0)
+    const bool lo_b = c1 || (!c2 && c3);          // b.lo for (a>=0, b>=0) and (a>=0, b<=0)
+    x1 = lo_a ? a.lo : a.hi; x2 = lo_a ? a.hi : a.lo;
+    y1 = lo_b ? b.lo : b.hi; y2 = lo_b ? b.hi : b.lo;
+  } else if (a_s) {
+    // b >= 0: [a.lo b.hi, a.hi b.hi]; b <= 0: [a.hi b.lo, a.lo b.lo]
+    const double m = b_nn ? b.hi : b.lo;
+    x1 = b_nn ? a.lo : a.hi; x2 = b_nn ? a.hi : a.lo;
+    y1 = m; y2 = m;
+  } else {
+    // a >= 0: [a.hi b.lo, a.hi b.hi]; a <= 0: [a.lo b.hi, a.lo b.lo]
+    const double m = a_nn ? a.hi : a.lo;
+    x1 = m; x2 = m;
+    y1 = a_nn ? b.lo : b.hi; y2 = a_nn ? b.hi : b.lo;
+  }
   return mk(__dmul_rd(x1, y1), __dmul_ru(x2, y2));
 }
 
@@ -269,6 +290,14 @@ __device__ __forceinline__ iv div(iv a, iv b) {
     return entire();
   }
   return mul(a, mk(__drcp_rd(b.hi), __drcp_ru(b.lo)));
+}
+
+// The reciprocal interval div(a, b) multiplies by when b does not touch zero
+// (div(a, b) == mul(a, div_recip(b)) then); NaN endpoints otherwise.  Tables of
+// divisors store it so that the reciprocals are formed once per table entry.
+__device__ __forceinline__ iv div_recip(iv b) {
+  if ((fneg(b.lo) && fpos(b.hi)) || feq(b.lo, 0.0) || feq(b.hi, 0.0)) return mk(u2d(~0ULL), u2d(~0ULL));
+  return mk(__drcp_rd(b.hi), __drcp_ru(b.lo));
 }
 
 // power(., 2): x*x rounded to nearest, widened by 5 ulp
