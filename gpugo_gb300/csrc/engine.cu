@@ -231,43 +231,59 @@ __device__ long long children_of(const Desc& D, int cyc) {
 
 // Lists for the next iteration: expanding instances (tables, children) and the
 // ready queue pre-filled with instances that only pop (width-rule emissions).
+// Large batches list the expanding instances family by family: warps walk the
+// work lists in order, so the SMs then run one family's code at a time instead
+// of all four side by side (instruction-cache pressure).  Results do not depend
+// on the order.
 __device__ void build_lists(const KArgs& a) {
   const int S = a.max_slots;
   const int per = (S + blockDim.x - 1) / blockDim.x;
   const int lo = threadIdx.x * per, hi = min(S, lo + per);
-  long long cA = 0, cE = 0, cR = 0, sA = 0, sB = 0;
+  const int prev = a.ctl->nA;   // 0 before the first iteration of an engine
+  const bool grouped = prev >= 128 || (prev == 0 && S >= 128);
+  long long cE = 0, cR = 0;
   for (int s = lo; s < hi; ++s) {
     int stt = a.st[s].status;
-    if (stt == ST_EXPAND) { cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children; }
     if (stt == ST_REPOP) cR++;
     if (stt == ST_EXPAND || stt == ST_REPOP) cE++;
   }
-  long long tA, tE, tR, tSA, tSB;
-  long long oA = block_exclusive_scan(cA, &tA);
-  long long oE = block_exclusive_scan(cE, &tE);
+  long long tE, tR;
+  block_exclusive_scan(cE, &tE);
   long long oR = block_exclusive_scan(cR, &tR);
-  long long oSA = block_exclusive_scan(sA, &tSA);
-  long long oSB = block_exclusive_scan(sB, &tSB);
-  (void)oE;
-  for (int s = lo; s < hi; ++s) {
-    int stt = a.st[s].status;
-    if (stt == ST_EXPAND) {
-      a.idsA[oA] = s;
-      a.prefA[oA] = oSA;
-      a.prefB[oA] = oSB;
-      oA++;
-      oSA += a.desc[s].a_items;
-      oSB += a.st[s].m_children;
+  long long baseA = 0, baseSA = 0, baseSB = 0;
+  for (int f = grouped ? 1 : 0; f <= (grouped ? 4 : 0); ++f) {
+    long long cA = 0, sA = 0, sB = 0;
+    for (int s = lo; s < hi; ++s) {
+      if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
+        cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children;
+      }
     }
-    if (stt == ST_REPOP) a.queue[oR++] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
+    long long tA, tSA, tSB;
+    long long oA = baseA + block_exclusive_scan(cA, &tA);
+    long long oSA = baseSA + block_exclusive_scan(sA, &tSA);
+    long long oSB = baseSB + block_exclusive_scan(sB, &tSB);
+    for (int s = lo; s < hi; ++s) {
+      if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
+        a.idsA[oA] = s;
+        a.prefA[oA] = oSA;
+        a.prefB[oA] = oSB;
+        oA++;
+        oSA += a.desc[s].a_items;
+        oSB += a.st[s].m_children;
+      }
+    }
+    baseA += tA; baseSA += tSA; baseSB += tSB;
   }
+  for (int s = lo; s < hi; ++s)
+    if (a.st[s].status == ST_REPOP) a.queue[oR++] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    a.prefA[tA] = tSA;
-    a.prefB[tA] = tSB;
-    a.ctl->nA = (int)tA;
+    a.prefA[baseA] = baseSA;
+    a.prefB[baseA] = baseSB;
+    a.ctl->nA = (int)baseA;
     a.ctl->nE = (int)tE;
-    a.ctl->totA = tSA;
-    a.ctl->totB = tSB;
+    a.ctl->totA = baseSA;
+    a.ctl->totB = baseSB;
     a.ctl->q_tail = (int)tR;
     a.ctl->q_head = 0;
     a.ctl->n_big_q = 0;
