@@ -421,7 +421,7 @@ __device__ void locate_who(const Desc& D, State& st) {
   for (long long c = lane; c < nc; c += 32) {
     double v = __ldcg(D.ubc_val + c);
     unsigned long long id = __ldcg(D.ubc_id + c);
-    if (v == ubv && id < who) who = id;
+    if (feq(v, ubv) && id < who) who = id;
   }
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long y = __shfl_xor_sync(0xffffffffu, who, o);
@@ -463,7 +463,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
       st.outcome = GPUGO_FINISHED;
     } else {
       double lbbest = ord_val(b.lbk);
-      double lbstar = lbbest < st.out_lb_min ? lbbest : st.out_lb_min;
+      double lbstar = flt(lbbest, st.out_lb_min) ? lbbest : st.out_lb_min;
       if (D.stop_mode == STOP_GAP && ord_val(st.ub) - lbstar <= D.gap_tol) {
         st.outcome = GPUGO_CERTIFIED;
       } else {
@@ -486,7 +486,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
           long long o = st.out_count;
           if (o < D.out_cap) { D.out_key[o] = key; D.out_lb[o] = lbbest; }
           st.out_count = o + 1;
-          if (lbbest < st.out_lb_min) st.out_lb_min = lbbest;
+          if (flt(lbbest, st.out_lb_min)) st.out_lb_min = lbbest;
         } else if (st.iter + 1 >= D.parent_cap) {
           st.outcome = GPUGO_ERR_PARENT_OVERFLOW;
         } else {
@@ -571,7 +571,7 @@ __device__ void block_instance(const KArgs& a, int s) {
     bool in = e < cnt;
     double lbv = in ? __ldcg(D.pool_lb[c] + e) : 0.0;
     unsigned long long key = in ? __ldcg(D.pool_key[c] + e) : 0ULL;
-    bool keep = in && !(compact && lbv > ub);
+    bool keep = in && !(compact && flt(ub, lbv));
     if (in && !keep && e >= before) removed_new++;
     long long pos = e;
     if (compact) {
@@ -676,13 +676,25 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   C.c0 = st.cyc - 1;
   C.gsz = group_size(D.n, D.group, st.cyc);
   double ub = atomic_ub_read(&st.ub);
-  if (lb > ub) return false;
+  if (flt(ub, lb)) return false;
   const unsigned long long pc = pack_code(D, C.gsz, code);
   double bv = 0.0;
   int bj = J_NONE;
-  for (int j = lane; j < D.S; j += 32) {
-    double v = samp_one(D, T, C, pc, j, ub, pfx);
-    if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
+  DerivPre P;
+  P.g = mk(0.0, 0.0);
+  P.u = P.g;
+  int skip = 0;
+  bool have_pre = false;
+  if (D.family == FAM_EXPSQRT && 2 * D.S + 4 <= 32) {
+    double v = 0.0;
+    expsqrt_warp(D, T, C, pc, ub, &v, &P, &skip);
+    if (lane < D.S) { bv = v; bj = lane; }
+    have_pre = true;
+  } else {
+    for (int j = lane; j < D.S; j += 32) {
+      double v = samp_one(D, T, C, pc, j, ub, pfx);
+      if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -691,7 +703,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
     if (samp_less(ov, oj, bv, bj)) { bv = ov; bj = oj; }
   }
   double sm = bv;
-  if (sm == 0.0) sm = 0.0;  // -0 -> +0
+  if (feq(sm, 0.0)) sm = 0.0;  // -0 -> +0
   if (lane == 0) {
     atomicAdd((unsigned long long*)&st.samples, 1ULL);
     if (flt(sm, ub)) {
@@ -706,12 +718,8 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   __syncwarp();
   ub = atomic_ub_read(&st.ub);
   ub = shfl_d(ub, 0);
-  if (lb > ub) return false;
-  DerivPre P;
-  P.g = mk(0.0, 0.0);
-  P.u = P.g;
-  int skip = 0;
-  if (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS) {
+  if (flt(ub, lb)) return false;
+  if (!have_pre && (D.family == FAM_EXPSQRT || D.family == FAM_PRODCOS)) {
     if (lane == 0) {
       if (aux && D.family == FAM_PRODCOS) deriv_pre_aux(aux, &P);
       else skip = deriv_pre(D, T, C, pc, &P);
@@ -788,7 +796,8 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   return 3;
 }
 
-// Term tables of a single-instance iteration go to shared memory.
+// Term tables of a single-instance iteration go to shared memory: the blocks copy
+// them in parallel, and every later access avoids an L2 round trip.
 __device__ int stage_tables(const KArgs& a) {
   extern __shared__ double s_tab[];
   if (a.ctl->nA != 1) return -1;
@@ -929,6 +938,7 @@ __device__ void prefill_ready(const KArgs& a) {
     if (a.cand_mode == GPUGO_CAND_WARP && k >= 32) k = 8;
     if (a.cand_mode == GPUGO_CAND_LANE && k < 32) k = 32;
     a.ctl->cand_claim = k;
+    a.ctl->cand_head = (k < 32) ? (unsigned long long)(W * k) : 0ULL;   // short queues: static first claims
     a.ctl->seed_on = (tot > 4 * W) ? 1 : 0;
     a.ctl->cand_tail = (unsigned long long)tot;
   }
@@ -1007,11 +1017,20 @@ __device__ void phase_candidates(const KArgs& a) {
   const unsigned long long tot = a.ctl->cand_tail;
   const unsigned long long K = (unsigned long long)a.ctl->cand_claim;
   const bool pfx_on = a.ctl->seed_on != 0;   // the seed pass stored the shared sample prefixes
+  // With a short queue (a warp per candidate) the first claim of warp g (numbered
+  // across the blocks first) is the range g*K: the candidates land on warps of
+  // different SMs, which do not share an FP64 unit.  Later claims, and every
+  // claim of a long queue, come from the shared counter.
+  const unsigned long long g = (unsigned long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  bool first = K < 32;
   for (;;) {
-    unsigned long long h = 0;
-    if (lane == 0) h = atomicAdd(&a.ctl->cand_head, K);
-    h = __shfl_sync(0xffffffffu, h, 0);
-    if (h >= tot) break;
+    unsigned long long h = g * K;
+    if (!first) {
+      if (lane == 0) h = atomicAdd(&a.ctl->cand_head, K);
+      h = __shfl_sync(0xffffffffu, h, 0);
+    }
+    first = false;
+    if (h >= tot) break;   // a static range past the end: the shared counter starts later still
     const unsigned long long e = min(tot, h + K);
     if (a.bstamps && lane == 0) atomicAdd(&s_claimed, e - h);
     if (K >= 32) {
@@ -1139,7 +1158,7 @@ __device__ void phase_pool(const KArgs& a) {
       bool in = e < hi;
       double lbv = in ? D.pool_lb[cur][e] : 0.0;
       unsigned long long key = in ? D.pool_key[cur][e] : 0ULL;
-      bool keep = in && (!compact || !(lbv > ub));
+      bool keep = in && (!compact || !flt(ub, lbv));
       unsigned long long pos = (unsigned long long)e;
       if (compact) {
         if (in && !keep && e >= st.count_before) removed_new++;
@@ -1299,7 +1318,7 @@ __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long lo
     double sm = child_samp(D, D.tab, C, pc, &jb);
     lb_out[t] = lb;
     samp_out[t] = sm;
-    flag_out[t] = (lb > ub) ? 1 : child_deriv(D, D.tab, C, pc);
+    flag_out[t] = flt(ub, lb) ? 1 : child_deriv(D, D.tab, C, pc);
   }
 }
 

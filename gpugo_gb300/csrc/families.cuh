@@ -113,6 +113,15 @@ __device__ __forceinline__ int ndig(const Desc& D, int c0, int gsz, int i) {
   return (k >= 0 && k < gsz) ? D.wid : 1;
 }
 
+// (double)v built from the bits (exact for every 32-bit v); an integer-to-FP64
+// conversion instruction costs as much as an FP64 add.
+__device__ __forceinline__ double u32_to_double(unsigned v) {
+  if (v == 0) return 0.0;
+  const int e = 31 - __clz(v);
+  const unsigned long long m = ((unsigned long long)v << (52 - e)) & ((1ULL << 52) - 1);
+  return u2d(((unsigned long long)(1023 + e) << 52) | m);
+}
+
 // child interval of coordinate i for digit d (ackley50.py:583-586, :903-906);
 // pw holds the parent's (hi - lo) / wid per coordinate
 __device__ __forceinline__ iv child_iv(const Desc& D, const double* pbox, const double* pw, int c0, int gsz, int i,
@@ -121,7 +130,7 @@ __device__ __forceinline__ iv child_iv(const Desc& D, const double* pbox, const 
   int k = i - c0;
   if (k >= 0 && k < gsz) {
     double w = pw[i];
-    return mk(__dadd_rn(__dmul_rn(w, (double)d), lo), __dadd_rn(__dmul_rn(w, (double)(d + 1)), lo));
+    return mk(__dadd_rn(__dmul_rn(w, u32_to_double(d)), lo), __dadd_rn(__dmul_rn(w, u32_to_double(d + 1)), lo));
   }
   return mk(lo, hi);
 }
@@ -132,8 +141,8 @@ __device__ __forceinline__ double part_width(const Desc& D, double lo, double hi
 
 // sample point j of an interval (ackley50.py:288-290)
 __device__ __forceinline__ double sample_pt(iv x, int S, int j) {
-  double inc = __ddiv_rn(__dsub_rn(x.hi, x.lo), (double)(S + 1));
-  return __dadd_rn(x.lo, __dmul_rn(inc, (double)(j + 1)));
+  double inc = __ddiv_rn(__dsub_rn(x.hi, x.lo), u32_to_double(S + 1));
+  return __dadd_rn(x.lo, __dmul_rn(inc, u32_to_double(j + 1)));
 }
 
 __device__ __forceinline__ int kkt_prune(iv d, iv x, double dlo, double dhi) {
@@ -241,21 +250,28 @@ __device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv
   return d;
 }
 
-__device__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
-  const int n = D.n, w = D.wid, S = D.S;
+// Work items are numbered kind by kind (all sample-point items, ordered by
+// sample index, then the interval items), so that the 32 lanes of a warp mostly
+// run the same code path; index arithmetic is 32-bit (U = unsigned) unless an
+// instance has 2^31 items or more.
+template <typename U>
+__device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, const double* pw, int cyc, U t) {
+  const int n = D.n, S = D.S;
+  const U w = (U)D.wid;
   const int c0 = cyc - 1, gsz = group_size(n, D.group, cyc);
   const double* k = D.cst;
   double* T = D.tab;
   const long long* off = D.t_off;
+  const U NW = (U)n * w;
   switch (D.family) {
     case FAM_COSQUAD: {
-      int j = (int)(t % (S + 2));
-      long long r = t / (S + 2);
-      int d = (int)(r % w), i = (int)(r / w);
+      // [S sample passes x n*w][LB terms: n*w][gradient tests: n*w]
+      const int j = (int)(t / NW);
+      const U e = t - (U)j * NW;
+      const int d = (int)(e % w), i = (int)(e / w);
       if (d >= ndig(D, c0, gsz, i)) return;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[i], a = k[2 * n + i], b = k[3 * n + i];
-      long long e = (long long)i * w + d;
       if (j == S) {
         iv term = minus(times(sqr(X), a), times(cos_iv(times(X, K)), b));
         T[off[T_LO] + e] = term.lo;
@@ -266,19 +282,22 @@ __device__ void build_item(const Desc& D, const double* pbox, const double* pw, 
         double x = sample_pt(X, S, j);
         iv P = mk(x, x);
         iv term = minus(times(sqr(P), a), times(cos_iv(times(P, K)), b));
-        T[off[T_SHI] + e * S + j] = term.hi;
+        T[off[T_SHI] + (long long)e * S + j] = term.hi;
       }
       return;
     }
     case FAM_CHAINED: {
-      const long long w2 = (long long)w * w;
-      const long long part1 = (long long)(n - 1) * w2 * (S + 1);
+      const U w2 = w * w;
+      const U P1 = (U)(n - 1) * w2;
+      const U part1 = P1 * (U)(S + 1);
       if (t < part1) {
-        int j = (int)(t % (S + 1));
-        long long r = t / (S + 1);
-        int d1 = (int)(r % w); r /= w;
-        int d0 = (int)(r % w);
-        int i = (int)(r / w);
+        // [S + 1 passes (samples, then LB) x (n-1)*w*w]
+        const int j = (int)(t / P1);
+        const U r = t - (U)j * P1;
+        const int d1 = (int)(r % w);
+        const U r2 = r / w;
+        const int d0 = (int)(r2 % w);
+        const int i = (int)(r2 / w);
         if (d0 >= ndig(D, c0, gsz, i) || d1 >= ndig(D, c0, gsz, i + 1)) return;
         iv X = child_iv(D, pbox, pw, c0, gsz, i, d0);
         iv Y = child_iv(D, pbox, pw, c0, gsz, i + 1, d1);
@@ -289,15 +308,15 @@ __device__ void build_item(const Desc& D, const double* pbox, const double* pw, 
         iv u = times(sqr(plus(X, -1.0)), k[n + i]);
         iv v = times(sqr(minus(sqr(X), Y)), k[i]);
         iv term = add(v, u);
-        long long e = (long long)i * w2 + (long long)d0 * w + d1;
+        const long long e = (long long)i * w2 + (long long)d0 * w + d1;
         if (j == S) T[off[T_LO] + e] = term.lo;
         else T[off[T_SHI] + e * S + j] = term.hi;
       } else {
-        long long r = t - part1;
-        const long long w3 = w2 * w;
-        int j = (int)(r / w3);
-        long long e = r % w3;
-        int dm = (int)(e / w2), d = (int)((e / w) % w), dp = (int)(e % w);
+        const U r = t - part1;
+        const U w3 = w2 * w;
+        const int j = (int)(r / w3);
+        const U e = r - (U)j * w3;
+        const int dm = (int)(e / w2), d = (int)((e / w) % w), dp = (int)(e % w);
         int nm = (j > 0) ? ndig(D, c0, gsz, j - 1) : 1;
         int np = (j + 1 < n) ? ndig(D, c0, gsz, j + 1) : 1;
         if (dm >= nm || d >= ndig(D, c0, gsz, j) || dp >= np) return;
@@ -311,53 +330,59 @@ __device__ void build_item(const Desc& D, const double* pbox, const double* pw, 
       return;
     }
     case FAM_EXPSQRT: {
-      int j = (int)(t % (S + 1));
-      long long r = t / (S + 1);
-      int d = (int)(r % w), i = (int)(r / w);
+      // [S sample passes x n*w][interval items: n*w]
+      const int j = (int)(t / NW);
+      const U e = t - (U)j * NW;
+      const int d = (int)(e % w), i = (int)(e / w);
       if (d >= ndig(D, c0, gsz, i)) return;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[8 + i];
-      long long e = (long long)i * w + d;
       if (j == S) {
-        stiv(T + off[T_SQ] + 2 * e, sqr(X));
-        stiv(T + off[T_CS] + 2 * e, cos_iv(times(X, K)));
-        stiv(T + off[T_XI] + 2 * e, X);
-        stiv(T + off[T_SN] + 2 * e, sin_iv(times(X, K)));
-        ((unsigned char*)(T + off[T_ZB]))[e] = (unsigned char)((X.lo > 0 || X.hi < 0) ? 0 : 1);
+        stiv(T + off[T_SQ] + 2 * (long long)e, sqr(X));
+        stiv(T + off[T_CS] + 2 * (long long)e, cos_iv(times(X, K)));
+        stiv(T + off[T_XI] + 2 * (long long)e, X);
+        stiv(T + off[T_SN] + 2 * (long long)e, sin_iv(times(X, K)));
+        ((unsigned char*)(T + off[T_ZB]))[e] = (unsigned char)((fpos(X.lo) || fneg(X.hi)) ? 0 : 1);
       } else {
         double x = sample_pt(X, S, j);
         iv P = mk(x, x);
-        stiv(T + off[T_SQS] + 2 * (e * S + j), sqr(P));
-        stiv(T + off[T_CSS] + 2 * (e * S + j), cos_iv(times(P, K)));
+        const long long q = 2 * ((long long)e * S + j);
+        stiv(T + off[T_SQS] + q, sqr(P));
+        stiv(T + off[T_CSS] + q, cos_iv(times(P, K)));
       }
       return;
     }
     case FAM_PRODCOS: {
-      int j = (int)(t % (S + 1));
-      long long r = t / (S + 1);
-      int d = (int)(r % w), i = (int)(r / w);
+      const int j = (int)(t / NW);
+      const U e = t - (U)j * NW;
+      const int d = (int)(e % w), i = (int)(e / w);
       if (d >= ndig(D, c0, gsz, i)) return;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
-      long long e = (long long)i * w + d;
       if (j == S) {
         iv a = mul(X, RSQ);
         iv cr = cos_iv(a);
-        stiv(T + off[T_CR] + 2 * e, cr);
-        stiv(T + off[T_RCP4] + 2 * e, div_recip(cr));
-        stiv(T + off[T_SQ4] + 2 * e, sqr(X));
-        stiv(T + off[T_SNA] + 2 * e, sin_iv(a));
-        stiv(T + off[T_XD2] + 2 * e, mul(X, mk(k[2], k[3])));
-        stiv(T + off[T_XI4] + 2 * e, X);
+        stiv(T + off[T_CR] + 2 * (long long)e, cr);
+        stiv(T + off[T_RCP4] + 2 * (long long)e, div_recip(cr));
+        stiv(T + off[T_SQ4] + 2 * (long long)e, sqr(X));
+        stiv(T + off[T_SNA] + 2 * (long long)e, sin_iv(a));
+        stiv(T + off[T_XD2] + 2 * (long long)e, mul(X, mk(k[2], k[3])));
+        stiv(T + off[T_XI4] + 2 * (long long)e, X);
       } else {
         double x = sample_pt(X, S, j);
         iv P = mk(x, x);
-        stiv(T + off[T_CRS] + 2 * (e * S + j), cos_iv(mul(P, RSQ)));
-        stiv(T + off[T_SQS4] + 2 * (e * S + j), sqr(P));
+        const long long q = 2 * ((long long)e * S + j);
+        stiv(T + off[T_CRS] + q, cos_iv(mul(P, RSQ)));
+        stiv(T + off[T_SQS4] + q, sqr(P));
       }
       return;
     }
   }
+}
+
+__device__ __forceinline__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
+  if (D.a_items < (1LL << 31)) build_item_t<unsigned>(D, pbox, pw, cyc, (unsigned)t);
+  else build_item_t<unsigned long long>(D, pbox, pw, cyc, (unsigned long long)t);
 }
 
 // ---------------------------------------------------------------------------
@@ -379,18 +404,20 @@ __device__ __forceinline__ double mulk_hi(double ah, double kl, double kh) {
 // one side of power(., 1/2) and exp (IA.py:209-304, :532-570)
 __device__ __forceinline__ double sqrt_lo(double l) { return bump_lo(__dsqrt_rn(fneg(l) ? 0.0 : l), 5); }
 __device__ __forceinline__ double sqrt_hi(double h) { return bump_hi(__dsqrt_rn(fneg(h) ? 0.0 : h), 5); }
-__device__ __forceinline__ double exp_lo(double x) {
-  double l = gg_exp(x);
+// our exp moved down / up by two units in the last place (exp_iv's endpoints)
+__device__ __forceinline__ double exp_lo_of(double l) {
   if (isnan_(l)) return l;
   uint64_t m = d2u(l);
   return (m < 2) ? 0.0 : u2d(m - 2);
 }
-__device__ __forceinline__ double exp_hi(double x) {
-  double h = gg_exp(x);
+__device__ __forceinline__ double exp_hi_of(double h) {
   if (isnan_(h)) return h;
   uint64_t m = d2u(h);
   return (m + 2 >= INF_BITS) ? u2d(INF_BITS) : u2d(m + 2);
 }
+__device__ __forceinline__ double exp_lo(double x) { return exp_lo_of(gg_exp(x)); }
+__device__ __forceinline__ double exp_hi(double x) { return exp_hi_of(gg_exp(x)); }
+__device__ __forceinline__ double neg_(double x) { return u2d(d2u(x) ^ 0x8000000000000000ULL); }
 
 // expsqrt f = -A exp(-B sqrt(mean x^2)) - exp(mean cos) + A + e (ackley50.py:166-212):
 // f's lower bound from the lower bound of the sum of squares and the upper bound of
@@ -715,6 +742,96 @@ __device__ __noinline__ int deriv_pre(const Desc& D, const double* T, ChildCtx C
 // multiplication commutes with negation bit for bit, so P is the negated value
 // product (griewank50.py:383-396).
 __device__ __forceinline__ void deriv_pre_aux(const double* aux, DerivPre* P) { P->g = mk(-aux[1], -aux[0]); }
+
+// One expsqrt candidate with the whole warp.  An FP64 instruction costs the same
+// however many lanes it serves, so the work is laid out across lanes:
+//   lanes j < S       sum of squares of sample pass j (upper side)
+//   lanes S + j       sum of cosines of sample pass j (lower side)
+//   lanes 2S .. 2S+3  the four endpoint sums of the derivative scalars
+// all run as one loop of upward additions (a downward sum is the negated upward
+// sum of the negated terms, RD(a + b) = -RU(-a - b), signed zeros included, so
+// the negated chains start from -0).  The square roots and exponentials of the
+// sample bounds (expsqrt_hi) and of the derivative scalars (deriv_pre) then share
+// instructions across lanes.  Every value is the one the per-pass code computes.
+// Lane j < S returns the value of sample pass j in *v (or, with a finite cut, a
+// lower bound of it not below cut, as samp_value); every lane returns P and the
+// skip flag of deriv_pre.  Requires 2S + 4 <= 32.
+__device__ __noinline__ void expsqrt_warp(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
+                                          double cut, double* v, DerivPre* P, int* skip) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, n = D.n, S = D.S;
+  const double* k = D.cst;
+  const long long* off = D.t_off;
+  // deriv_pre's origin test: every coordinate's child interval contains 0
+  const unsigned char* zb = (const unsigned char*)(T + off[T_ZB]);
+  int notzero = 0;
+  for (int i = lane; i < n; i += 32) notzero |= !zb[eidx(D, C, pc, i)];
+  *skip = !__any_sync(FULL, notzero);
+  const double* src;
+  long long stride, add;
+  bool dn;
+  if (lane < S) { src = T + off[T_SQS]; stride = 2 * S; add = 2 * lane + 1; dn = false; }
+  else if (lane < 2 * S) { src = T + off[T_CSS]; stride = 2 * S; add = 2 * (lane - S); dn = true; }
+  else if (lane < 2 * S + 4) {
+    const int q = lane - 2 * S;   // s.lo, s.hi, c.lo, c.hi
+    src = T + off[q < 2 ? T_SQ : T_CS]; stride = 2; add = q & 1; dn = !(q & 1);
+  } else { src = T + off[T_SQ]; stride = 2; add = 0; dn = false; }
+  double acc = dn ? -0.0 : 0.0;
+  // terms are loaded eight at a time ahead of the additions
+  int i = 0;
+  for (; i + 8 <= n; i += 8) {
+    double t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = src[eidx(D, C, pc, i + q) * stride + add];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc = __dadd_ru(acc, dn ? neg_(t[q]) : t[q]);
+  }
+  for (; i < n; ++i) {
+    const double t = src[eidx(D, C, pc, i) * stride + add];
+    acc = __dadd_ru(acc, dn ? neg_(t) : t);
+  }
+  const double val = dn ? neg_(acc) : acc;
+  const iv inv_n = mk(k[2], k[3]);
+  const iv m = mul(mk(__shfl_sync(FULL, val, 2 * S), __shfl_sync(FULL, val, 2 * S + 1)), inv_n);
+  const iv mc = mul(mk(__shfl_sync(FULL, val, 2 * S + 2), __shfl_sync(FULL, val, 2 * S + 3)), inv_n);
+  const double my_c = __shfl_sync(FULL, val, lane < S ? lane + S : lane);
+  // square roots: sample lanes sqrt_hi of their pass, lanes S and S+1 sqrt_iv(m)
+  const double sa = (lane < S) ? mulk_hi(val, k[2], k[3]) : (lane == S ? m.lo : m.hi);
+  const double sy = __dsqrt_rn(fneg(sa) ? 0.0 : sa);
+  const double pl = __shfl_sync(FULL, sy, S), ph = __shfl_sync(FULL, sy, S + 1);
+  const iv r = mk(bump_lo(pmin(pl, ph), 5), bump_hi(pmax(pl, ph), 5));
+  // sample bounds, screened first (samp_value)
+  double a1 = 0.0, a2 = 0.0, vb = 0.0;
+  bool need = false;
+  if (lane < S) {
+    a1 = __dmul_rd(bump_hi(sy, 5), -k[1]);
+    a2 = mulk_lo(my_c, k[2], k[3]);
+    double E, U;
+    if (exp_upper(a1, &E) && exp_upper(a2, &U)) {
+      vb = __dadd_ru(__dadd_ru(__dmul_ru(E, -k[0]), -U), k[5]);
+      need = flt(vb, cut);
+    } else {
+      need = true;
+    }
+  }
+  // exponentials: the derivative endpoints and the first one of unscreened
+  // samples in one round, the second one of unscreened samples in another
+  double x1 = 0.0;
+  if (lane < S) x1 = need ? a1 : 0.0;
+  else if (lane == S) x1 = __dmul_rd(r.hi, -k[1]);       // times(r, -B).lo
+  else if (lane == S + 1) x1 = __dmul_ru(r.lo, -k[1]);   // times(r, -B).hi
+  else if (lane == S + 2) x1 = mc.lo;
+  else if (lane == S + 3) x1 = mc.hi;
+  const double y1 = gg_exp(x1);
+  double y2 = 0.0;
+  if (__any_sync(FULL, need)) y2 = gg_exp(need ? a2 : 0.0);
+  if (lane < S) {
+    *v = need ? __dadd_ru(__dadd_ru(__dmul_ru(exp_lo_of(y1), -k[0]), -exp_lo_of(y2)), k[5]) : vb;
+  }
+  const iv E = mk(exp_lo_of(__shfl_sync(FULL, y1, S)), exp_hi_of(__shfl_sync(FULL, y1, S + 1)));
+  P->u = mk(exp_lo_of(__shfl_sync(FULL, y1, S + 2)), exp_hi_of(__shfl_sync(FULL, y1, S + 3)));
+  P->g = mul(div(E, r), mk(k[6], k[7]));
+}
 
 // generalized KKT test of coordinate j (rastrigin50.py:365-370); 1 = rule out
 __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
