@@ -287,15 +287,27 @@ def run_batched(args):
     """Config 4: a mixed batch solved by one engine vs the same problems solved
     one per launch (gpugo_solve in a loop); results must be identical."""
     import gpugo_gb300 as G
+    from gpugo_gb300 import autotune as A
     from gpugo_gb300 import problems as P
     probs = P.config4(count=args.count)
+    tuned = None
+    ecfg = A.EngineConfig()
+    if args.autotune:
+        # block size, candidates per warp and fan-out picked on a sample of the batch;
+        # the plain loop then solves the same (re-split) problems
+        t0 = time.perf_counter()
+        tuned = A.tune(probs, sample=min(128, args.count))
+        tune_s = time.perf_counter() - t0
+        probs = tuned.apply(probs)
+        ecfg = tuned.engine
     for p in probs[:8]:
         G.solve(p, box_cap=4)                      # warm-up
     t0 = time.perf_counter()
     plain = [G.solve(p, box_cap=4) for p in probs]
     t_plain = time.perf_counter() - t0
     dev_plain = sum(r.device_ms for r in plain) * 1e-3
-    with G.Engine(max_slots=args.count, arena_bytes=args.arena_gb << 30) as eng:
+    with G.Engine(max_slots=args.count, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
+                  blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as eng:
         eng.solve_all(probs[:8], box_cap=4)        # warm-up
         st0 = eng.stats()
         t0 = time.perf_counter()
@@ -314,23 +326,41 @@ def run_batched(args):
             "batched_wall_s": t_b, "batched_device_s": (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
             "batched_launches": st1["kernel_launches"] - st0["kernel_launches"],
             "plain_wall_s": t_plain, "plain_device_s": dev_plain, "plain_launches": 2 * len(probs),
-            "speedup_vs_plain": t_plain / t_b, "identical_to_plain": same}
+            "speedup_vs_plain": t_plain / t_b, "identical_to_plain": same,
+            "engine": ecfg.label(),
+            **({"autotune": {"seconds": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in
+                                                             tuned.fanout.items()},
+                             "trials": tuned.trials}} if tuned else {})}
 
 
 def run_serving(args):
     """Config 5: Poisson stream of requests, continuous batching, p50/p99."""
+    import gpugo_gb300 as G
+    from gpugo_gb300 import autotune as A
     from gpugo_gb300 import problems as P
     from gpugo_gb300.serve import serve
     stream = P.config5(count=args.count, rate=args.rate)
-    rep = serve(stream, max_slots=min(args.count, 2048), arena_bytes=args.arena_gb << 30,
-                slice_iters=args.slice)
+    ecfg, tuned, tune_s = A.EngineConfig(), None, 0.0
+    if args.autotune:
+        # tuned on a sample of the request mix before the stream starts
+        t0 = time.perf_counter()
+        tuned = A.tune([p for _, p in stream], sample=min(128, args.count))
+        tune_s = time.perf_counter() - t0
+        stream = list(zip([t for t, _ in stream], tuned.apply([p for _, p in stream])))
+        ecfg = tuned.engine
+    slots = min(args.count, 2048)
+    with G.Engine(max_slots=slots, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
+                  blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as eng:
+        rep = serve(stream, max_slots=slots, slice_iters=args.slice, engine=eng)
     sm = rep.summary()
     return {"metric": "time-to-certified p50/p99 (ms) and boxes/s", "value": sm["boxes_per_s"], "unit": "boxes/s",
             "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"], "n_gpus": 1, "dtype": "f64",
             "data": "synthetic (config 5 generator, MASTER_SEED+5)",
             "config": {"workload": f"cfg5-serve{args.count}: Poisson {args.rate}/s, F1-F4, n log-uniform 2..128, "
                                    f"tol 1e-6 or 1e-4, pool arena {args.arena_gb} GiB",
-                       "slice_iters": args.slice},
+                       "slice_iters": args.slice, "engine": ecfg.label(),
+                       **({"autotune_s": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in
+                                                             tuned.fanout.items()}} if tuned else {})},
             **{k: v for k, v in sm.items() if k not in ("p50_ms", "p99_ms")}}
 
 
@@ -364,6 +394,8 @@ def main():
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="cfg4/cfg5: skip the autotuner (block size, candidates per warp, fan-out)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -330,7 +330,7 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       return;
     }
     case FAM_EXPSQRT: {
-      // [S sample passes x n*w][interval items: n*w]
+      // [S sample passes x n*w][interval items: n*w][sine items: n*w]
       const int j = (int)(t / NW);
       const U e = t - (U)j * NW;
       const int d = (int)(e % w), i = (int)(e / w);
@@ -341,8 +341,9 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
         stiv(T + off[T_SQ] + 2 * (long long)e, sqr(X));
         stiv(T + off[T_CS] + 2 * (long long)e, cos_iv(times(X, K)));
         stiv(T + off[T_XI] + 2 * (long long)e, X);
-        stiv(T + off[T_SN] + 2 * (long long)e, sin_iv(times(X, K)));
         ((unsigned char*)(T + off[T_ZB]))[e] = (unsigned char)((fpos(X.lo) || fneg(X.hi)) ? 0 : 1);
+      } else if (j == S + 1) {
+        stiv(T + off[T_SN] + 2 * (long long)e, sin_iv(times(X, K)));
       } else {
         double x = sample_pt(X, S, j);
         iv P = mk(x, x);
@@ -353,6 +354,7 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       return;
     }
     case FAM_PRODCOS: {
+      // [S sample passes x n*w][interval items: n*w][sine items: n*w]
       const int j = (int)(t / NW);
       const U e = t - (U)j * NW;
       const int d = (int)(e % w), i = (int)(e / w);
@@ -360,14 +362,14 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
       if (j == S) {
-        iv a = mul(X, RSQ);
-        iv cr = cos_iv(a);
+        iv cr = cos_iv(mul(X, RSQ));
         stiv(T + off[T_CR] + 2 * (long long)e, cr);
         stiv(T + off[T_RCP4] + 2 * (long long)e, div_recip(cr));
         stiv(T + off[T_SQ4] + 2 * (long long)e, sqr(X));
-        stiv(T + off[T_SNA] + 2 * (long long)e, sin_iv(a));
         stiv(T + off[T_XD2] + 2 * (long long)e, mul(X, mk(k[2], k[3])));
         stiv(T + off[T_XI4] + 2 * (long long)e, X);
+      } else if (j == S + 1) {
+        stiv(T + off[T_SNA] + 2 * (long long)e, sin_iv(mul(X, RSQ)));
       } else {
         double x = sample_pt(X, S, j);
         iv P = mk(x, x);
