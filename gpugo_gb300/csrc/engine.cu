@@ -235,8 +235,59 @@ __device__ long long children_of(const Desc& D, int cyc) {
 // work lists in order, so the SMs then run one family's code at a time instead
 // of all four side by side (instruction-cache pressure).  Results do not depend
 // on the order.
+// At most 32 slots (single solves, small engines): warp 0 builds the lists with
+// shuffles, no block barriers.
+__device__ void build_lists_warp(const KArgs& a) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  const int s = lane;
+  const bool have = s < a.max_slots;
+  const int stt = have ? a.st[s].status : ST_DONE;
+  const bool ex = stt == ST_EXPAND, rp = stt == ST_REPOP;
+  const long long items = ex ? a.desc[s].a_items : 0, kids = ex ? a.st[s].m_children : 0;
+  const unsigned mA = __ballot_sync(0xffffffffu, ex), mR = __ballot_sync(0xffffffffu, rp);
+  const unsigned mE = __ballot_sync(0xffffffffu, ex || rp);
+  const unsigned below = (1u << lane) - 1u;
+  long long pA = items, pB = kids;   // inclusive scans
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    long long ya = __shfl_up_sync(0xffffffffu, pA, o), yb = __shfl_up_sync(0xffffffffu, pB, o);
+    if (lane >= o) { pA += ya; pB += yb; }
+  }
+  if (ex) {
+    const int o = __popc(mA & below);
+    a.idsA[o] = s;
+    a.prefA[o] = pA - items;
+    a.prefB[o] = pB - kids;
+  }
+  if (rp) a.queue[__popc(mR & below)] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
+  const long long totA = __shfl_sync(0xffffffffu, pA, 31), totB = __shfl_sync(0xffffffffu, pB, 31);
+  __syncwarp();
+  if (lane == 0) {
+    const int nA = __popc(mA);
+    a.prefA[nA] = totA;
+    a.prefB[nA] = totB;
+    a.ctl->nA = nA;
+    a.ctl->nE = __popc(mE);
+    a.ctl->totA = totA;
+    a.ctl->totB = totB;
+    a.ctl->q_tail = __popc(mR);
+    a.ctl->q_head = 0;
+    a.ctl->n_big_q = 0;
+    a.ctl->nBig = 0;
+    a.ctl->epoch = a.ctl->epoch + 1;
+    a.ctl->chunk_next = 0;
+    a.ctl->cand_tail = 0;
+    a.ctl->cand_head = 0;
+  }
+}
+
 __device__ void build_lists(const KArgs& a) {
   const int S = a.max_slots;
+  if (S <= 32) {
+    build_lists_warp(a);
+    return;
+  }
   const int per = (S + blockDim.x - 1) / blockDim.x;
   const int lo = threadIdx.x * per, hi = min(S, lo + per);
   const int prev = a.ctl->nA;   // 0 before the first iteration of an engine
