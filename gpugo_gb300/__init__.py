@@ -23,7 +23,7 @@ from .problems import (CHAINED, COSQUAD, EXPSQRT, PRODCOS, STOP_GAP, STOP_WIDTH,
 
 __all__ = ["solve", "eval_children", "Engine", "SolveResult", "Problem", "GpugoError", "instance", "config1",
            "config2", "config3", "config4", "config5", "COSQUAD", "CHAINED", "EXPSQRT", "PRODCOS",
-           "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info"]
+           "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info", "combine"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -120,6 +120,20 @@ def eval_children(p: Problem, parent_box: np.ndarray, cyc: int, codes: np.ndarra
                                flag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
     _lib.check(rc, "gpugo_eval_children")
     return lb, samp, flag
+
+
+def combine(boxes: np.ndarray, tol: float = 1e-3) -> np.ndarray:
+    """Merge result boxes ([k, n, 2], in emission order) into connected roots on
+    the GPU (``gpugo_combine``; the reference's combine / connectivity,
+    rosenbrock50.py:926-1049, with its combineTolerance 1e-3 as the default)."""
+    L = _lib.load()
+    b = np.ascontiguousarray(boxes, dtype=np.float64)
+    k, n = int(b.shape[0]), int(b.shape[1])
+    out = np.empty((max(k, 1), n, 2))
+    nr = ctypes.c_int64()
+    _lib.check(L.gpugo_combine(b.ctypes.data_as(_dp), k, n, float(tol), out.ctypes.data_as(_dp), k,
+                               ctypes.byref(nr)), "gpugo_combine")
+    return out[:nr.value].copy()
 
 
 def device_info() -> tuple[int, int]:

@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -1373,6 +1374,62 @@ __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long lo
   }
 }
 
+// ---------------------------------------------------------------------------
+// result-box merging (rosenbrock50.py:926-1049, combine / connectivity)
+// ---------------------------------------------------------------------------
+// A new box joins the first root it is connected to: in every coordinate it lies
+// inside the root, or |new.lo - root.hi| < tol and |new.hi - new.lo| < tol (the
+// reference's second difference is the new box's own width); the root becomes
+// the coordinate-wise hull.  Otherwise the box is a new root.  The boxes are
+// taken in order (the result depends on it); one block tests the roots in
+// parallel for each box.
+__device__ __forceinline__ bool box_connected(const double* root, const double* nb, int n, double tol) {
+  for (int i = 0; i < n; ++i) {
+    const double rl = root[2 * i], rh = root[2 * i + 1], nl = nb[2 * i], nh = nb[2 * i + 1];
+    if (rl <= nl && nl <= rh && rl <= nh && nh <= rh) continue;
+    if (!(fabs(__dsub_rn(nl, rh)) < tol)) return false;
+    if (!(fabs(__dsub_rn(nh, nl)) < tol)) return false;
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(256) combine_kernel(const double* boxes, long long nbox, int n, double tol,
+                                                      double* roots, long long* nroots) {
+  __shared__ long long s_nr, s_hit[8];
+  if (threadIdx.x == 0) s_nr = 0;
+  __syncthreads();
+  for (long long b = 0; b < nbox; ++b) {
+    const double* nb = boxes + 2LL * n * b;
+    const long long nr = s_nr;
+    long long mine = LLONG_MAX;
+    for (long long r = threadIdx.x; r < nr; r += blockDim.x)
+      if (box_connected(roots + 2LL * n * r, nb, n, tol)) { mine = r; break; }
+    for (int o = 16; o > 0; o >>= 1) {
+      long long y = __shfl_xor_sync(0xffffffffu, mine, o);
+      mine = y < mine ? y : mine;
+    }
+    if ((threadIdx.x & 31) == 0) s_hit[threadIdx.x >> 5] = mine;
+    __syncthreads();
+    long long hit = LLONG_MAX;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) hit = s_hit[w] < hit ? s_hit[w] : hit;
+    double* dst = roots + 2LL * n * (hit == LLONG_MAX ? nr : hit);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      if (hit == LLONG_MAX) {
+        dst[2 * i] = nb[2 * i];
+        dst[2 * i + 1] = nb[2 * i + 1];
+      } else {
+        // np.minimum(root, new) / np.maximum(root, new)
+        if (!(dst[2 * i] < nb[2 * i])) dst[2 * i] = nb[2 * i];
+        if (!(dst[2 * i + 1] > nb[2 * i + 1])) dst[2 * i + 1] = nb[2 * i + 1];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && hit == LLONG_MAX) s_nr = nr + 1;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *nroots = s_nr;
+}
+
 // FP64 peak probe: 8 independent DFMA chains per thread, 4096 steps each
 __global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, double seed, int steps) {
   double a0 = seed + threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
@@ -1821,6 +1878,40 @@ int gpugo_device_info(int32_t* sm_out, int32_t* num_sms_out) {
   if (sm_out) *sm_out = p.major * 10 + p.minor;
   if (num_sms_out) *num_sms_out = p.multiProcessorCount;
   return GPUGO_OK;
+}
+
+int gpugo_combine(const double* boxes, int64_t nbox, int32_t n, double tol, double* roots_out, int64_t cap,
+                  int64_t* nroots_out) {
+  if (nbox < 0 || n < 1 || cap < 0 || !nroots_out || (nbox > 0 && !boxes) || (cap > 0 && !roots_out) ||
+      !(tol >= 0.0))
+    return GPUGO_ERR_INVALID;
+  *nroots_out = 0;
+  if (nbox == 0) return GPUGO_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
+  const size_t bytes = sizeof(double) * 2 * (size_t)n * (size_t)nbox;
+  double *d_boxes = nullptr, *d_roots = nullptr;
+  long long* d_nr = nullptr;
+  int rc = GPUGO_OK;
+  do {
+    if ((rc = cuda_err(cudaMalloc(&d_boxes, bytes)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_roots, bytes)))) break;
+    if ((rc = cuda_err(cudaMalloc(&d_nr, sizeof(long long))))) break;
+    if ((rc = cuda_err(cudaMemcpy(d_boxes, boxes, bytes, cudaMemcpyHostToDevice)))) break;
+    combine_kernel<<<1, 256>>>(d_boxes, nbox, n, tol, d_roots, d_nr);
+    if ((rc = cuda_err(cudaGetLastError()))) break;
+    long long nr = 0;
+    if ((rc = cuda_err(cudaMemcpy(&nr, d_nr, sizeof(long long), cudaMemcpyDeviceToHost)))) break;
+    const int64_t k = std::min<int64_t>(nr, cap);
+    if (k > 0 && (rc = cuda_err(cudaMemcpy(roots_out, d_roots, sizeof(double) * 2 * (size_t)n * (size_t)k,
+                                           cudaMemcpyDeviceToHost))))
+      break;
+    *nroots_out = nr;
+  } while (0);
+  cudaFree(d_boxes);
+  cudaFree(d_roots);
+  cudaFree(d_nr);
+  return rc;
 }
 
 int gpugo_fp64_peak(int32_t repeats, double* tflops_out, double* ms_out) {

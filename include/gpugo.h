@@ -221,6 +221,18 @@ int gpugo_device_info(int32_t* sm_out, int32_t* num_sms_out);
  * roofline denominator for the FP64-bound bound kernels. */
 int gpugo_fp64_peak(int32_t repeats, double* tflops_out, double* ms_out);
 
+/* Result-box merging: replaces the reference's host functions combine /
+   connectivity (GPUGO_1.1/11-Rosenbrock/rosenbrock50.py:926-1049, called at
+   :1439 on every emitted output region with combineTolerance = 1e-3, :1115).
+   boxes: nbox boxes of n coordinates, lo/hi interleaved, in emission order.
+   A box joins the first earlier root it is connected to (in every coordinate it
+   lies inside the root, or |lo - root.hi| < tol and its own width < tol) and the
+   root becomes the hull; otherwise it becomes a new root.  Runs on the device
+   (one block tests the roots of each box in parallel).  *nroots_out receives the
+   number of roots; roots_out the first cap of them. */
+int gpugo_combine(const double* boxes, int64_t nbox, int32_t n, double tol, double* roots_out, int64_t cap,
+                  int64_t* nroots_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -192,5 +192,18 @@ def solve(p, box_cap: int = 4096, trace_cap: int = 0, skip_samples: bool = True)
                         res.status, res.samples_evaluated, boxes[:n_out].copy(), lbs[:n_out].copy(), trace)
 
 
+def combine(boxes: np.ndarray, tol: float) -> np.ndarray:
+    """Result-box merging in order (rosenbrock50.py:926-1049); boxes [k, n, 2]."""
+    b = np.ascontiguousarray(boxes, dtype=np.float64)
+    k, n = b.shape[0], b.shape[1]
+    out = np.empty_like(b) if k else np.empty((0, n, 2))
+    L = lib()
+    L.oc_combine.restype = ctypes.c_int64
+    L.oc_combine.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+                             ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    nr = L.oc_combine(_dp(b.reshape(-1)) if k else None, k, n, float(tol), _dp(out.reshape(-1)) if k else None, k)
+    return out[:nr].copy()
+
+
 def num_threads() -> int:
     return int(lib().oc_num_threads())

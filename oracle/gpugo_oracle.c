@@ -18,6 +18,8 @@
  *   - kernels                 ackley50.py:602-684 (sampling), :686-766 (ruleOutGPU),
  *                             :768-810 (constructFlagArr)
  *   - host B&B loop           ackley50.py:950-1396 (rastrigin50.py:844-1289)
+ *   - result-box merging      GPUGO_1.1/11-Rosenbrock/rosenbrock50.py:926-1049
+ *                             (combine, connectivity)
  *
  * The reference calls libdevice's dadd_rd/dmul_ru/... (emulated here exactly with
  * error-free transformations and an exact 128-bit slow path) and libdevice's
@@ -1147,6 +1149,51 @@ OC_API int oc_solve(const oc_spec* sp, int mode, oc_result* res, double* boxes_o
     free(parents); free(pcyc); free(list); free(clb); free(ckeep);
     consts_free(&c);
     return 0;
+}
+
+/* Result-box merging, in order (rosenbrock50.py:926-985 combine, :987-1049
+ * connectivity).  A new box joins the first root it is connected to: in every
+ * coordinate it lies inside the root, or |new.lo - root.hi| < tol and
+ * |new.hi - new.lo| < tol (the reference's second difference is the new box's own
+ * width); the root becomes the coordinate-wise hull.  Otherwise the box becomes a
+ * new root.  Returns the number of roots (roots_out holds the first cap). */
+static int connected(const double* root, const double* nb, int n, double tol)
+{
+    for (int i = 0; i < n; ++i) {
+        double rl = root[2 * i], rh = root[2 * i + 1], nl = nb[2 * i], nh = nb[2 * i + 1];
+        if (rl <= nl && nl <= rh && rl <= nh && nh <= rh) continue;
+        if (!(fabs(nl - rh) < tol)) return 0;
+        if (!(fabs(nh - nl) < tol)) return 0;
+    }
+    return 1;
+}
+
+OC_API int64_t oc_combine(const double* boxes, int64_t nbox, int n, double tol, double* roots_out, int64_t cap)
+{
+    double* roots = (double*)malloc(sizeof(double) * 2 * (size_t)n * (size_t)(nbox > 0 ? nbox : 1));
+    int64_t nr = 0;
+    for (int64_t b = 0; b < nbox; ++b) {
+        const double* nb = boxes + 2 * (int64_t)n * b;
+        int64_t hit = -1;
+        for (int64_t r = 0; r < nr && hit < 0; ++r)
+            if (connected(roots + 2 * (int64_t)n * r, nb, n, tol)) hit = r;
+        double* dst = roots + 2 * (int64_t)n * (hit < 0 ? nr : hit);
+        if (hit < 0) {
+            memcpy(dst, nb, sizeof(double) * 2 * (size_t)n);
+            ++nr;
+        } else {
+            /* np.minimum(root, new) / np.maximum(root, new): the root's value
+               only when it is strictly better (no NaN here) */
+            for (int i = 0; i < n; ++i) {
+                if (!(dst[2 * i] < nb[2 * i])) dst[2 * i] = nb[2 * i];
+                if (!(dst[2 * i + 1] > nb[2 * i + 1])) dst[2 * i + 1] = nb[2 * i + 1];
+            }
+        }
+    }
+    int64_t k = nr < cap ? nr : cap;
+    if (k > 0) memcpy(roots_out, roots, sizeof(double) * 2 * (size_t)n * (size_t)k);
+    free(roots);
+    return nr;
 }
 
 OC_API int oc_num_threads(void)

@@ -26,7 +26,9 @@ semantics the product follows.  Its ``times`` assumes a non-negative scalar
 Griewank vectors are generated with a sign-aware ``times``.
 
 Only the imports and function definitions of each script are executed; its
-top-level statements (the whole 50-variable B&B run) are skipped.
+top-level statements (the whole 50-variable B&B run) are skipped.  The result-box
+merging vectors come from the same execution of ``rosenbrock50.py``'s host
+functions ``combine`` / ``connectivity``.
 """
 from __future__ import annotations
 
@@ -244,9 +246,50 @@ def main(ref_root: str):
             out["decoder_code"] = np.array(dec_code)
             out["decoder_complete"] = np.stack(dec_box)
             out["decoder_select"] = np.stack(dec_sel)
+    out.update(combine_cases(ref_root))
     dst = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst)
+
+
+def combine_cases(ref_root: str) -> dict:
+    """Result-box merging: the reference's host functions ``combine`` and
+    ``connectivity`` (rosenbrock50.py:926-1049) run on sequences of small boxes,
+    some within the combine tolerance of each other, some not."""
+    ia_mod = load_updated_ia(ref_root, False)
+    ns = load_script(ref_root, FAMILIES["rosenbrock"][0], "IARosenbrock", ia_mod)
+    combine = ns["combine"]
+    rng = np.random.default_rng(0x636F6D62)
+    ns_, tols, boxes, boff, roots, roff = [], [], [], [0], [], [0]
+    for case in range(24):
+        n = int(rng.choice([1, 2, 3, 5, 8]))
+        tol = float(rng.choice([1e-3, 1e-4]))
+        centres = rng.uniform(-2.0, 2.0, size=(int(rng.integers(1, 4)), n))
+        seq = []
+        for _ in range(int(rng.integers(1, 40))):
+            c = centres[int(rng.integers(0, len(centres)))]
+            lo = c + rng.uniform(-3.0, 3.0, size=n) * tol
+            w = rng.choice([0.01, 0.1, 0.5, 2.0]) * tol * rng.uniform(0.5, 1.0, size=n)
+            box = np.empty(2 * n)
+            box[0::2] = lo
+            box[1::2] = lo + w
+            if seq and rng.random() < 0.15:          # a box inside an earlier one
+                prev = seq[int(rng.integers(0, len(seq)))]
+                box = prev.copy()
+                box[0::2] += 0.25 * (prev[1::2] - prev[0::2])
+                box[1::2] -= 0.25 * (prev[1::2] - prev[0::2])
+            seq.append(box)
+        combined: list = []
+        for box in seq:
+            combine(box.copy(), combined, tol)
+        ns_.append(n); tols.append(tol)
+        boxes.extend(seq); boff.append(boff[-1] + len(seq))
+        roots.extend(np.asarray(r, dtype=np.float64) for r in combined); roff.append(roff[-1] + len(combined))
+    flat = lambda arrs: np.concatenate([np.asarray(a, dtype=np.float64).ravel() for a in arrs])
+    print("combine cases", len(ns_), "boxes", len(boxes), "roots", len(roots), flush=True)
+    return {"combine_n": np.array(ns_, dtype=np.int64), "combine_tol": np.array(tols),
+            "combine_box_offsets": np.array(boff, dtype=np.int64), "combine_boxes": flat(boxes),
+            "combine_root_offsets": np.array(roff, dtype=np.int64), "combine_roots": flat(roots)}
 
 
 if __name__ == "__main__":
