@@ -986,8 +986,8 @@ __device__ void prefill_ready(const KArgs& a) {
     long long c = tot / (2 * W);
     // a warp per candidate while there are fewer candidates than warps x 32;
     // beyond that each lane takes its own candidate, 32 or 64 per claim
-    long long k = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 8 ? 8 : c));
-    if (a.cand_mode == GPUGO_CAND_WARP && k >= 32) k = 8;
+    long long k = (c >= 32) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : c);
+    if (a.cand_mode == GPUGO_CAND_WARP && k >= 32) k = 31;
     if (a.cand_mode == GPUGO_CAND_LANE && k < 32) k = 32;
     a.ctl->cand_claim = k;
     a.ctl->cand_head = (k < 32) ? (unsigned long long)(W * k) : 0ULL;   // short queues: static first claims
@@ -1152,27 +1152,51 @@ __device__ void phase_candidates(const KArgs& a) {
       __syncwarp();
       continue;
     }
-    int acc_s = -1;
-    long long acc_n = 0;
-    for (unsigned long long q = h; q < e; ++q) {
-      const unsigned long long* en = a.cands + CAND_WORDS * q;
-      unsigned long long w0 = en[0];
-      double lb = __longlong_as_double((long long)en[1]);
-      double aux[2];
-#pragma unroll
-      for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
-      int s = (int)(w0 >> 32);
-      unsigned long long code = w0 & 0xffffffffULL;
-      const double* T = (s == si) ? s_tab : a.desc[s].tab;
-      bool keep = warp_candidate(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
-      if (keep && lane == 0) append_survivor(a, s, code, lb);
-      if (lane == 0) {
-        if (s != acc_s && acc_s >= 0) { count_done(a, acc_s, acc_n); acc_n = 0; }
-        acc_s = s;
-        acc_n++;
+    // A warp per candidate.  The claim (at most 32 entries) is loaded by the
+    // lanes at once and filtered against the current UB; the survivors of the
+    // filter are then processed one after the other by the whole warp.
+    {
+      const unsigned long long q = h + lane;
+      const bool valid = q < e;
+      int s = -1;
+      unsigned long long code = 0;
+      double lb = 0.0, aux[2] = {0.0, 0.0};
+      bool live = false;
+      if (valid) {
+        const unsigned long long* en = a.cands + CAND_WORDS * q;
+        const unsigned long long w0 = en[0];
+        s = (int)(w0 >> 32);
+        code = w0 & 0xffffffffULL;
+        lb = __longlong_as_double((long long)en[1]);
+        aux[0] = __longlong_as_double((long long)en[2]);
+        aux[1] = __longlong_as_double((long long)en[3]);
+        live = !flt(atomic_ub_read(&a.st[s].ub), lb);
+      }
+      unsigned int lm = __ballot_sync(0xffffffffu, live);
+      while (lm) {
+        const int b = __ffs(lm) - 1;
+        lm &= lm - 1;
+        const int cs = __shfl_sync(0xffffffffu, s, b);
+        const unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
+        const double cl = shfl_d(lb, b);
+        double ca[2];
+        ca[0] = shfl_d(aux[0], b);
+        ca[1] = shfl_d(aux[1], b);
+        const double* T = (cs == si) ? s_tab : a.desc[cs].tab;
+        const bool keep = warp_candidate(a, cs, T, cc, cl, ca, pfx_on ? T + a.desc[cs].t_off[T_PFX] : nullptr);
+        if (keep && lane == 0) append_survivor(a, cs, cc, cl);
+      }
+      __syncwarp();
+      // every entry of the claim is done: count them per instance
+      unsigned int act = __ballot_sync(0xffffffffu, valid);
+      while (act) {
+        const int leader = __ffs(act) - 1;
+        const int ls = __shfl_sync(0xffffffffu, s, leader);
+        const unsigned int m = __ballot_sync(0xffffffffu, valid && s == ls);
+        if (lane == leader) count_done(a, ls, __popc(m));
+        act &= ~m;
       }
     }
-    if (lane == 0 && acc_s >= 0) count_done(a, acc_s, acc_n);
     __syncwarp();
   }
   __syncthreads();
