@@ -654,8 +654,37 @@ __device__ __forceinline__ void samp_multi(const Desc& D, const double* T, Child
     for (int q = 0; q < M; ++q) acc[q] = sacc_init(D);
   }
   samp_run<M>(D, T, C, pc, j0, ib, samp_terms(D), acc);
+  if (D.family != FAM_EXPSQRT || M == 1) {
 #pragma unroll
-  for (int q = 0; q < M; ++q) v[q] = samp_value(D, acc[q], cut);
+    for (int q = 0; q < M; ++q) v[q] = samp_value(D, acc[q], cut);
+    return;
+  }
+  // exp-sqrt: screen all M values first; the exact tails that remain run one per
+  // lane per round (a lane takes its next pending value), so the warp pays for
+  // max-over-lanes of them instead of one round per sample index any lane needs
+  const double* k = D.cst;
+  unsigned pend = 0;
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+    double b;
+    if (expsqrt_hi_bound(k, acc[q].a, acc[q].b, &b) && !flt(b, cut)) v[q] = b;
+    else pend |= 1u << q;
+  }
+  const unsigned am = __activemask();
+  while (__any_sync(am, pend != 0)) {
+    if (pend) {
+      const int q = __ffs(pend) - 1;
+      pend &= pend - 1;
+      double sa = acc[0].a, sb = acc[0].b;
+#pragma unroll
+      for (int t = 1; t < M; ++t)
+        if (t == q) { sa = acc[t].a; sb = acc[t].b; }
+      const double e = expsqrt_hi(k, sa, sb);
+#pragma unroll
+      for (int t = 0; t < M; ++t)
+        if (t == q) v[t] = e;
+    }
+  }
 }
 
 // Running values of sample pass j after the shared terms, stored in pfx
