@@ -299,14 +299,15 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
         const int d0 = (int)(r2 % w);
         const int i = (int)(r2 / w);
         if (d0 >= ndig(D, c0, gsz, i) || d1 >= ndig(D, c0, gsz, i + 1)) return;
+        const double kq = k[n + i], kp = k[i];   // loaded with the parent box, not after the chain
         iv X = child_iv(D, pbox, pw, c0, gsz, i, d0);
         iv Y = child_iv(D, pbox, pw, c0, gsz, i + 1, d1);
         if (j < S) {
           double x = sample_pt(X, S, j), y = sample_pt(Y, S, j);
           X = mk(x, x); Y = mk(y, y);
         }
-        iv u = times(sqr(plus(X, -1.0)), k[n + i]);
-        iv v = times(sqr(minus(sqr(X), Y)), k[i]);
+        iv u = times(sqr(plus(X, -1.0)), kq);
+        iv v = times(sqr(minus(sqr(X), Y)), kp);
         iv term = add(v, u);
         const long long e = (long long)i * w2 + (long long)d0 * w + d1;
         if (j == S) T[off[T_LO] + e] = term.lo;
