@@ -497,7 +497,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     if (expanded) {
       st.bounded += st.m_children;
       if (st.iter < D.trace_cap) {
-        D.tr_ub[st.iter] = ord_val(st.ub);
+        D.tr_ub[st.iter] = ord_val(vload(st.ub));
         D.tr_surv[st.iter] = n_surv;
         D.tr_pool[st.iter] = cnt;
         D.tr_sel[st.iter] = -1;
@@ -516,7 +516,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
     } else {
       double lbbest = ord_val(b.lbk);
       double lbstar = flt(lbbest, st.out_lb_min) ? lbbest : st.out_lb_min;
-      if (D.stop_mode == STOP_GAP && ord_val(st.ub) - lbstar <= D.gap_tol) {
+      if (D.stop_mode == STOP_GAP && ord_val(vload(st.ub)) - lbstar <= D.gap_tol) {
         st.outcome = GPUGO_CERTIFIED;
       } else {
         const int c = st.cur;
@@ -588,7 +588,7 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
         st.status = ST_EXPAND;
       }
     }
-    st.ub_start = st.ub;
+    st.ub_start = vload(st.ub);
     st.count_before = st.count;
     st.ubc_count = 0;
     st.b_done = 0;
@@ -650,6 +650,57 @@ __device__ void block_instance(const KArgs& a, int s) {
     finish_iteration(D, st, b, kept, n_surv, expanded);
   }
   __syncthreads();
+}
+
+// The same list update done by one warp, for small lists: the warp that finishes
+// an instance's last candidate runs it at once (no ready-queue round trip, no
+// block barriers).  Compaction positions come from ballots; every lane has read
+// its entry before any lane of the chunk writes (positions never pass the entry
+// being read).
+constexpr long long POOL_WARP_MAX = 256;
+__device__ void warp_instance(const KArgs& a, int s) {
+  const int lane = threadIdx.x & 31;
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  const bool expanded = (vload(st.status) == ST_EXPAND);
+  const long long count = vload(st.count);
+  long long cnt = count < D.pool_cap ? count : D.pool_cap;
+  if (vload(st.outcome) < 0) cnt = 0;
+  const unsigned long long ubk = vload(st.ub);
+  const bool compact = ubk != vload(st.ub_start);
+  const double ub = ord_val(ubk);
+  const long long before = vload(st.count_before);
+  const int c = vload(st.cur);
+  if (expanded && compact) locate_who(D, st);
+  Best b = best_none();
+  long long kept = 0, removed_new = 0;
+  for (long long base = 0; base < cnt; base += 32) {
+    const long long e = base + lane;
+    const bool in = e < cnt;
+    const double lbv = in ? __ldcg(D.pool_lb[c] + e) : 0.0;
+    const unsigned long long key = in ? __ldcg(D.pool_key[c] + e) : 0ULL;
+    const bool keep = in && !(compact && flt(ub, lbv));
+    if (in && !keep && e >= base && e >= before) removed_new++;
+    long long pos = e;
+    if (compact) {
+      const unsigned int km = __ballot_sync(0xffffffffu, keep);
+      pos = kept + __popc(km & ((1u << lane) - 1u));
+      if (keep) {
+        D.pool_lb[c][pos] = lbv;
+        D.pool_key[c][pos] = key;
+      }
+      kept += __popc(km);
+    }
+    if (keep) {
+      Best cb; cb.lbk = ord_key(lbv); cb.key = key; cb.idx = (unsigned long long)pos;
+      if (best_less(cb, b)) b = cb;
+    }
+  }
+  if (!compact) kept = cnt;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
+  b = warp_min(b);
+  finish_iteration(D, st, b, kept, (cnt - before) - removed_new, expanded);
 }
 
 // ---------------------------------------------------------------------------
@@ -1050,11 +1101,26 @@ __device__ void phase_seed(const KArgs& a) {
 // instance's last candidate queues it for its list update.  Short queues give a
 // whole warp to each candidate (samples and KKT coordinates across the lanes);
 // long queues give each lane its own candidate.
-__device__ __forceinline__ void count_done(const KArgs& a, int s, long long n) {
+// Called by one lane; returns true when these were the instance's last candidates.
+__device__ __forceinline__ bool count_done(const KArgs& a, int s, long long n) {
   __threadfence();
   State& st = a.st[s];
   unsigned long long old = atomicAdd((unsigned long long*)&st.cand_done, (unsigned long long)n);
-  if ((long long)old + n == st.cand_total) queue_push(a, s);
+  return (long long)old + n == st.cand_total;
+}
+
+// Every lane of the warp: an instance whose candidates are all done gets its list
+// update from this warp when the list is small, from a block (ready queue) otherwise.
+__device__ __forceinline__ void instance_ready(const KArgs& a, int s) {
+  const State& st = a.st[s];
+  const long long count = vload(st.count);
+  const long long cnt = count < a.desc[s].pool_cap ? count : a.desc[s].pool_cap;
+  if (cnt <= POOL_WARP_MAX) {
+    warp_instance(a, s);
+  } else if ((threadIdx.x & 31) == 0) {
+    queue_push(a, s);
+  }
+  __syncwarp();
 }
 
 __device__ void phase_candidates(const KArgs& a) {
@@ -1111,7 +1177,11 @@ __device__ void phase_candidates(const KArgs& a) {
           int leader = __ffs(act) - 1;
           int ls = __shfl_sync(0xffffffffu, s, leader);
           unsigned int m = __ballot_sync(0xffffffffu, valid && !live && s == ls);
-          if (lane == leader) count_done(a, ls, __popc(m));
+          {
+            int fin = 0;
+            if (lane == leader) fin = count_done(a, ls, __popc(m));
+            if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
+          }
           act &= ~m;
         }
       }
@@ -1142,10 +1212,12 @@ __device__ void phase_candidates(const KArgs& a) {
           int ls = __shfl_sync(0xffffffffu, s, leader);
           unsigned int m = __ballot_sync(0xffffffffu, valid && s == ls);
           unsigned int sm = __ballot_sync(0xffffffffu, valid && s == ls && sampled);
+          int fin = 0;
           if (lane == leader) {
             if (sm) atomicAdd((unsigned long long*)&a.st[ls].samples, (unsigned long long)__popc(sm));
-            count_done(a, ls, __popc(m));
+            fin = count_done(a, ls, __popc(m));
           }
+          if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
           act &= ~m;
         }
       }
@@ -1193,7 +1265,11 @@ __device__ void phase_candidates(const KArgs& a) {
         const int leader = __ffs(act) - 1;
         const int ls = __shfl_sync(0xffffffffu, s, leader);
         const unsigned int m = __ballot_sync(0xffffffffu, valid && s == ls);
-        if (lane == leader) count_done(a, ls, __popc(m));
+        {
+            int fin = 0;
+            if (lane == leader) fin = count_done(a, ls, __popc(m));
+            if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
+          }
         act &= ~m;
       }
     }
