@@ -492,58 +492,82 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
                                  bool expanded) {
   const int lane = threadIdx.x & 31;
   const int n = D.n;
-  if (lane == 0) {
-    st.count = cnt;
-    if (expanded) {
-      st.bounded += st.m_children;
-      if (st.iter < D.trace_cap) {
-        D.tr_ub[st.iter] = ord_val(vload(st.ub));
-        D.tr_surv[st.iter] = n_surv;
-        D.tr_pool[st.iter] = cnt;
-        D.tr_sel[st.iter] = -1;
-      }
-    }
+  // Every field read below is loaded up front, in one round of independent
+  // loads, instead of one L2 round trip after another along the decisions.
+  const int outcome0 = vload(st.outcome);
+  const unsigned long long ubk = vload(st.ub);
+  const long long iter = st.iter;
+  const int cur = st.cur;
+  const long long out_count = st.out_count;
+  const double out_lb_min = st.out_lb_min;
+  const long long bounded = st.bounded, m_children = st.m_children;
+  const int stop_mode = D.stop_mode, max_cyc = D.max_cyc, group = D.group;
+  const long long trace_cap = D.trace_cap, parent_cap = D.parent_cap, out_cap = D.out_cap, max_iter = D.max_iter;
+  const double gap_tol = D.gap_tol, width_tol = D.width_tol;
+  const bool have_best = !(cnt == 0 || b.idx == ~0ULL);
+  const long long prow = (long long)(b.key >> 32);
+  const unsigned long long code = b.key & 0xffffffffULL;
+  // the selected entry's parent cycle and box, and the list's last entry (moved
+  // into the selected slot), fetched together
+  int pcyc = 1;
+  double plo = 0.0, phi = 0.0, pwd = 0.0, last_lb = 0.0;
+  unsigned long long last_key = 0;
+  if (lane == 0 && have_best && outcome0 >= 0) {
+    pcyc = D.pcyc[prow];
+    plo = D.parents[2LL * n * prow];
+    phi = D.parents[2LL * n * prow + 1];
+    pwd = D.pwid[(long long)n * prow];
+    last_lb = __ldcg(D.pool_lb[cur] + cnt - 1);
+    last_key = __ldcg(D.pool_key[cur] + cnt - 1);
   }
-  __syncwarp();
   int decision = 0;  // 0 stop, 1 emit (pop again next iteration), 2 expand
   unsigned long long key = 0;
   int ccyc = 1;
   if (lane == 0) {
-    if (vload(st.outcome) < 0) {
+    st.count = cnt;
+    if (expanded) {
+      st.bounded = bounded + m_children;
+      if (iter < trace_cap) {
+        D.tr_ub[iter] = ord_val(ubk);
+        D.tr_surv[iter] = n_surv;
+        D.tr_pool[iter] = cnt;
+        D.tr_sel[iter] = -1;
+      }
+    }
+    if (outcome0 < 0) {
       decision = 0;
-    } else if (cnt == 0 || b.idx == ~0ULL) {
+    } else if (!have_best) {
       st.outcome = GPUGO_FINISHED;
     } else {
-      double lbbest = ord_val(b.lbk);
-      double lbstar = flt(lbbest, st.out_lb_min) ? lbbest : st.out_lb_min;
-      if (D.stop_mode == STOP_GAP && ord_val(vload(st.ub)) - lbstar <= D.gap_tol) {
+      const double lbbest = ord_val(b.lbk);
+      const double lbstar = flt(lbbest, out_lb_min) ? lbbest : out_lb_min;
+      if (stop_mode == STOP_GAP && ord_val(ubk) - lbstar <= gap_tol) {
         st.outcome = GPUGO_CERTIFIED;
       } else {
-        const int c = st.cur;
-        long long last = cnt - 1;
-        D.pool_lb[c][b.idx] = __ldcg(D.pool_lb[c] + last);
-        D.pool_key[c][b.idx] = __ldcg(D.pool_key[c] + last);
-        st.count = last;
+        D.pool_lb[cur][b.idx] = last_lb;
+        D.pool_key[cur][b.idx] = last_key;
+        st.count = cnt - 1;
         key = b.key;
-        long long prow = (long long)(key >> 32);
-        unsigned long long code = key & 0xffffffffULL;
-        ccyc = D.pcyc[prow];
-        const double* pb = D.parents + 2LL * n * prow;
-        int gsz = group_size(n, D.group, ccyc);
-        iv x0 = child_iv(D, pb, D.pwid + (long long)n * prow, ccyc - 1, gsz, 0,
-                         digit(D, ccyc - 1, gsz, pack_code(D, gsz, code), 0));
+        ccyc = pcyc;
+        const int gsz = group_size(n, group, ccyc);
+        // child interval of coordinate 0 (child_iv on the prefetched parent values)
+        iv x0 = mk(plo, phi);
+        if (ccyc - 1 <= 0 && 0 < ccyc - 1 + gsz) {
+          const int dg = digit(D, ccyc - 1, gsz, pack_code(D, gsz, code), 0);
+          x0 = mk(__dadd_rn(__dmul_rn(pwd, u32_to_double(dg)), plo),
+                  __dadd_rn(__dmul_rn(pwd, u32_to_double(dg + 1)), plo));
+        }
         double width = __dsub_rn(x0.hi, x0.lo);
-        if (width < D.width_tol && ccyc == D.max_cyc) {
+        if (width < width_tol && ccyc == max_cyc) {
           decision = 1;
-          long long o = st.out_count;
-          if (o < D.out_cap) { D.out_key[o] = key; D.out_lb[o] = lbbest; }
-          st.out_count = o + 1;
-          if (flt(lbbest, st.out_lb_min)) st.out_lb_min = lbbest;
-        } else if (st.iter + 1 >= D.parent_cap) {
+          if (out_count < out_cap) { D.out_key[out_count] = key; D.out_lb[out_count] = lbbest; }
+          st.out_count = out_count + 1;
+          if (flt(lbbest, out_lb_min)) st.out_lb_min = lbbest;
+        } else if (iter + 1 >= parent_cap) {
           st.outcome = GPUGO_ERR_PARENT_OVERFLOW;
         } else {
           decision = 2;
-          if (st.iter < D.trace_cap) D.tr_sel[st.iter] = (long long)key;
+          if (iter < trace_cap) D.tr_sel[iter] = (long long)key;
         }
       }
     }
@@ -552,14 +576,13 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
   key = __shfl_sync(0xffffffffu, key, 0);
   ccyc = __shfl_sync(0xffffffffu, ccyc, 0);
   if (decision == 2) {
-    const long long prow = (long long)(key >> 32);
-    const unsigned long long code = key & 0xffffffffULL;
-    const double* pb = D.parents + 2LL * n * prow;
-    const double* pw = D.pwid + (long long)n * prow;
-    double* nb = D.parents + 2LL * n * (st.iter + 1);
-    double* nw = D.pwid + (long long)n * (st.iter + 1);
-    const int gsz = group_size(n, D.group, ccyc);
-    const unsigned long long pc = pack_code(D, gsz, code);
+    const long long row = (long long)(key >> 32);
+    const double* pb = D.parents + 2LL * n * row;
+    const double* pw = D.pwid + (long long)n * row;
+    double* nb = D.parents + 2LL * n * (iter + 1);
+    double* nw = D.pwid + (long long)n * (iter + 1);
+    const int gsz = group_size(n, group, ccyc);
+    const unsigned long long pc = pack_code(D, gsz, key & 0xffffffffULL);
     for (int i = lane; i < n; i += 32) {
       iv x = child_iv(D, pb, pw, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, pc, i));
       nb[2 * i] = x.lo;
@@ -571,25 +594,25 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
   if (lane == 0) {
     if (decision == 0) {
       st.status = ST_DONE;
-      if (st.outcome == 0) st.outcome = GPUGO_FINISHED;
+      if (vload(st.outcome) == 0) st.outcome = GPUGO_FINISHED;
     } else if (decision == 1) {
       st.status = ST_REPOP;
     } else {
-      long long row = st.iter + 1;
-      int ncyc = (ccyc == D.max_cyc) ? 1 : ccyc + D.group;
+      const long long row = iter + 1;
+      const int ncyc = (ccyc == max_cyc) ? 1 : ccyc + group;
       D.pcyc[row] = ncyc;
       st.iter = row;
       st.cyc = ncyc;
       st.m_children = children_of(D, ncyc);
-      if (D.max_iter > 0 && row >= D.max_iter) {
+      if (max_iter > 0 && row >= max_iter) {
         st.status = ST_DONE;
         st.outcome = GPUGO_ITER_LIMIT;
       } else {
         st.status = ST_EXPAND;
       }
     }
-    st.ub_start = vload(st.ub);
-    st.count_before = st.count;
+    st.ub_start = ubk;
+    st.count_before = vload(st.count);
     st.ubc_count = 0;
     st.b_done = 0;
     st.cand_total = 0;
