@@ -922,11 +922,12 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   return 3;
 }
 
-// Term tables of a single-instance iteration go to shared memory: the blocks copy
-// them in parallel, and every later access avoids an L2 round trip.
-__device__ int stage_tables(const KArgs& a) {
+// Term tables of a single-instance iteration go to shared memory (when the block
+// has enough work to pay for the copy): the blocks copy them in parallel, and
+// every later access avoids an L2 round trip.
+__device__ int stage_tables(const KArgs& a, bool worth = true) {
   extern __shared__ double s_tab[];
-  if (a.ctl->nA != 1) return -1;
+  if (a.ctl->nA != 1 || !worth) return -1;
   const int si = a.idsA[0];
   const Desc& D = a.desc[si];
   if (D.tab_doubles * 8 > SMEM_TAB_BYTES) return -1;
@@ -1150,7 +1151,8 @@ __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ double s_tab[];
   __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
   __shared__ unsigned long long s_claimed;
-  const int si = stage_tables(a);
+  // a few candidates per block do not pay for copying the tables
+  const int si = stage_tables(a, a.ctl->cand_tail >= 16ULL * gridDim.x);
   if (threadIdx.x == 0) s_claimed = 0;
   __syncthreads();
   bstamp(a, 6);
