@@ -2109,6 +2109,9 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel, E->threads, SMEM_TAB_BYTES)))) break;
     if (occ < 1) { rc = GPUGO_ERR_CUDA; break; }
     if (cfg->blocks_per_sm > 0) occ = std::min(occ, cfg->blocks_per_sm);
+    // an engine for a handful of solves is latency-bound: one block per SM halves
+    // the arrivals at every grid barrier (measured faster on single solves)
+    else if (cfg->max_slots <= 4) occ = std::min(occ, 1);
     E->blocks = occ * E->nsm;
     if ((rc = cuda_err(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking)))) break;
     if ((rc = cuda_err(cudaMalloc(&E->d_desc, sizeof(Desc) * E->max_slots)))) break;
@@ -2434,7 +2437,6 @@ int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, do
     memset(&cfg, 0, sizeof(cfg));
     cfg.max_slots = 1;
     cfg.threads = 256;
-    cfg.blocks_per_sm = 1;   // a single solve: half the blocks at each grid barrier (measured faster)
     cfg.arena_bytes = std::max<int64_t>(L.bytes, 64LL << 20);
     cfg.wait_timeout_s = 60.0;
     if ((rc = gpugo_engine_create(&cfg, &g_single))) return rc;

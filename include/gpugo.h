@@ -162,7 +162,7 @@ typedef struct gpugo_engine_cfg {
     int32_t threads;            /* threads per block (0: 256) */
     int64_t arena_bytes;        /* device memory for pools, tables and parent tables */
     double  wait_timeout_s;     /* bound of every device-side wait (0: 60 s) */
-    int32_t blocks_per_sm;      /* 0: occupancy maximum */
+    int32_t blocks_per_sm;      /* 0: occupancy maximum (one per SM for engines of at most 4 slots) */
     int32_t cand_mode;          /* candidate scheduling, GPUGO_CAND_* (results are the same in every mode) */
 } gpugo_engine_cfg;
 
