@@ -1463,12 +1463,144 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->iters = it;
 }
 
-// one thread per newly admitted slot
-__global__ void init_slots_kernel(Desc* desc, State* st, const int* slots, int m) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  int s = slots[t];
-  init_consts(desc[s]);
+// Results of finished instances, one block each, written as one record per
+// instance into a buffer the host copies back at once (instead of copying each
+// instance's list and parent table).  Record (doubles): [0] LB, [1] boxes k,
+// [2, 2+k) their LBs, then k boxes of 2n endpoints, then the sample point that
+// set the UB (n) and [end] 1 when it exists.  The k boxes are the emitted
+// (width-rule) boxes first, then, in gap mode, the k - emitted smallest list
+// entries in (LB, key) order -- the order the host path sorts into.
+struct FinRec {
+  long long slot, k, emitted, off;
+};
+
+__device__ void decode_box(const Desc& D, unsigned long long key, double* out) {
+  const int n = D.n;
+  const long long prow = (long long)(key >> 32);
+  const int cyc = D.pcyc[prow];
+  const int gsz = group_size(n, D.group, cyc);
+  const unsigned long long pc = pack_code(D, gsz, key & 0xffffffffULL);
+  const double* pb = D.parents + 2LL * n * prow;
+  const double* pw = D.pwid + (long long)n * prow;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const iv x = child_iv(D, pb, pw, cyc - 1, gsz, i, digit(D, cyc - 1, gsz, pc, i));
+    out[2 * i] = x.lo;
+    out[2 * i + 1] = x.hi;
+  }
+}
+
+__global__ void __launch_bounds__(256) finalize_kernel(const Desc* desc, const State* st, const FinRec* recs,
+                                                       double* outbuf) {
+  __shared__ double s_v[8];
+  __shared__ unsigned long long s_k[8];
+  const FinRec fr = recs[blockIdx.x];
+  const Desc& D = desc[fr.slot];
+  const State& S = st[fr.slot];
+  const int n = D.n;
+  double* o = outbuf + fr.off;
+  double* lbs = o + 2;
+  double* boxes = lbs + fr.k;
+  double* xh = boxes + 2LL * n * fr.k;
+  const long long cnt = S.count < D.pool_cap ? S.count : D.pool_cap;
+  const double* plb = D.pool_lb[S.cur];
+  const unsigned long long* pkey = D.pool_key[S.cur];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // LB: the smallest of the emitted boxes' LBs and the list's
+  double m = S.out_lb_min;
+  for (long long i = threadIdx.x; i < cnt; i += blockDim.x) m = flt(plb[i], m) ? plb[i] : m;
+  for (int off = 16; off > 0; off >>= 1) {
+    const double y = __shfl_xor_sync(0xffffffffu, m, off);
+    m = flt(y, m) ? y : m;
+  }
+  if (lane == 0) s_v[wid] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = s_v[0];
+    for (int w = 1; w < nw; ++w) b = flt(s_v[w], b) ? s_v[w] : b;
+    o[0] = b;
+    o[1] = (double)fr.k;
+  }
+  __syncthreads();
+  for (long long i = 0; i < fr.emitted; ++i) {
+    if (threadIdx.x == 0) lbs[i] = D.out_lb[i];
+    decode_box(D, D.out_key[i], boxes + 2LL * n * i);
+  }
+  // the smallest list entries, one selection pass each, in (LB, key) order
+  unsigned long long prev_lbk = 0, prev_key = 0;
+  bool first = true;
+  for (long long r = fr.emitted; r < fr.k; ++r) {
+    unsigned long long bl = ~0ULL, bk = ~0ULL;
+    for (long long i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const unsigned long long l = ord_key(plb[i]), k = pkey[i];
+      const bool after = first || l > prev_lbk || (l == prev_lbk && k > prev_key);
+      if (after && (l < bl || (l == bl && k < bk))) { bl = l; bk = k; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long yl = __shfl_xor_sync(0xffffffffu, bl, off);
+      const unsigned long long yk = __shfl_xor_sync(0xffffffffu, bk, off);
+      if (yl < bl || (yl == bl && yk < bk)) { bl = yl; bk = yk; }
+    }
+    if (lane == 0) { s_k[wid] = bl; s_v[wid] = __longlong_as_double((long long)bk); }
+    __syncthreads();
+    bl = s_k[0]; bk = (unsigned long long)__double_as_longlong(s_v[0]);
+    for (int w = 1; w < nw; ++w) {
+      const unsigned long long yl = s_k[w], yk = (unsigned long long)__double_as_longlong(s_v[w]);
+      if (yl < bl || (yl == bl && yk < bk)) { bl = yl; bk = yk; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) lbs[r] = ord_val(bl);
+    decode_box(D, bk, boxes + 2LL * n * r);
+    prev_lbk = bl; prev_key = bk; first = false;
+  }
+  // the sample point that set the UB
+  const long long rows = (S.iter + 1 < D.parent_cap) ? S.iter + 1 : D.parent_cap;
+  const long long prow = (long long)(S.ub_who >> 40);
+  const bool has = S.has_who && prow < rows;
+  if (has) {
+    const unsigned long long key = ((unsigned long long)prow << 32) | ((S.ub_who >> 8) & 0xffffffffULL);
+    const int j = (int)(S.ub_who & 0xff);
+    const int cyc = D.pcyc[prow];
+    const int gsz = group_size(n, D.group, cyc);
+    const unsigned long long pc = pack_code(D, gsz, key & 0xffffffffULL);
+    const double* pb = D.parents + 2LL * n * prow;
+    const double* pw = D.pwid + (long long)n * prow;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const iv x = child_iv(D, pb, pw, cyc - 1, gsz, i, digit(D, cyc - 1, gsz, pc, i));
+      xh[i] = sample_pt(x, D.S, j);
+    }
+  }
+  if (threadIdx.x == 0) xh[n] = has ? 1.0 : 0.0;
+}
+
+// Admission of the problems submitted since the last run: one block per record
+// (word offsets in offs): slot, 2n, ncoef, the Desc, the initial State, domain,
+// coefficients.  The block writes them into place (the domain also as parent
+// row 0) and derives the constants.
+constexpr int DESC_WORDS = (int)((sizeof(Desc) + 7) / 8);
+constexpr int STATE_WORDS = (int)((sizeof(State) + 7) / 8);
+__global__ void admit_kernel(Desc* desc, State* st, const unsigned long long* stage, const long long* offs) {
+  const unsigned long long* r = stage + offs[blockIdx.x];
+  const int s = (int)r[0];
+  const long long ndom = (long long)r[1], ncoef = (long long)r[2];
+  const unsigned long long* dw = r + 3;
+  const unsigned long long* sw = dw + DESC_WORDS;
+  const double* dom = (const double*)(sw + STATE_WORDS);
+  const double* coef = dom + ndom;
+  unsigned long long* ddst = (unsigned long long*)(desc + s);
+  unsigned long long* sdst = (unsigned long long*)(st + s);
+  for (int i = threadIdx.x; i < DESC_WORDS; i += blockDim.x) ddst[i] = dw[i];
+  for (int i = threadIdx.x; i < STATE_WORDS; i += blockDim.x) sdst[i] = sw[i];
+  const Desc* hd = (const Desc*)dw;  // the record's copy (its pointers are device addresses)
+  double* ddom = (double*)hd->dom;
+  double* dcoef = (double*)hd->coef;
+  for (long long i = threadIdx.x; i < ndom; i += blockDim.x) {
+    ddom[i] = dom[i];
+    hd->parents[i] = dom[i];
+  }
+  for (long long i = threadIdx.x; i < ncoef; i += blockDim.x) dcoef[i] = coef[i];
+  if (threadIdx.x == 0) hd->pcyc[0] = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) init_consts(desc[s]);
 }
 
 // standalone table build and per-child evaluation (gpugo_eval_children)
@@ -1646,6 +1778,14 @@ struct gpugo_engine {
   Arena arena;
   std::vector<HostSlot> slots;
   std::vector<int> pending_init;
+  // admissions since the last run, packed as records (admit_kernel's layout)
+  std::vector<unsigned long long> stage;
+  std::vector<long long> stage_offs;
+  char* d_stage = nullptr;
+  size_t d_stage_cap = 0;
+  // results of finished instances (finalize_kernel records)
+  char* d_fin = nullptr;
+  size_t d_fin_cap = 0;
   int64_t next_ticket = 1;
   std::vector<State> h_state;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -2148,6 +2288,8 @@ int gpugo_engine_destroy(gpugo_engine* E) {
   if (E->stream) cudaStreamSynchronize(E->stream);
   cudaFree(E->d_desc); cudaFree(E->d_state); cudaFree(E->d_ctl);
   cudaFree(E->d_ids); cudaFree(E->d_queue); cudaFree(E->d_cands); cudaFree(E->d_pref); cudaFree(E->d_arena); cudaFree(E->d_stamps); cudaFree(E->d_bstamps);
+  cudaFree(E->d_stage);
+  cudaFree(E->d_fin);
   if (E->ev0) cudaEventDestroy(E->ev0);
   if (E->ev1) cudaEventDestroy(E->ev1);
   if (E->stream) cudaStreamDestroy(E->stream);
@@ -2199,31 +2341,30 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
   if (trace) { h.trace = *trace; h.has_trace = true; }
   char* base = E->d_arena + off;
   fill_desc(&h.spec, L, base, &h.desc);
-  cudaStream_t st = E->stream;
-  rc = GPUGO_OK;
-  do {
-    if ((rc = cuda_err(cudaMemcpyAsync((void*)h.desc.dom, h.dom.data(), 8 * h.dom.size(), cudaMemcpyHostToDevice, st)))) break;
-    if ((rc = cuda_err(cudaMemcpyAsync((void*)h.desc.coef, h.coef.data(), 8 * h.coef.size(), cudaMemcpyHostToDevice, st)))) break;
-    if ((rc = cuda_err(cudaMemcpyAsync(h.desc.parents, h.dom.data(), 8 * h.dom.size(), cudaMemcpyHostToDevice, st)))) break;
-    int one = 1;
-    if ((rc = cuda_err(cudaMemcpyAsync(h.desc.pcyc, &one, 4, cudaMemcpyHostToDevice, st)))) break;
-    if ((rc = cuda_err(cudaMemcpyAsync(E->d_desc + slot, &h.desc, sizeof(Desc), cudaMemcpyHostToDevice, st)))) break;
-    State s0;
-    memset(&s0, 0, sizeof(s0));
-    s0.status = ST_EXPAND;
-    s0.cyc = 1;
-    double ub0 = spec->ub_init;
-    if (ub0 == 0.0) ub0 = 0.0;
-    s0.ub = ord_key_host(ub0);
-    s0.ub_start = s0.ub;
-    s0.seed_key = ~0ULL;
-    s0.out_lb_min = INFINITY;
-    s0.m_children = children_host(spec, 1);
-    if ((rc = cuda_err(cudaMemcpyAsync(E->d_state + slot, &s0, sizeof(State), cudaMemcpyHostToDevice, st)))) break;
-    if ((rc = cuda_err(cudaStreamSynchronize(st)))) break;
-    E->h2d += (int64_t)(8 * h.dom.size() * 2 + 8 * h.coef.size() + 4 + sizeof(Desc) + sizeof(State));
-  } while (0);
-  if (rc) { E->arena.release(off, h.arena_bytes); h = HostSlot(); return rc; }
+  State s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.status = ST_EXPAND;
+  s0.cyc = 1;
+  double ub0 = spec->ub_init;
+  if (ub0 == 0.0) ub0 = 0.0;
+  s0.ub = ord_key_host(ub0);
+  s0.ub_start = s0.ub;
+  s0.seed_key = ~0ULL;
+  s0.out_lb_min = INFINITY;
+  s0.m_children = children_host(spec, 1);
+  // one record for admit_kernel; copied with the others when the engine next runs
+  const size_t at = E->stage.size();
+  const size_t words = 3 + DESC_WORDS + STATE_WORDS + h.dom.size() + h.coef.size();
+  E->stage.resize(at + words, 0ULL);
+  unsigned long long* rec = E->stage.data() + at;
+  rec[0] = (unsigned long long)slot;
+  rec[1] = (unsigned long long)h.dom.size();
+  rec[2] = (unsigned long long)h.coef.size();
+  memcpy(rec + 3, &h.desc, sizeof(Desc));
+  memcpy(rec + 3 + DESC_WORDS, &s0, sizeof(State));
+  memcpy(rec + 3 + DESC_WORDS + STATE_WORDS, h.dom.data(), 8 * h.dom.size());
+  memcpy(rec + 3 + DESC_WORDS + STATE_WORDS + h.dom.size(), h.coef.data(), 8 * h.coef.size());
+  E->stage_offs.push_back((long long)at);
   E->pending_init.push_back(slot);
   if (ticket_out) *ticket_out = h.ticket;
   return GPUGO_OK;
@@ -2233,14 +2374,31 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   if (!E) return GPUGO_ERR_INVALID;
   cudaStream_t st = E->stream;
   if (!E->pending_init.empty()) {
-    int m = (int)E->pending_init.size();
-    int* d_list = E->d_ids + 2 * E->max_slots;
-    CK(cudaMemcpyAsync(d_list, E->pending_init.data(), 4 * m, cudaMemcpyHostToDevice, st));
-    init_slots_kernel<<<(m + 127) / 128, 128, 0, st>>>(E->d_desc, E->d_state, d_list, m);
+    // every admission since the last run: one copy, one kernel
+    const int m = (int)E->stage_offs.size();
+    const size_t rec_bytes = 8 * E->stage.size(), off_bytes = 8 * (size_t)m;
+    const size_t need = ((off_bytes + 255) & ~size_t(255)) + rec_bytes;
+    if (need > E->d_stage_cap) {
+      const size_t cap = std::max<size_t>(need, 2 * E->d_stage_cap);
+      CK(cudaStreamSynchronize(st));
+      cudaFree(E->d_stage);
+      E->d_stage = nullptr;
+      E->d_stage_cap = 0;
+      CK(cudaMalloc(&E->d_stage, cap));
+      E->d_stage_cap = cap;
+    }
+    long long* d_offs = (long long*)E->d_stage;
+    unsigned long long* d_rec = (unsigned long long*)(E->d_stage + ((off_bytes + 255) & ~size_t(255)));
+    // pageable sources: the copies are staged by the runtime before the calls return
+    CK(cudaMemcpyAsync(d_offs, E->stage_offs.data(), off_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_rec, E->stage.data(), rec_bytes, cudaMemcpyHostToDevice, st));
+    admit_kernel<<<m, 128, 0, st>>>(E->d_desc, E->d_state, d_rec, d_offs);
     CK(cudaGetLastError());
-    E->h2d += 4 * m;
+    E->h2d += (int64_t)(rec_bytes + off_bytes);
     E->launches++;
     E->pending_init.clear();
+    E->stage.clear();
+    E->stage_offs.clear();
   }
   CK(cudaMemsetAsync(E->d_ctl, 0, sizeof(Ctl), st));
   KArgs a;
@@ -2308,20 +2466,101 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
 
 int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_done_out) {
   if (!E) return GPUGO_ERR_INVALID;
+  std::vector<int> fin;
+  for (int s = 0; s < E->max_slots && (int)fin.size() < max_done; ++s)
+    if (E->slots[s].used && E->h_state[s].status == ST_DONE) fin.push_back(s);
+  // Small outputs (no trace, at most 64 boxes) come from finalize_kernel records,
+  // all finished instances in one launch and one copy; the others are collected
+  // from their lists and parent tables.
+  std::vector<FinRec> recs;
+  std::vector<int> rec_of(fin.size(), -1);
+  long long total = 0;
+  for (size_t f = 0; f < fin.size(); ++f) {
+    const int s = fin[f];
+    const HostSlot& h = E->slots[s];
+    const State& st = E->h_state[s];
+    if (h.has_trace || h.cap > 64) continue;
+    const long long cnt = std::min<long long>(st.count, h.desc.pool_cap);
+    const long long nout = std::min<long long>(st.out_count, h.desc.out_cap);
+    const long long emitted = std::min<long long>(nout, h.cap);
+    const long long pool_boxes = (h.spec.stop_mode == GPUGO_STOP_GAP) ? cnt : 0;
+    const long long k = std::min<long long>(h.cap, nout + pool_boxes);
+    FinRec r;
+    r.slot = s; r.k = k; r.emitted = emitted; r.off = total;
+    total += 2 + k + 2LL * h.spec.n * k + h.spec.n + 1;
+    rec_of[f] = (int)recs.size();
+    recs.push_back(r);
+  }
+  std::vector<double> out;
+  if (!recs.empty()) {
+    cudaStream_t st = E->stream;
+    const size_t rb = (sizeof(FinRec) * recs.size() + 255) & ~size_t(255);
+    const size_t need = rb + 8 * (size_t)total;
+    if (need > E->d_fin_cap) {
+      const size_t cap = std::max<size_t>(need, 2 * E->d_fin_cap);
+      CK(cudaStreamSynchronize(st));
+      cudaFree(E->d_fin);
+      E->d_fin = nullptr;
+      E->d_fin_cap = 0;
+      CK(cudaMalloc(&E->d_fin, cap));
+      E->d_fin_cap = cap;
+    }
+    FinRec* d_recs = (FinRec*)E->d_fin;
+    double* d_out = (double*)(E->d_fin + rb);
+    CK(cudaMemcpyAsync(d_recs, recs.data(), sizeof(FinRec) * recs.size(), cudaMemcpyHostToDevice, st));
+    finalize_kernel<<<(unsigned)recs.size(), 256, 0, st>>>(E->d_desc, E->d_state, d_recs, d_out);
+    CK(cudaGetLastError());
+    out.resize((size_t)total);
+    CK(cudaMemcpyAsync(out.data(), d_out, 8 * (size_t)total, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    E->launches++;
+    E->h2d += (int64_t)(sizeof(FinRec) * recs.size());
+    E->d2h += (int64_t)(8 * total);
+  }
   int k = 0;
-  for (int s = 0; s < E->max_slots && k < max_done; ++s) {
+  for (size_t f = 0; f < fin.size(); ++f) {
+    const int s = fin[f];
     HostSlot& h = E->slots[s];
-    if (!h.used || E->h_state[s].status != ST_DONE) continue;
     gpugo_result r;
-    int rc = collect(E, s, &r);
-    if (rc) return rc;
+    if (rec_of[f] < 0) {
+      int rc = collect(E, s, &r);
+      if (rc) return rc;
+    } else {
+      const FinRec& fr = recs[rec_of[f]];
+      const State& st = E->h_state[s];
+      const int n = h.spec.n;
+      const double* o = out.data() + fr.off;
+      memset(&r, 0, sizeof(r));
+      r.lb = o[0];
+      r.ub = ord_val_host(st.ub);
+      r.boxes_bounded = st.bounded;
+      r.samples_evaluated = st.samples;
+      r.status = st.outcome;
+      r.iterations = (st.outcome == GPUGO_ITER_LIMIT) ? st.iter : st.iter + 1;
+      const long long cnt = std::min<long long>(st.count, h.desc.pool_cap);
+      r.pool_size = cnt;
+      r.n_boxes = st.out_count + ((h.spec.stop_mode == GPUGO_STOP_GAP) ? cnt : 0);
+      r.n_out = (int32_t)fr.k;
+      const double* lbs = o + 2;
+      const double* boxes = lbs + fr.k;
+      const double* xh = boxes + 2LL * n * fr.k;
+      if (h.boxes_out && fr.k) memcpy(h.boxes_out, boxes, sizeof(double) * 2 * n * (size_t)fr.k);
+      if (h.box_lb_out && fr.k) memcpy(h.box_lb_out, lbs, sizeof(double) * (size_t)fr.k);
+      r.has_xhat = 0;
+      if (xh[n] != 0.0 && h.xhat_out) {
+        memcpy(h.xhat_out, xh, sizeof(double) * n);
+        r.has_xhat = 1;
+      }
+      r.d2h_bytes = (int64_t)(8 * (2 + fr.k + 2LL * n * fr.k + n + 1));
+    }
     done[k].ticket = h.ticket;
     done[k].result = r;
     k++;
     E->arena.release(h.arena_off, h.arena_bytes);
+    // the device state keeps ST_DONE (out of every work list) until the slot's
+    // next admission overwrites it
     State z;
     memset(&z, 0, sizeof(z));
-    CK(cudaMemcpy(E->d_state + s, &z, sizeof(State), cudaMemcpyHostToDevice));
     E->h_state[s] = z;
     h = HostSlot();
   }

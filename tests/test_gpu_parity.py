@@ -187,6 +187,29 @@ def test_engine_batch_matches_oracle(oracle_lib, mode):
         assert _same(rg.box_lbs, ro.box_lbs), p.tag
 
 
+def test_finalized_results_match_collected():
+    """Results of small outputs are assembled on the device (finalize_kernel);
+    the host path (taken with a trace) gives the same bits."""
+    probs = [make() for _, make in CFGS + WIDE]
+    w = P.instance(P.COSQUAD, 4, 99, tol=0.0, split=(4, 2))
+    w.stop_mode = P.STOP_WIDTH
+    w.width_tol = 1e-3
+    w.ub_init = 1e6
+    probs.append(w)
+    for p in probs:
+        p.max_iter = 3000
+    for cap in (1, 16):
+        for p in probs:
+            x = G.solve(p, box_cap=cap, trace_cap=100000)   # host path
+            y = G.solve(p, box_cap=cap)                     # device records
+            assert (x.lb, x.ub, x.iterations, x.status, x.pool_size, x.n_boxes) == \
+                (y.lb, y.ub, y.iterations, y.status, y.pool_size, y.n_boxes), p.tag
+            assert _same(x.boxes, y.boxes) and _same(x.box_lbs, y.box_lbs), p.tag
+            assert (x.xhat is None) == (y.xhat is None), p.tag
+            if x.xhat is not None:
+                assert _same(x.xhat, y.xhat), p.tag
+
+
 def test_pool_overflow_reports_error():
     """Host-side fault injection: a pool too small for the survivors."""
     p = P.config2()
