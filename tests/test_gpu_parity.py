@@ -187,6 +187,26 @@ def test_engine_batch_matches_oracle(oracle_lib, mode):
         assert _same(rg.box_lbs, ro.box_lbs), p.tag
 
 
+EDGE = [
+    ("cosquad1", lambda: P.instance(P.COSQUAD, 1, 31, 1e-6)),
+    ("chained2_s1", lambda: P.instance(P.CHAINED, 2, 32, 1e-6, samples=1)),
+    ("expsqrt6_s20", lambda: P.instance(P.EXPSQRT, 6, 33, 1e-5, samples=20)),
+    ("expsqrt9_s14", lambda: P.instance(P.EXPSQRT, 9, 34, 1e-5, samples=14)),
+    ("prodcos5_s40", lambda: P.instance(P.PRODCOS, 5, 35, 1e-6, samples=40)),
+    ("cosquad3_w9", lambda: P.instance(P.COSQUAD, 3, 36, 1e-6, split=(9, 3), samples=3)),
+]
+
+
+@pytest.mark.parametrize("name,make", EDGE, ids=[c[0] for c in EDGE])
+def test_solve_trace_parity_edge_shapes(oracle_lib, name, make):
+    """One variable, one sample point, more sample points than lanes, the largest
+    sample count the warp-wide exp-sqrt path takes and the first it does not."""
+    p = make()
+    p.max_iter = 3000
+    rg, ro = _compare_solves(p, oracle_lib, box_cap=16)
+    assert rg.status == G.CERTIFIED
+
+
 def test_finalized_results_match_collected():
     """Results of small outputs are assembled on the device (finalize_kernel);
     the host path (taken with a trace) gives the same bits."""
