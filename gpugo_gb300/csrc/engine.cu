@@ -1330,29 +1330,45 @@ __device__ void phase_pool(const KArgs& a) {
     const long long lo = tile * TD, hi = min(cnt, lo + TD);
     Best b = best_none();
     long long removed_new = 0;
-    for (long long e0 = lo; e0 < hi; e0 += blockDim.x) {
-      long long e = e0 + threadIdx.x;
-      bool in = e < hi;
-      double lbv = in ? D.pool_lb[cur][e] : 0.0;
-      unsigned long long key = in ? D.pool_key[cur][e] : 0ULL;
-      bool keep = in && (!compact || !flt(ub, lbv));
-      unsigned long long pos = (unsigned long long)e;
+    // the tile's entries are loaded all at once (TD / blockDim per thread, at most
+    // 8), then filtered; the kept ones get one block-wide offset from a single
+    // atomic per tile (the order inside the new buffer is free: selection ties
+    // are broken by key, not by position)
+    constexpr int PER = 8;
+    double lbv[PER];
+    unsigned long long key[PER];
+    bool keep[PER];
+    int nk = 0;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const long long e = lo + threadIdx.x + (long long)j * blockDim.x;
+      const bool in = e < hi && j * (int)blockDim.x < TD;
+      lbv[j] = in ? D.pool_lb[cur][e] : 0.0;
+      key[j] = in ? D.pool_key[cur][e] : 0ULL;
+      keep[j] = in && (!compact || !flt(ub, lbv[j]));
+      if (compact && in && !keep[j] && e >= st.count_before) removed_new++;
+      nk += keep[j] ? 1 : 0;
+    }
+    unsigned long long base = 0;
+    if (compact) {
+      __shared__ unsigned long long s_base;
+      long long tk;
+      const long long off = block_exclusive_scan((long long)nk, &tk);
+      if (threadIdx.x == 0) s_base = tk ? atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk) : 0ULL;
+      __syncthreads();
+      base = s_base + (unsigned long long)off;
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      if (!keep[j]) continue;
+      unsigned long long pos = (unsigned long long)(lo + threadIdx.x + (long long)j * blockDim.x);
       if (compact) {
-        if (in && !keep && e >= st.count_before) removed_new++;
-        unsigned int km = __ballot_sync(0xffffffffu, keep);
-        unsigned long long wbase = 0;
-        if (lane == 0 && km) wbase = atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)__popc(km));
-        wbase = __shfl_sync(0xffffffffu, wbase, 0);
-        if (keep) {
-          pos = wbase + __popc(km & ((1u << lane) - 1u));
-          D.pool_lb[cur ^ 1][pos] = lbv;
-          D.pool_key[cur ^ 1][pos] = key;
-        }
+        pos = base++;
+        D.pool_lb[cur ^ 1][pos] = lbv[j];
+        D.pool_key[cur ^ 1][pos] = key[j];
       }
-      if (keep) {
-        Best c; c.lbk = ord_key(lbv); c.key = key; c.idx = pos;
-        if (best_less(c, b)) b = c;
-      }
+      Best c; c.lbk = ord_key(lbv[j]); c.key = key[j]; c.idx = pos;
+      if (best_less(c, b)) b = c;
     }
     if (compact) {
       for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
