@@ -364,6 +364,46 @@ def run_serving(args):
             **{k: v for k, v in sm.items() if k not in ("p50_ms", "p99_ms")}}
 
 
+def run_list_pass(args):
+    """The grid-wide list pass on large lists: the 50-variable Rastrigin script's
+    loop (4^10 children per iteration, rastrigin50.py:844-1289) for a few
+    iterations; the list grows by about 1 Mi entries per iteration.  The pass
+    is timed with the engine's phase stamps (GPUGO_PHASE_STAMPS) and its
+    algorithmic bytes are 16 B per entry read plus 16 B per entry written."""
+    import os
+    import tempfile
+    import numpy as np
+    path = os.path.join(tempfile.mkdtemp(), "stamps")
+    os.environ["GPUGO_PHASE_STAMPS"] = path
+    import gpugo_gb300 as G
+    from gpugo_gb300 import problems as P
+    n = 50
+    p = P.Problem(P.COSQUAD, n, np.tile([-5.5, 6.0], n), np.concatenate([np.ones(n), np.full(n, 10.0), np.ones(n)]),
+                  wid=4, group=10, samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6,
+                  max_iter=args.steps, pool_cap=1 << 26)
+    with G.Engine(max_slots=1, arena_bytes=8 << 30) as eng:
+        eng.submit(p, box_cap=4, trace_cap=4096)
+        eng.run(0)
+        (_, r), = eng.poll()
+    rows = open(path).read().strip().split("run ")[-1].split("\n")[1:]
+    st = np.array([[int(x) for x in l.split()] for l in rows], dtype=np.float64)
+    per = []
+    for it in range(st.shape[0]):
+        if st[it, 3] <= 0:
+            continue
+        us = (st[it, 3] - st[it, 2]) / 1e3
+        n_in = (r.trace["pool"][it - 1] if it > 0 else 0) + r.trace["n_surv"][it]
+        n_out = r.trace["pool"][it]
+        per.append({"iteration": it, "entries_in": int(n_in), "entries_out": int(n_out), "us": round(us, 1),
+                    "GBps": round((n_in + n_out) * 16 / (us * 1e-6) / 1e9, 1)})
+    big = [d for d in per if d["entries_in"] >= (1 << 20) and d["entries_out"] >= (1 << 20)]
+    best = max(big, key=lambda d: d["GBps"]) if big else None
+    return {"metric": "list pass GB/s (algorithmic)", "value": best["GBps"] if best else None, "unit": "GB/s",
+            "n_gpus": 1, "dtype": "f64/u64", "config": {"workload": "rastrigin50 reference loop, 4^10 children/iter",
+                                                      "iterations": int(st.shape[0])},
+            "per_iteration": per}
+
+
 def run_single(args):
     import gpugo_gb300 as G
     from gpugo_gb300 import problems as P
@@ -388,7 +428,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpugo", choices=["gpugo", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5"],
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "listpass"],
                     help="cfg2 is the benchmark line; the others print their own records")
     ap.add_argument("--count", type=int, default=1024)
     ap.add_argument("--rate", type=float, default=20000.0)
@@ -400,7 +440,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     if args.workload != "cfg2" and args.impl == "gpugo":
-        fn = {"cfg1": run_single, "cfg3": run_single, "cfg4": run_batched, "cfg5": run_serving}[args.workload]
+        fn = {"cfg1": run_single, "cfg3": run_single, "cfg4": run_batched, "cfg5": run_serving,
+              "listpass": run_list_pass}[args.workload]
         print(json.dumps(fn(args)))
         return
     if args.impl == "reference":
