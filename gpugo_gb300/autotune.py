@@ -29,7 +29,7 @@ from . import _lib
 from .problems import Problem
 
 # split options tried for instances of n >= 8 (odd wid: see problems.default_split)
-FANOUT_OPTIONS: tuple[tuple[int, int], ...] = ((3, 6), (3, 8), (5, 5), (3, 10))
+FANOUT_OPTIONS: tuple[tuple[int, int], ...] = ((3, 4), (3, 5), (3, 6), (3, 8), (5, 4), (5, 5), (3, 10))
 # dimension classes for the fan-out choice (instances with n < 8 keep the default table)
 N_CLASSES: tuple[tuple[int, int], ...] = ((8, 16), (17, 32), (33, 64), (65, 4096))
 
