@@ -201,6 +201,31 @@ class Engine:
         self._pending[t.value] = (p, boxes, lbs, xhat, arrs, tr, keep)
         return t.value
 
+    def checkpoint(self, ticket: int) -> bytes:
+        """Serialise a resident solve (between runs): problem, state, parent table,
+        list, emitted boxes and trace."""
+        size = ctypes.c_int64()
+        _lib.check(self._L.gpugo_checkpoint(self._h, int(ticket), None, 0, ctypes.byref(size)), "gpugo_checkpoint")
+        buf = ctypes.create_string_buffer(size.value)
+        _lib.check(self._L.gpugo_checkpoint(self._h, int(ticket), buf, size.value, ctypes.byref(size)),
+                   "gpugo_checkpoint")
+        return buf.raw[:size.value]
+
+    def restore(self, p: Problem, data: bytes, box_cap: int = 16, trace_cap: int = 0) -> int | None:
+        """Admit a checkpointed solve of problem ``p``; it continues where the
+        checkpoint was taken.  ``None`` when no slot or memory is free."""
+        boxes, lbs, xhat, tr, arrs = _alloc_out(p, box_cap, trace_cap)
+        t = ctypes.c_int64()
+        buf = ctypes.create_string_buffer(bytes(data), len(data))
+        rc = self._L.gpugo_restore(self._h, buf, len(data), boxes.ctypes.data_as(_dp), lbs.ctypes.data_as(_dp),
+                                   box_cap, xhat.ctypes.data_as(_dp), ctypes.byref(tr) if tr is not None else None,
+                                   ctypes.byref(t))
+        if rc == _lib.ERR_BUSY:
+            return None
+        _lib.check(rc, "gpugo_restore")
+        self._pending[t.value] = (p, boxes, lbs, xhat, arrs, tr, None)
+        return t.value
+
     def run(self, max_iters: int = 0) -> int:
         active = ctypes.c_int32()
         _lib.check(self._L.gpugo_run(self._h, int(max_iters), ctypes.byref(active)), "gpugo_run")

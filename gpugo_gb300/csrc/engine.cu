@@ -1590,8 +1590,10 @@ __global__ void __launch_bounds__(256) finalize_kernel(const Desc* desc, const S
 
 // Admission of the problems submitted since the last run: one block per record
 // (word offsets in offs): slot, 2n, ncoef, the Desc, the initial State, domain,
-// coefficients.  The block writes them into place (the domain also as parent
-// row 0) and derives the constants.
+// coefficients, then segments (device address, bytes, payload in words) that a
+// restored checkpoint carries (parent table, list, emitted boxes, trace).  The
+// block writes them into place (the domain also as parent row 0) and derives
+// the constants.
 constexpr int DESC_WORDS = (int)((sizeof(Desc) + 7) / 8);
 constexpr int STATE_WORDS = (int)((sizeof(State) + 7) / 8);
 __global__ void admit_kernel(Desc* desc, State* st, const unsigned long long* stage, const long long* offs) {
@@ -1615,6 +1617,17 @@ __global__ void admit_kernel(Desc* desc, State* st, const unsigned long long* st
   }
   for (long long i = threadIdx.x; i < ncoef; i += blockDim.x) dcoef[i] = coef[i];
   if (threadIdx.x == 0) hd->pcyc[0] = 1;
+  __syncthreads();
+  const unsigned long long* sg = (const unsigned long long*)(coef + ncoef);
+  const long long nseg = (long long)sg[0];
+  sg += 1;
+  for (long long q = 0; q < nseg; ++q) {
+    unsigned char* dst = (unsigned char*)sg[0];
+    const long long nbytes = (long long)sg[1];
+    const unsigned char* src = (const unsigned char*)(sg + 2);
+    for (long long i = threadIdx.x; i < nbytes; i += blockDim.x) dst[i] = src[i];
+    sg += 2 + (nbytes + 7) / 8;
+  }
   __syncthreads();
   if (threadIdx.x == 0) init_consts(desc[s]);
 }
@@ -2330,8 +2343,22 @@ int gpugo_engine_free_bytes(gpugo_engine* E, int64_t* free_out) {
   return GPUGO_OK;
 }
 
-int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* box_lb_out, int64_t cap,
-                 double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+}  // extern "C"
+
+namespace {
+// A payload piece of an admission record: bytes copied into the instance's region.
+struct Piece {
+  size_t arena_rel;     // destination: byte offset inside the instance's arena region
+  const void* src;      // host bytes
+  size_t bytes;
+};
+
+// Admission of one problem: a slot, an arena region, the record admit_kernel
+// applies at the next run.  `saved` (may be null) replaces the initial state and
+// `pieces` are copied into the region (a restored checkpoint).
+int admit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* box_lb_out, int64_t cap,
+          double* xhat_out, gpugo_trace* trace, const State* saved, const std::vector<Piece>& pieces,
+          int64_t* ticket_out) {
   if (!E) return GPUGO_ERR_INVALID;
   int rc = validate(spec);
   if (rc) return rc;
@@ -2368,9 +2395,12 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
   s0.seed_key = ~0ULL;
   s0.out_lb_min = INFINITY;
   s0.m_children = children_host(spec, 1);
+  if (saved) s0 = *saved;
   // one record for admit_kernel; copied with the others when the engine next runs
   const size_t at = E->stage.size();
-  const size_t words = 3 + DESC_WORDS + STATE_WORDS + h.dom.size() + h.coef.size();
+  size_t seg_words = 1;
+  for (const Piece& pc : pieces) seg_words += 2 + (pc.bytes + 7) / 8;
+  const size_t words = 3 + DESC_WORDS + STATE_WORDS + h.dom.size() + h.coef.size() + seg_words;
   E->stage.resize(at + words, 0ULL);
   unsigned long long* rec = E->stage.data() + at;
   rec[0] = (unsigned long long)slot;
@@ -2380,10 +2410,157 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
   memcpy(rec + 3 + DESC_WORDS, &s0, sizeof(State));
   memcpy(rec + 3 + DESC_WORDS + STATE_WORDS, h.dom.data(), 8 * h.dom.size());
   memcpy(rec + 3 + DESC_WORDS + STATE_WORDS + h.dom.size(), h.coef.data(), 8 * h.coef.size());
+  unsigned long long* sg = rec + 3 + DESC_WORDS + STATE_WORDS + h.dom.size() + h.coef.size();
+  *sg++ = (unsigned long long)pieces.size();
+  for (const Piece& pc : pieces) {
+    sg[0] = (unsigned long long)(uintptr_t)(base + pc.arena_rel);
+    sg[1] = (unsigned long long)pc.bytes;
+    memcpy(sg + 2, pc.src, pc.bytes);
+    sg += 2 + (pc.bytes + 7) / 8;
+  }
   E->stage_offs.push_back((long long)at);
   E->pending_init.push_back(slot);
   if (ticket_out) *ticket_out = h.ticket;
   return GPUGO_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* box_lb_out, int64_t cap,
+                 double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+  return admit(E, spec, boxes_out, box_lb_out, cap, xhat_out, trace, nullptr, {}, ticket_out);
+}
+
+// ---------------------------------------------------------------------------
+// checkpoint / resume of one instance (between runs)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+namespace {
+struct CkptHeader {
+  char magic[8];                      // "GPUGOCK1"
+  int32_t family, n, wid, group, samples, stop_mode;
+  double width_tol, gap_tol, ub_init;
+  int64_t ncoef, max_iter, pool_cap, parent_cap;
+  State st;
+  int64_t rows, cnt, nout, ntrace;
+};
+const char CKPT_MAGIC[8] = {'G', 'P', 'U', 'G', 'O', 'C', 'K', '1'};
+size_t pad8(size_t b) { return (b + 7) & ~size_t(7); }
+}  // namespace
+extern "C" {
+
+int gpugo_checkpoint(gpugo_engine* E, int64_t ticket, void* buf, int64_t cap, int64_t* bytes_out) {
+  if (!E || !bytes_out) return GPUGO_ERR_INVALID;
+  int slot = -1;
+  for (int s = 0; s < E->max_slots; ++s)
+    if (E->slots[s].used && E->slots[s].ticket == ticket) { slot = s; break; }
+  if (slot < 0) return GPUGO_ERR_NOT_FOUND;
+  for (int p : E->pending_init)
+    if (p == slot) return GPUGO_ERR_BUSY;   // not admitted to the device yet: run first
+  const HostSlot& h = E->slots[slot];
+  const State& st = E->h_state[slot];
+  const Desc& D = h.desc;
+  const int n = h.spec.n;
+  CkptHeader hd;
+  memset(&hd, 0, sizeof(hd));
+  memcpy(hd.magic, CKPT_MAGIC, 8);
+  hd.family = h.spec.family; hd.n = n; hd.wid = h.spec.wid; hd.group = h.spec.group;
+  hd.samples = h.spec.samples; hd.stop_mode = h.spec.stop_mode;
+  hd.width_tol = h.spec.width_tol; hd.gap_tol = h.spec.gap_tol; hd.ub_init = h.spec.ub_init;
+  hd.ncoef = h.spec.ncoef; hd.max_iter = h.spec.max_iter; hd.pool_cap = h.spec.pool_cap;
+  hd.parent_cap = h.spec.parent_cap;
+  hd.st = st;
+  hd.rows = std::min<int64_t>(st.iter + 1, D.parent_cap);
+  hd.cnt = std::min<int64_t>(st.count, D.pool_cap);
+  hd.nout = std::min<int64_t>(st.out_count, D.out_cap);
+  hd.ntrace = std::min<int64_t>(st.iter + 1, D.trace_cap);
+  const size_t total = pad8(sizeof(hd)) + 8 * (2 * (size_t)n + (size_t)hd.ncoef) + 8 * 3 * (size_t)n * hd.rows +
+                       pad8(4 * (size_t)hd.rows) + 16 * (size_t)hd.cnt + 16 * (size_t)hd.nout +
+                       32 * (size_t)hd.ntrace;
+  *bytes_out = (int64_t)total;
+  if (!buf) return GPUGO_OK;
+  if (cap < (int64_t)total) return GPUGO_ERR_INVALID;
+  char* o = (char*)buf;
+  memset(o, 0, total);
+  memcpy(o, &hd, sizeof(hd));
+  o += pad8(sizeof(hd));
+  memcpy(o, h.dom.data(), 16 * (size_t)n); o += 16 * (size_t)n;
+  memcpy(o, h.coef.data(), 8 * (size_t)hd.ncoef); o += 8 * (size_t)hd.ncoef;
+  auto D2H = [&](const void* src, size_t bytes, size_t advance) -> int {
+    if (bytes) {
+      int rc = cuda_err(cudaMemcpy(o, src, bytes, cudaMemcpyDeviceToHost));
+      if (rc) return rc;
+      E->d2h += (int64_t)bytes;
+    }
+    o += advance;
+    return GPUGO_OK;
+  };
+  int rc;
+  if ((rc = D2H(D.parents, 16 * (size_t)n * hd.rows, 16 * (size_t)n * hd.rows))) return rc;
+  if ((rc = D2H(D.pwid, 8 * (size_t)n * hd.rows, 8 * (size_t)n * hd.rows))) return rc;
+  if ((rc = D2H(D.pcyc, 4 * (size_t)hd.rows, pad8(4 * (size_t)hd.rows)))) return rc;
+  if ((rc = D2H(D.pool_lb[st.cur], 8 * (size_t)hd.cnt, 8 * (size_t)hd.cnt))) return rc;
+  if ((rc = D2H(D.pool_key[st.cur], 8 * (size_t)hd.cnt, 8 * (size_t)hd.cnt))) return rc;
+  if ((rc = D2H(D.out_key, 8 * (size_t)hd.nout, 8 * (size_t)hd.nout))) return rc;
+  if ((rc = D2H(D.out_lb, 8 * (size_t)hd.nout, 8 * (size_t)hd.nout))) return rc;
+  if ((rc = D2H(D.tr_ub, 8 * (size_t)hd.ntrace, 8 * (size_t)hd.ntrace))) return rc;
+  if ((rc = D2H(D.tr_surv, 8 * (size_t)hd.ntrace, 8 * (size_t)hd.ntrace))) return rc;
+  if ((rc = D2H(D.tr_pool, 8 * (size_t)hd.ntrace, 8 * (size_t)hd.ntrace))) return rc;
+  if ((rc = D2H(D.tr_sel, 8 * (size_t)hd.ntrace, 8 * (size_t)hd.ntrace))) return rc;
+  return GPUGO_OK;
+}
+
+int gpugo_restore(gpugo_engine* E, const void* buf, int64_t bytes, double* boxes_out, double* box_lb_out,
+                  int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+  if (!E || !buf || bytes < (int64_t)sizeof(CkptHeader)) return GPUGO_ERR_INVALID;
+  CkptHeader hd;
+  memcpy(&hd, buf, sizeof(hd));
+  if (memcmp(hd.magic, CKPT_MAGIC, 8) != 0 || hd.n < 1 || hd.rows < 1 || hd.cnt < 0 || hd.nout < 0 ||
+      hd.ntrace < 0 || hd.ncoef < 0)
+    return GPUGO_ERR_INVALID;
+  const int n = hd.n;
+  const size_t total = pad8(sizeof(hd)) + 8 * (2 * (size_t)n + (size_t)hd.ncoef) + 8 * 3 * (size_t)n * hd.rows +
+                       pad8(4 * (size_t)hd.rows) + 16 * (size_t)hd.cnt + 16 * (size_t)hd.nout +
+                       32 * (size_t)hd.ntrace;
+  if ((size_t)bytes < total) return GPUGO_ERR_INVALID;
+  const char* o = (const char*)buf + pad8(sizeof(hd));
+  const double* dom = (const double*)o; o += 16 * (size_t)n;
+  const double* coef = (const double*)o; o += 8 * (size_t)hd.ncoef;
+  gpugo_spec sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.family = hd.family; sp.n = n; sp.wid = hd.wid; sp.group = hd.group; sp.samples = hd.samples;
+  sp.stop_mode = hd.stop_mode; sp.width_tol = hd.width_tol; sp.gap_tol = hd.gap_tol; sp.ub_init = hd.ub_init;
+  sp.domain = dom; sp.coef = coef; sp.ncoef = hd.ncoef; sp.max_iter = hd.max_iter; sp.pool_cap = hd.pool_cap;
+  sp.parent_cap = hd.parent_cap;
+  int rc = validate(&sp);
+  if (rc) return rc;
+  Layout L;
+  layout(&sp, cap, trace ? trace->cap : 0, &L);
+  if (hd.rows > L.parent_cap || hd.cnt > L.pool_cap) return GPUGO_ERR_INVALID;
+  std::vector<Piece> pcs;
+  auto take = [&](int64_t rel, size_t b, size_t advance) {
+    if (b) pcs.push_back(Piece{(size_t)rel, o, b});
+    o += advance;
+  };
+  take(L.o_par, 16 * (size_t)n * hd.rows, 16 * (size_t)n * hd.rows);
+  take(L.o_pw, 8 * (size_t)n * hd.rows, 8 * (size_t)n * hd.rows);
+  take(L.o_pcyc, 4 * (size_t)hd.rows, pad8(4 * (size_t)hd.rows));
+  take(L.o_plb0, 8 * (size_t)hd.cnt, 8 * (size_t)hd.cnt);
+  take(L.o_pk0, 8 * (size_t)hd.cnt, 8 * (size_t)hd.cnt);
+  const int64_t nout = std::min<int64_t>(hd.nout, L.out_cap);
+  take(L.o_outk, 8 * (size_t)nout, 8 * (size_t)hd.nout);
+  take(L.o_outl, 8 * (size_t)nout, 8 * (size_t)hd.nout);
+  const int64_t ntr = std::min<int64_t>(hd.ntrace, L.trace_cap);
+  take(L.o_trub, 8 * (size_t)ntr, 8 * (size_t)hd.ntrace);
+  take(L.o_trs, 8 * (size_t)ntr, 8 * (size_t)hd.ntrace);
+  take(L.o_trp, 8 * (size_t)ntr, 8 * (size_t)hd.ntrace);
+  take(L.o_trsel, 8 * (size_t)ntr, 8 * (size_t)hd.ntrace);
+  State st = hd.st;
+  st.cur = 0;               // the list was packed into buffer 0
+  st.count = hd.cnt;
+  st.count_new = 0;
+  return admit(E, &sp, boxes_out, box_lb_out, cap, xhat_out, trace, &st, pcs, ticket_out);
 }
 
 int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {

@@ -205,6 +205,20 @@ typedef struct gpugo_stats {
 
 int gpugo_engine_stats(gpugo_engine* eng, gpugo_stats* out);
 
+/* Checkpoint / resume of one resident solve (between runs), for long solves that
+   must survive a process or a device: the reference has no counterpart (its
+   list lives in host NumPy arrays for the length of one script run,
+   ackley50.py:1269-1370).  gpugo_checkpoint serialises the instance's problem,
+   state, parent table, list, emitted boxes and trace into buf (pass buf = NULL
+   to get the size in *bytes_out; GPUGO_ERR_BUSY if the instance has not run
+   yet).  gpugo_restore admits a serialised instance into an engine (any engine
+   on any device); it continues exactly where the checkpoint was taken: the
+   restored solve's remaining iterations and result are bit-identical to the
+   uninterrupted solve's. */
+int gpugo_checkpoint(gpugo_engine* eng, int64_t ticket, void* buf, int64_t cap, int64_t* bytes_out);
+int gpugo_restore(gpugo_engine* eng, const void* buf, int64_t bytes, double* boxes_out, double* box_lb_out,
+                  int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out);
+
 /* Free bytes of the engine's arena (admission control). */
 int gpugo_engine_free_bytes(gpugo_engine* eng, int64_t* free_out);
 

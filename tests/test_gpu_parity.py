@@ -260,3 +260,59 @@ def test_bounded_wait_expires_cleanly():
         assert e.value.code == -6
     r = G.solve(P.config1())
     assert r.certified
+
+
+CKPT = [
+    ("cfg2", lambda: P.config2()),
+    ("expsqrt20", lambda: P.instance(P.EXPSQRT, 20, 18, 1e-6)),
+    ("chained30", lambda: P.instance(P.CHAINED, 30, 22, 1e-6)),
+]
+
+
+@pytest.mark.parametrize("name,make", CKPT, ids=[c[0] for c in CKPT])
+def test_checkpoint_resume_is_bit_identical(oracle_lib, name, make):
+    """A solve checkpointed after three iterations and restored into another engine
+    (next to another solve) ends exactly like the uninterrupted solve and the oracle."""
+    p = make()
+    p.max_iter = 3000
+    ro = oracle_lib.solve(p, box_cap=16, trace_cap=100000)
+    with G.Engine(max_slots=4, arena_bytes=2 << 30) as e1:
+        t = e1.submit(p, box_cap=16, trace_cap=100000)
+        e1.run(3)
+        data = e1.checkpoint(t)
+        e1.run(0)
+        (_, a), = e1.poll()
+    with G.Engine(max_slots=4, arena_bytes=2 << 30) as e2:
+        e2.submit(P.config1(), box_cap=4)
+        t2 = e2.restore(p, data, box_cap=16, trace_cap=100000)
+        e2.run(0)
+        done = dict(e2.poll())
+    b = done[t2]
+    for x in (a, b):
+        assert (x.iterations, x.lb, x.ub, x.status, x.pool_size, x.n_boxes) == \
+            (ro.iterations, ro.lb, ro.ub, G.CERTIFIED, ro.pool_size, ro.n_boxes)
+        for k in ("ub", "n_surv", "pool", "sel"):
+            assert _same(x.trace[k], ro.trace[k]), k
+        assert _same(x.box_lbs, ro.box_lbs)
+    assert _same(a.boxes, b.boxes) and a.samples_evaluated == b.samples_evaluated
+    assert (a.xhat is None) == (b.xhat is None)
+    if a.xhat is not None:
+        assert _same(a.xhat, b.xhat)
+
+
+def test_checkpoint_rejects_unadmitted_and_bad_data():
+    p = P.config1()
+    with G.Engine(max_slots=2, arena_bytes=1 << 30) as e:
+        t = e.submit(p, box_cap=4)
+        with pytest.raises(G.GpugoError) as err:
+            e.checkpoint(t)                       # not run yet
+        assert err.value.code == -7
+        e.run(1)
+        data = bytearray(e.checkpoint(t))
+        data[0] ^= 0xFF                           # corrupt the magic
+        with pytest.raises(G.GpugoError) as err:
+            e.restore(p, bytes(data))
+        assert err.value.code == -1
+        e.run(0)
+        (_, r), = e.poll()
+        assert r.certified
