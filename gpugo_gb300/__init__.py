@@ -6,7 +6,9 @@ GPUGO_1.1/1-Ackley/ackley50.py:950-1396) is :func:`solve`.  :func:`eval_children
 is one sampling + ruleOutGPU pass (ackley50.py:602-766) over chosen children,
 and :class:`Engine` runs many solves in one persistent kernel (batching and
 serving).  All compute runs in libgpugo.so (hand-written CUDA for sm_103a);
-Python only marshals arguments.
+Python only marshals arguments.  Objectives outside the four built-in families
+are written with :mod:`gpugo_gb300.codelist` (family ``CODELIST``); the
+reference's other benchmarks are in :mod:`gpugo_gb300.objectives`.
 """
 from __future__ import annotations
 
@@ -18,11 +20,11 @@ import numpy as np
 
 from . import _lib
 from ._lib import CERTIFIED, FINISHED, ITER_LIMIT, GpugoError
-from .problems import (CHAINED, COSQUAD, EXPSQRT, PRODCOS, STOP_GAP, STOP_WIDTH, Problem, config1, config2,
-                       config3, config4, config5, instance)
+from .problems import (CHAINED, CODELIST, COSQUAD, EXPSQRT, PRODCOS, STOP_GAP, STOP_WIDTH, Problem, config1,
+                       config2, config3, config4, config5, instance)
 
 __all__ = ["solve", "eval_children", "Engine", "SolveResult", "Problem", "GpugoError", "instance", "config1",
-           "config2", "config3", "config4", "config5", "COSQUAD", "CHAINED", "EXPSQRT", "PRODCOS",
+           "config2", "config3", "config4", "config5", "COSQUAD", "CHAINED", "EXPSQRT", "PRODCOS", "CODELIST",
            "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info", "combine"]
 
 _dp = ctypes.POINTER(ctypes.c_double)

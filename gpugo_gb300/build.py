@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgpugo.so")
 SOURCES = ["engine.cu"]
-HEADERS = ["ia.cuh", "families.cuh"]
+HEADERS = ["ia.cuh", "families.cuh", "codelist.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

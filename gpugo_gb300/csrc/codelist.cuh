@@ -1,0 +1,165 @@
+// codelist.cuh -- device interpreter of compiled objective code lists (family 5).
+//
+// The reference writes each objective as hand-made code lists of interval
+// operations: value (e.g. GPUGO_1.1/6-Levy/levy50.py:141-226), sample (the same
+// list on the diagonal points, :235-379) and derivative (:382-563).  A compiled
+// code list (format written by gpugo_gb300/codelist.py, checked by the host
+// before admission) holds the same operations as instructions over a small
+// file of interval registers; this file runs them for one child box.
+//
+// Coordinates come from a per-iteration table, like the term tables of the
+// built-in families: entry (i, digit) holds the child interval of coordinate i
+// (T_LO, two doubles) and its S sample points (T_SHI).  A child then reads
+// every coordinate with one shift-and-mask digit lookup and one load.
+//
+// Every instruction is one operation of ia.cuh applied in the order written,
+// so every bound is the one the oracle's interpreter computes, bit for bit.
+#pragma once
+
+namespace gg {
+
+enum {
+  CL_LDX = 1, CL_LDC, CL_LDI, CL_LDK, CL_LDKI, CL_ADD, CL_MINUS, CL_MUL, CL_DIV, CL_TIMES, CL_PLUS,
+  CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP
+};
+enum { CL_HEADER = 12, CL_SEC = 8, CL_INS = 4, CL_MAXREG = 16 };
+enum { CLH_MAGIC, CLH_N, CLH_NREG, CLH_NINS, CLH_NCST, CLH_VS, CLH_VL, CLH_PS, CLH_PL, CLH_NSEC, CLH_SKIP, CLH_RES };
+constexpr unsigned CL_NONE = 0xFFFFFFFFu;
+constexpr unsigned CL_MAGIC = 0x314C4347u;
+
+// word k of a compiled code list: the low 32 bits of coef[k]
+__device__ __forceinline__ unsigned cl_word(const double* c, long long k) {
+  return (unsigned)(unsigned long long)__double_as_longlong(c[k]);
+}
+
+// Table entries of one iteration: items [0, n w) are coordinate intervals,
+// items [n w, n w (S + 1)) sample points (coordinate-major, then digit, then j).
+__device__ __forceinline__ void cl_build_item(const Desc& D, const double* pbox, const double* pw, int cyc,
+                                              long long t) {
+  const int n = D.n, S = D.S, w = D.wid;
+  const int c0 = cyc - 1, gsz = group_size(n, D.group, cyc);
+  const long long NW = (long long)n * w;
+  double* T = D.tab;
+  if (t < NW) {
+    const int i = (int)(t / w), d = (int)(t - (long long)i * w);
+    if (d >= ndig(D, c0, gsz, i)) return;
+    stiv(T + D.t_off[T_LO] + 2 * t, child_iv(D, pbox, pw, c0, gsz, i, d));
+  } else {
+    const long long u = t - NW;
+    const long long e = u / S;
+    const int js = (int)(u - e * S);
+    const int i = (int)(e / w), d = (int)(e - (long long)i * w);
+    if (d >= ndig(D, c0, gsz, i)) return;
+    T[D.t_off[T_SHI] + u] = sample_pt(child_iv(D, pbox, pw, c0, gsz, i, d), S, js);
+  }
+}
+
+// coordinate i of the child: its interval (js < 0) or sample point js
+__device__ __forceinline__ iv cl_x(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int js,
+                                   int i) {
+  const long long e = (long long)i * D.wid + digit(D, C.c0, C.gsz, pc, i);
+  if (js < 0) return ldiv(T + D.t_off[T_LO] + 2 * e);
+  const double p = T[D.t_off[T_SHI] + e * D.S + js];
+  return mk(p, p);
+}
+
+// Runs instructions start .. start+len-1 on the register file R.  j is the
+// gradient coordinate (index base 2); the loop index (base 1) lives here.
+__device__ __noinline__ void cl_exec(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int js,
+                                     int start, int len, int j, iv* R) {
+  const double* cf = D.coef;
+  const long long I = CL_HEADER + (long long)CL_SEC * cl_word(cf, CLH_NSEC);
+  const double* K = cf + I + (long long)CL_INS * cl_word(cf, CLH_NINS);
+  const double2* ins = (const double2*)(cf + I);   // I is even: 16-byte aligned
+  int i = 0, hi = 0, body = 0;
+  for (int p = start; p < start + len; ++p) {
+    const double2 w01 = ins[2 * p];
+    const unsigned w0 = (unsigned)(unsigned long long)__double_as_longlong(w01.x);
+    const int i1 = (int)(unsigned)(unsigned long long)__double_as_longlong(w01.y);
+    const int i2 = (int)cl_word(cf, I + (long long)CL_INS * p + 2);
+    const int op = (int)(w0 & 255u), d = (int)((w0 >> 8) & 255u), a = (int)((w0 >> 16) & 255u),
+              b = (int)(w0 >> 24);
+    switch (op) {
+      case CL_LDX: R[d] = cl_x(D, T, C, pc, js, (a == 0 ? 0 : a == 1 ? i : j) + i1); break;
+      case CL_LDC: R[d] = mk(K[i2], K[i2]); break;
+      case CL_LDI: R[d] = mk(K[i2], K[i2 + 1]); break;
+      case CL_LDK: {
+        const double v = K[i2 + (a == 0 ? 0 : a == 1 ? i : j) + i1];
+        R[d] = mk(v, v);
+        break;
+      }
+      case CL_LDKI: R[d] = ldiv(K + i2 + 2 * ((a == 0 ? 0 : a == 1 ? i : j) + i1)); break;
+      case CL_ADD: R[d] = add(R[a], R[b]); break;
+      case CL_MINUS: R[d] = minus(R[a], R[b]); break;
+      case CL_MUL: R[d] = mul(R[a], R[b]); break;
+      case CL_DIV: R[d] = div(R[a], R[b]); break;
+      case CL_TIMES: R[d] = times(R[a], K[i2]); break;
+      case CL_PLUS: R[d] = plus(R[a], K[i2]); break;
+      case CL_TIMESK: R[d] = times(R[a], K[i2 + (b == 0 ? 0 : b == 1 ? i : j) + i1]); break;
+      case CL_PLUSK: R[d] = plus(R[a], K[i2 + (b == 0 ? 0 : b == 1 ? i : j) + i1]); break;
+      case CL_SQR: R[d] = sqr(R[a]); break;
+      case CL_SQRT: R[d] = sqrt_iv(R[a]); break;
+      case CL_EXP: R[d] = exp_iv(R[a]); break;
+      case CL_SIN: R[d] = sin_iv(R[a]); break;
+      case CL_COS: R[d] = cos_iv(R[a]); break;
+      case CL_MOV: R[d] = R[a]; break;
+      case CL_LOOP: i = i1; hi = i2; body = p + 1; break;
+      case CL_ENDLOOP:
+        if (++i < hi) p = body - 1;
+        break;
+      default: break;
+    }
+  }
+}
+
+// interval of f over the child (js < 0) or at its sample point js
+__device__ __noinline__ iv cl_value(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int js) {
+  iv R[CL_MAXREG];
+  cl_exec(D, T, C, pc, js, (int)cl_word(D.coef, CLH_VS), (int)cl_word(D.coef, CLH_VL), 0, R);
+  return R[cl_word(D.coef, CLH_RES)];
+}
+
+// Generalized KKT test of coordinates j0, j0 + jstep, ... (1 = rule out).
+// Every caller runs the once-per-box prologue itself: an FP64 instruction costs
+// the same for one lane or for 32, so lanes that split the coordinates share it.
+__device__ __noinline__ int cl_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j0,
+                                     int jstep) {
+  const double* cf = D.coef;
+  const int nsec = (int)cl_word(cf, CLH_NSEC);
+  if (nsec == 0) return 0;
+  const unsigned skc = cl_word(cf, CLH_SKIP);
+  if (skc != CL_NONE) {
+    // the box contains the given point in every coordinate (salomon50.py:374-381)
+    const double v = cf[CL_HEADER + (long long)CL_SEC * nsec + (long long)CL_INS * cl_word(cf, CLH_NINS) + skc];
+    bool all = true;
+    for (int k = 0; k < D.n && all; ++k) {
+      const iv x = cl_x(D, T, C, pc, -1, k);
+      if (flt(v, x.lo) || flt(x.hi, v)) all = false;
+    }
+    if (all) return 0;
+  }
+  iv R[CL_MAXREG];
+  cl_exec(D, T, C, pc, -1, (int)cl_word(cf, CLH_PS), (int)cl_word(cf, CLH_PL), 0, R);
+  for (int s = 0; s < nsec; ++s) {
+    const long long q = CL_HEADER + (long long)CL_SEC * s;
+    const int lo = (int)cl_word(cf, q), hi = (int)cl_word(cf, q + 1);
+    const int st = (int)cl_word(cf, q + 2), ln = (int)cl_word(cf, q + 3);
+    const int rg = (int)cl_word(cf, q + 4), chk = (int)cl_word(cf, q + 5);
+    const unsigned rs = cl_word(cf, q + 6);
+    // first coordinate of this caller's stride in [lo, hi)
+    int j = j0;
+    if (j < lo) j += ((lo - j + jstep - 1) / jstep) * jstep;
+    for (; j < hi; j += jstep) {
+      cl_exec(D, T, C, pc, -1, st, ln, j, R);
+      if (rs != CL_NONE) {
+        const iv t = R[rs];
+        if (feq(t.lo, -INF_D) || feq(t.hi, INF_D)) continue;   // corrupted50.py:418-421
+      }
+      const int k = j + chk;
+      if (kkt_prune(R[rg], cl_x(D, T, C, pc, -1, k), D.dom[2 * k], D.dom[2 * k + 1])) return 1;
+    }
+  }
+  return 0;
+}
+
+}  // namespace gg

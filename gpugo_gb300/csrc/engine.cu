@@ -303,7 +303,7 @@ __device__ void build_lists(const KArgs& a) {
   block_exclusive_scan(cE, &tE);
   long long oR = block_exclusive_scan(cR, &tR);
   long long baseA = 0, baseSA = 0, baseSB = 0;
-  for (int f = grouped ? 1 : 0; f <= (grouped ? 4 : 0); ++f) {
+  for (int f = grouped ? 1 : 0; f <= (grouped ? FAM_CODELIST : 0); ++f) {
     long long cA = 0, sA = 0, sB = 0;
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
@@ -855,9 +855,41 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
     P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
   }
   int pruned = 0;
-  if (!skip)
+  if (D.family == FAM_CODELIST) {
+    pruned = cl_deriv(D, T, C, pc, lane, 32);
+  } else if (!skip) {
     for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
+  }
   return !__any_sync(0xffffffffu, pruned);
+}
+
+// thread_candidate for a code-list instance (one interpreter run per sample)
+__device__ __noinline__ int thread_candidate_cl(const KArgs& a, int s, const double* T, unsigned long long code,
+                                                double lb) {
+  const Desc& D = a.desc[s];
+  State& st = a.st[s];
+  ChildCtx C;
+  C.c0 = st.cyc - 1;
+  C.gsz = group_size(D.n, D.group, st.cyc);
+  double ub = atomic_ub_read(&st.ub);
+  if (flt(ub, lb)) return 0;
+  const unsigned long long pc = pack_code(D, C.gsz, code);
+  for (int j = 0; j < D.S; ++j) {
+    double v = cl_value(D, T, C, pc, j).hi;
+    if (feq(v, 0.0)) v = 0.0;
+    if (flt(v, ub)) {
+      long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+      if (slot < D.ubc_cap) {
+        D.ubc_val[slot] = v;
+        D.ubc_id[slot] = (code << 8) | (unsigned long long)j;
+      }
+      atomicMin(&st.ub, ord_key(v));
+      ub = v;
+    }
+  }
+  ub = atomic_ub_read(&st.ub);
+  if (flt(ub, lb)) return 2;
+  return cl_deriv(D, T, C, pc, 0, 1) ? 2 : 3;
 }
 
 // One candidate processed by one thread (long queues): the samples run one after
@@ -866,6 +898,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
 // returns bit 0: the child survives, bit 1: its samples were evaluated
 __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
                                 const double* aux, const double* pfx) {
+  if (a.desc[s].family == FAM_CODELIST) return thread_candidate_cl(a, s, T, code, lb);
   const Desc& D = a.desc[s];
   State& st = a.st[s];
   ChildCtx C;
@@ -1088,7 +1121,8 @@ __device__ void phase_seed(const KArgs& a) {
     const Desc& D = a.desc[s];
     State& st = a.st[s];
     const unsigned long long sk = st.seed_key;
-    if (sk == ~0ULL) continue;
+    // code lists have no seed pass: it only lowers the UB earlier in the iteration
+    if (sk == ~0ULL || D.family == FAM_CODELIST) continue;
     const unsigned long long code = sk & 0xffffffffULL;
     const double* T = (s == si) ? s_tab : D.tab;
     ChildCtx C;
@@ -1844,9 +1878,119 @@ int ilog2_exact(int w) {
   return l;
 }
 
+// A compiled code list (GPUGO_CODELIST): the header, every index an instruction
+// can form over the range of its loop or gradient section (coordinates,
+// constants, registers), and that every register is written before it is read.
+// The device interpreter relies on this and checks nothing itself.
+static int cl_check_code(const double* cf, int64_t I, int nins, int start, int len, int n, int64_t ncst, int nreg,
+                         int jlo, int jhi, bool allow_j, uint32_t* written) {
+  if (start < 0 || len < 0 || (int64_t)start + len > nins) return GPUGO_ERR_INVALID;
+  auto word = [&](int64_t k) { uint64_t u; memcpy(&u, cf + k, 8); return (uint32_t)u; };
+  bool in_loop = false;
+  int64_t lo = 0, hi = 0;
+  for (int p = start; p < start + len; ++p) {
+    const int64_t q = I + (int64_t)CL_INS * p;
+    const uint32_t w0 = word(q);
+    const int32_t i1 = (int32_t)word(q + 1), i2 = (int32_t)word(q + 2);
+    const int op = (int)(w0 & 255u), d = (int)((w0 >> 8) & 255u), a = (int)((w0 >> 16) & 255u), b = (int)(w0 >> 24);
+    int base = -1, per = 0;  // per > 0: index into the constants with this stride
+    int64_t kbase = 0;
+    uint32_t reads = 0;
+    switch (op) {
+      case CL_LDX: base = a; break;
+      case CL_LDC: if (i2 < 0 || i2 >= ncst) return GPUGO_ERR_INVALID; break;
+      case CL_LDI: if (i2 < 0 || (int64_t)i2 + 1 >= ncst) return GPUGO_ERR_INVALID; break;
+      case CL_LDK: base = a; kbase = i2; per = 1; break;
+      case CL_LDKI: base = a; kbase = i2; per = 2; break;
+      case CL_TIMESK: case CL_PLUSK: base = b; kbase = i2; per = 1; reads = 1u << (a & 31); if (a >= nreg) return GPUGO_ERR_INVALID; break;
+      case CL_ADD: case CL_MINUS: case CL_MUL: case CL_DIV:
+        if (a >= nreg || b >= nreg) return GPUGO_ERR_INVALID;
+        reads = (1u << a) | (1u << b);
+        break;
+      case CL_TIMES: case CL_PLUS:
+        if (i2 < 0 || i2 >= ncst) return GPUGO_ERR_INVALID;
+        // fall through
+      case CL_SQR: case CL_SQRT: case CL_EXP: case CL_SIN: case CL_COS: case CL_MOV:
+        if (a >= nreg) return GPUGO_ERR_INVALID;
+        reads = 1u << a;
+        break;
+      case CL_LOOP:
+        if (in_loop || i1 < 0 || i1 >= i2 || i2 > n) return GPUGO_ERR_INVALID;
+        in_loop = true; lo = i1; hi = i2;
+        continue;
+      case CL_ENDLOOP:
+        if (!in_loop) return GPUGO_ERR_INVALID;
+        in_loop = false;
+        continue;
+      default:
+        return GPUGO_ERR_INVALID;
+    }
+    if (d >= nreg || (reads & ~*written)) return GPUGO_ERR_INVALID;
+    if (base >= 0) {
+      int64_t mn, mx;
+      if (base == 0) { mn = mx = i1; }
+      else if (base == 1) { if (!in_loop) return GPUGO_ERR_INVALID; mn = lo + i1; mx = hi - 1 + i1; }
+      else if (base == 2) { if (!allow_j) return GPUGO_ERR_INVALID; mn = (int64_t)jlo + i1; mx = (int64_t)jhi - 1 + i1; }
+      else return GPUGO_ERR_INVALID;
+      if (mn < 0) return GPUGO_ERR_INVALID;
+      if (per == 0) {
+        if (mx >= n) return GPUGO_ERR_INVALID;
+      } else if (kbase < 0 || kbase + per * mx + per - 1 >= ncst) {
+        return GPUGO_ERR_INVALID;
+      }
+    }
+    *written |= 1u << d;
+  }
+  return in_loop ? GPUGO_ERR_INVALID : GPUGO_OK;
+}
+
+int validate_codelist(const gpugo_spec* s) {
+  const double* cf = s->coef;
+  if (s->ncoef < CL_HEADER) return GPUGO_ERR_INVALID;
+  auto word = [&](int64_t k, uint32_t* out) {
+    uint64_t u; memcpy(&u, cf + k, 8);
+    *out = (uint32_t)u;
+    return (u >> 32) == 0;
+  };
+  uint32_t h[CL_HEADER];
+  for (int k = 0; k < CL_HEADER; ++k) if (!word(k, &h[k])) return GPUGO_ERR_INVALID;
+  if (h[CLH_MAGIC] != CL_MAGIC || (int)h[CLH_N] != s->n) return GPUGO_ERR_INVALID;
+  if (h[CLH_NREG] < 1 || h[CLH_NREG] > CL_MAXREG || h[CLH_NINS] > (1u << 20) || h[CLH_NCST] > (1u << 26))
+    return GPUGO_ERR_INVALID;
+  if (h[CLH_NSEC] > (uint32_t)s->n) return GPUGO_ERR_INVALID;
+  const int64_t I = CL_HEADER + (int64_t)CL_SEC * h[CLH_NSEC];
+  const int64_t C = I + (int64_t)CL_INS * h[CLH_NINS];
+  if (s->ncoef < C + (int64_t)h[CLH_NCST]) return GPUGO_ERR_INVALID;
+  for (int64_t k = CL_HEADER; k < C; ++k) { uint32_t t; if (!word(k, &t)) return GPUGO_ERR_INVALID; }
+  const int n = s->n, nreg = (int)h[CLH_NREG], nins = (int)h[CLH_NINS];
+  const int64_t ncst = h[CLH_NCST];
+  uint32_t wv = 0;
+  if (h[CLH_VL] < 1 || h[CLH_RES] >= (uint32_t)nreg) return GPUGO_ERR_INVALID;
+  if (cl_check_code(cf, I, nins, (int)h[CLH_VS], (int)h[CLH_VL], n, ncst, nreg, 0, 0, false, &wv)) return GPUGO_ERR_INVALID;
+  if (!(wv & (1u << h[CLH_RES]))) return GPUGO_ERR_INVALID;
+  uint32_t wp = 0;
+  if (cl_check_code(cf, I, nins, (int)h[CLH_PS], (int)h[CLH_PL], n, ncst, nreg, 0, 0, false, &wp)) return GPUGO_ERR_INVALID;
+  if (h[CLH_SKIP] != CL_NONE && h[CLH_SKIP] >= (uint32_t)ncst) return GPUGO_ERR_INVALID;
+  int prev_hi = 0;
+  for (uint32_t q = 0; q < h[CLH_NSEC]; ++q) {
+    uint32_t w[7];
+    for (int t = 0; t < 7; ++t) word(CL_HEADER + (int64_t)CL_SEC * q + t, &w[t]);
+    const int lo = (int)w[0], hi = (int)w[1];
+    const int32_t chk = (int32_t)w[5];
+    if (lo < prev_hi || lo >= hi || hi > n) return GPUGO_ERR_INVALID;  // ascending, disjoint
+    prev_hi = hi;
+    if (w[4] >= (uint32_t)nreg || (w[6] != CL_NONE && w[6] >= (uint32_t)nreg)) return GPUGO_ERR_INVALID;
+    if ((int64_t)lo + chk < 0 || (int64_t)hi - 1 + chk >= n) return GPUGO_ERR_INVALID;
+    uint32_t ws = wp;
+    if (cl_check_code(cf, I, nins, (int)w[2], (int)w[3], n, ncst, nreg, lo, hi, true, &ws)) return GPUGO_ERR_INVALID;
+    if (!(ws & (1u << w[4])) || (w[6] != CL_NONE && !(ws & (1u << w[6])))) return GPUGO_ERR_INVALID;
+  }
+  return GPUGO_OK;
+}
+
 int validate(const gpugo_spec* s) {
   if (!s || !s->domain || !s->coef) return GPUGO_ERR_INVALID;
-  if (s->family < 1 || s->family > 4) return GPUGO_ERR_INVALID;
+  if (s->family < 1 || s->family > 5) return GPUGO_ERR_INVALID;
   if (s->n < 1 || s->n > 4096) return GPUGO_ERR_INVALID;
   if (s->family == GPUGO_CHAINED && s->n < 2) return GPUGO_ERR_INVALID;
   if (s->wid < 2 || s->group < 1 || s->samples < 1 || s->samples > 255) return GPUGO_ERR_INVALID;
@@ -1865,6 +2009,7 @@ int validate(const gpugo_spec* s) {
     case GPUGO_CHAINED: need = 2LL * (s->n - 1); break;
     case GPUGO_EXPSQRT: need = 2LL + s->n; break;
     case GPUGO_PRODCOS: need = 1; break;
+    case GPUGO_CODELIST: return validate_codelist(s);
   }
   if (s->ncoef < need) return GPUGO_ERR_INVALID;
   if (s->family == GPUGO_EXPSQRT && !(s->coef[0] > 0 && s->coef[1] > 0)) return GPUGO_ERR_INVALID;
@@ -1896,6 +2041,7 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
     case GPUGO_COSQUAD: L->cst = 6 * n + 2; break;
     case GPUGO_CHAINED: L->cst = 8 * n; break;
     case GPUGO_EXPSQRT: L->cst = 8 + 3 * n; break;
+    case GPUGO_CODELIST: L->cst = 0; break;
     default: L->cst = 4 + 2 * n; break;
   }
   int64_t o = 0;
@@ -1908,6 +2054,10 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
     case GPUGO_CHAINED:
       put(T_LO, (n - 1) * w * w); put(T_SHI, (n - 1) * w * w * S); put(T_PRB, (n * w * w * w + 7) / 8);
       L->a_items = (n - 1) * w * w * (S + 1) + n * w * w * w;
+      break;
+    case GPUGO_CODELIST:
+      put(T_LO, 2 * n * w); put(T_SHI, n * w * S);
+      L->a_items = n * w * (S + 1);
       break;
     case GPUGO_EXPSQRT:
       put(T_SQ, 2 * n * w); put(T_CS, 2 * n * w); put(T_XI, 2 * n * w); put(T_SN, 2 * n * w);

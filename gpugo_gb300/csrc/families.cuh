@@ -17,7 +17,7 @@
 
 namespace gg {
 
-enum { FAM_COSQUAD = 1, FAM_CHAINED = 2, FAM_EXPSQRT = 3, FAM_PRODCOS = 4 };
+enum { FAM_COSQUAD = 1, FAM_CHAINED = 2, FAM_EXPSQRT = 3, FAM_PRODCOS = 4, FAM_CODELIST = 5 };
 enum { STOP_WIDTH = 0, STOP_GAP = 1 };
 
 constexpr double TWO_PI = 0x1.921fb54442d18p+2;   // 2*math.pi in the reference
@@ -26,7 +26,7 @@ constexpr double E_HI = 0x1.5bf0a8b14576ap+1;     // next double, above e
 
 // Table offsets (doubles) within an instance's table region.
 enum {
-  T_LO = 0, T_SHI, T_PRB,                               // cosquad / chained
+  T_LO = 0, T_SHI, T_PRB,                               // cosquad / chained / codelist
   T_SQ = 0, T_CS, T_XI, T_SN, T_ZB, T_SQS, T_CSS,       // expsqrt
   T_CR = 0, T_SQ4, T_SNA, T_XD2, T_XI4, T_CRS, T_SQS4, T_RCP4,  // prodcos
   T_PFX = 8,                                            // shared sample prefixes (all families)
@@ -153,6 +153,16 @@ __device__ __forceinline__ int kkt_prune(iv d, iv x, double dlo, double dhi) {
 
 __device__ __forceinline__ iv ldiv(const double* p) { return mk(p[0], p[1]); }
 __device__ __forceinline__ void stiv(double* p, iv v) { p[0] = v.lo; p[1] = v.hi; }
+
+struct ChildCtx {
+  int c0, gsz;
+};
+
+}  // namespace gg
+
+#include "codelist.cuh"
+
+namespace gg {
 
 // ---------------------------------------------------------------------------
 // derived constants (one thread per instance)
@@ -384,6 +394,7 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
 }
 
 __device__ __forceinline__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
+  if (D.family == FAM_CODELIST) { cl_build_item(D, pbox, pw, cyc, t); return; }
   if (D.a_items < (1LL << 31)) build_item_t<unsigned>(D, pbox, pw, cyc, (unsigned)t);
   else build_item_t<unsigned long long>(D, pbox, pw, cyc, (unsigned long long)t);
 }
@@ -391,9 +402,6 @@ __device__ __forceinline__ void build_item(const Desc& D, const double* pbox, co
 // ---------------------------------------------------------------------------
 // per-child reductions
 // ---------------------------------------------------------------------------
-struct ChildCtx {
-  int c0, gsz;
-};
 
 // One side of the interval operations with a positive interval constant [kl, kh]
 // (IA.py:117-152 with the sign of the constant known): the lower bound of a*k
@@ -530,6 +538,8 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
       if (aux) { aux[0] = pr.lo; aux[1] = pr.hi; }
       return __dadd_rd(__dadd_rd(mulk_lo(s_lo, k[0], k[1]), 1.0), pr.lo);
     }
+    case FAM_CODELIST:
+      return cl_value(D, T, C, pc, -1).lo;
   }
   return 0.0;
 }
@@ -553,6 +563,7 @@ __device__ __forceinline__ SAcc sacc_init(const Desc& D) {
 // same for all children of the parent
 __device__ __forceinline__ int samp_terms(const Desc& D) { return D.family == FAM_CHAINED ? D.n - 1 : D.n; }
 __device__ __forceinline__ int samp_shared(const Desc& D, ChildCtx C) {
+  if (D.family == FAM_CODELIST) return 0;   // no shared prefix: the list is not a plain reduction
   return D.family == FAM_CHAINED ? (C.c0 > 0 ? C.c0 - 1 : 0) : C.c0;
 }
 
@@ -702,6 +713,7 @@ __device__ __forceinline__ SAcc samp_prefix(const Desc& D, const double* T, Chil
 // upper bound of f at sample point j of the child (one pass of the sample code list)
 __device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j,
                                         double cut = INF_D, const double* pfx = nullptr) {
+  if (D.family == FAM_CODELIST) return cl_value(D, T, C, pc, j).hi;
   double v;
   samp_multi<1>(D, T, C, pc, j, &v, cut, pfx);
   return v;
@@ -903,6 +915,7 @@ __device__ __forceinline__ int deriv_coord(const Desc& D, const double* T, Child
 
 // 1 when the generalized KKT test rules the child out
 __device__ __noinline__ int child_deriv(const Desc& D, const double* T, ChildCtx C, unsigned long long pc) {
+  if (D.family == FAM_CODELIST) return cl_deriv(D, T, C, pc, 0, 1);
   DerivPre P;
   if (deriv_pre(D, T, C, pc, &P)) return 0;
   for (int j = 0; j < D.n; ++j)

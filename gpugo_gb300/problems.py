@@ -16,6 +16,7 @@ Families (coefficient layout in ``coef``):
 * ``EXPSQRT``  f = -A exp(-B sqrt(mean x^2)) - exp(mean cos(K_i x_i)) + A + e,
   K_i = fl(fl(2 pi) w_i)                                       coef = A, B, w[n]
 * ``PRODCOS``  f = 1 + sum_i x_i^2 / d - prod_i cos(x_i / sqrt(i))      coef = d
+* ``CODELIST`` any objective compiled by :mod:`gpugo_gb300.codelist`   coef = the code list
 
 The reference's Rastrigin, Rosenbrock, Ackley and Griewank scripts are the
 special cases a=1,b=10,c=1 / p=100,q=1 / A=20,B=0.02,w=1 / d=4000.
@@ -27,8 +28,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-COSQUAD, CHAINED, EXPSQRT, PRODCOS = 1, 2, 3, 4
-FAMILY_NAMES = {COSQUAD: "cosquad", CHAINED: "chained", EXPSQRT: "expsqrt", PRODCOS: "prodcos"}
+COSQUAD, CHAINED, EXPSQRT, PRODCOS, CODELIST = 1, 2, 3, 4, 5
+FAMILY_NAMES = {COSQUAD: "cosquad", CHAINED: "chained", EXPSQRT: "expsqrt", PRODCOS: "prodcos", CODELIST: "codelist"}
 STOP_WIDTH, STOP_GAP = 0, 1
 MASTER_SEED = 0x6770756F
 
@@ -82,6 +83,9 @@ class Problem:
             d = c[0]
             i = np.arange(1, n + 1, dtype=np.float64)
             return float(1 + np.sum(x * x) / d - np.prod(np.cos(x / np.sqrt(i))))
+        if self.family == CODELIST:
+            from .codelist import point_value
+            return point_value(self.coef, x)
         raise ValueError(self.family)
 
     def minimiser(self) -> np.ndarray:

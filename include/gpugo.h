@@ -47,13 +47,25 @@ extern "C" {
 #define GPUGO_CHAINED 2   /* sum_{i<n} p_i (x_{i+1} - x_i^2)^2 + q_i (1 - x_i)^2; coef p[n-1] q[n-1]       (rosenbrock50.py:168-198) */
 #define GPUGO_EXPSQRT 3   /* -A exp(-B sqrt(mean x^2)) - exp(mean cos(K_i x_i)) + A + e; coef A B w[n]     (ackley50.py:166-212) */
 #define GPUGO_PRODCOS 4   /* 1 + sum x_i^2 / d - prod cos(x_i / sqrt(i)); coef d                          (griewank50.py:161-198) */
+/* Any objective as a compiled code list (value, sample and derivative code lists
+ * as in levy50.py:103-563): coef is the array gpugo_gb300/codelist.py writes.
+ * Word k of its header and code is the low 32 bits of coef[k]:
+ *   [0] 0x314C4347 [1] n [2] registers (<= 16) [3] instructions [4] constants
+ *   [5] value start [6] value length [7] gradient prologue start [8] length
+ *   [9] sections [10] skip constant (0xFFFFFFFF none) [11] value result register
+ *   [12 + 8s] section: lo, hi, start, length, gradient register, check offset, skip register, 0
+ *   [I + 4t]  instruction: op | dst << 8 | a << 16 | b << 24, imm1, imm2, 0   (I = 12 + 8 sections)
+ *   [I + 4 instructions ...] constants (doubles)
+ * The library checks every index an instruction can form against n, the
+ * constants and the registers before it accepts the problem (GPUGO_ERR_INVALID). */
+#define GPUGO_CODELIST 5
 
 #define GPUGO_STOP_WIDTH 0   /* reference rule: emit a box when width(x_1) < width_tol at the last cycle (ackley50.py:1306-1343) */
 #define GPUGO_STOP_GAP   1   /* certify when UB - LB <= gap_tol */
 
 /* One problem: the constants of a reference script made explicit. */
 typedef struct gpugo_spec {
-    int32_t family;        /* GPUGO_COSQUAD .. GPUGO_PRODCOS */
+    int32_t family;        /* GPUGO_COSQUAD .. GPUGO_CODELIST */
     int32_t n;             /* variables (reference: 50..10000, hard-coded per script) */
     int32_t wid;           /* parts per split coordinate (reference wid = 4, ackley50.py:527) */
     int32_t group;         /* coordinates split per iteration (reference cycleSize = 10, :530) */

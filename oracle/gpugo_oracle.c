@@ -15,6 +15,11 @@
  *                             GPUGO_1.1/11-Rosenbrock/rosenbrock50.py:116-451 (family F2)
  *                             GPUGO_1.1/1-Ackley/ackley50.py:116-479        (family F3)
  *                             GPUGO_1.1/5-Griewank/griewank50.py:111-433    (family F4)
+ *                             any objective as a code list (family 5): the value,
+ *                             sample and derivative code lists of e.g.
+ *                             GPUGO_1.1/6-Levy/levy50.py:103-563 run by an
+ *                             interpreter of the compiled form that
+ *                             gpugo_gb300/codelist.py writes
  *   - kernels                 ackley50.py:602-684 (sampling), :686-766 (ruleOutGPU),
  *                             :768-810 (constructFlagArr)
  *   - host B&B loop           ackley50.py:950-1396 (rastrigin50.py:844-1289)
@@ -515,7 +520,7 @@ static iv ia_exp(iv a)
 /* ------------------------------------------------------------------------- */
 /* problem description                                                       */
 /* ------------------------------------------------------------------------- */
-enum { FAM_COSQUAD = 1, FAM_CHAINED = 2, FAM_EXPSQRT = 3, FAM_PRODCOS = 4 };
+enum { FAM_COSQUAD = 1, FAM_CHAINED = 2, FAM_EXPSQRT = 3, FAM_PRODCOS = 4, FAM_CODELIST = 5 };
 enum { STOP_WIDTH = 0, STOP_GAP = 1 };
 
 /* Same field layout as gpugo_spec in include/gpugo.h. */
@@ -544,9 +549,14 @@ typedef struct {
     double A, B; iv inv_n, ape, abn; iv *kn;
     /* F4 */
     iv *rsq, inv_d, inv_d2;
+    /* code list: words of the header, sections and instructions; constants */
+    const double* clc;
+    uint32_t* clw;
     double* store;
     iv* istore;
 } consts;
+
+static int cl_parse(const oc_spec* sp, consts* c);
 
 static int consts_init(const oc_spec* sp, consts* c)
 {
@@ -598,6 +608,8 @@ static int consts_init(const oc_spec* sp, consts* c)
             c->kn[i] = mk(div_rd(c->k[i], (double)n), div_ru(c->k[i], (double)n));
         }
         break; }
+    case FAM_CODELIST:
+        return cl_parse(sp, c);
     case FAM_PRODCOS: {                     /* coef = d */
         if (sp->ncoef < 1 || !(cf[0] > 0)) return -2;
         c->rsq = is;
@@ -614,7 +626,7 @@ static int consts_init(const oc_spec* sp, consts* c)
     return 0;
 }
 
-static void consts_free(consts* c) { free(c->store); free(c->istore); }
+static void consts_free(consts* c) { free(c->store); free(c->istore); free(c->clw); }
 
 /* ------------------------------------------------------------------------- */
 /* box decoder (ackley50.py:482-594, :820-948)                               */
@@ -648,6 +660,221 @@ static inline double sample_pt(iv x, int S, int j)
 {
     double inc = (x.hi - x.lo) / (double)(S + 1);
     return x.lo + inc * (double)(j + 1);
+}
+
+/* ------------------------------------------------------------------------- */
+/* family 5: compiled code lists (format in gpugo_gb300/codelist.py)           */
+/* ------------------------------------------------------------------------- */
+enum {
+    CL_LDX = 1, CL_LDC, CL_LDI, CL_LDK, CL_LDKI, CL_ADD, CL_MINUS, CL_MUL, CL_DIV, CL_TIMES, CL_PLUS,
+    CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP
+};
+enum { CL_MAGIC = 0x314C4347u, CL_HEADER = 12, CL_SEC = 8, CL_INS = 4, CL_MAXREG = 16 };
+#define CL_NONE 0xFFFFFFFFu
+
+/* header words */
+enum { H_MAGIC, H_N, H_NREG, H_NINS, H_NCST, H_VS, H_VL, H_PS, H_PL, H_NSEC, H_SKIP, H_RES };
+
+static inline uint32_t cl_u32(double d) { uint64_t u = d2u(d); return (uint32_t)u; }
+static inline int cl_hi_zero(double d) { return (d2u(d) >> 32) == 0; }
+
+/* index of base + off; base 0 absolute, 1 loop index i, 2 gradient coordinate j */
+static inline long cl_idx(int base, int32_t off, long i, long j)
+{
+    return (base == 0 ? 0 : base == 1 ? i : j) + (long)off;
+}
+
+/* Checks every instruction once, over the ranges its indexes can take, so that
+ * the interpreter never reads outside the coordinates, constants or registers. */
+static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int n, int ncst, int nreg,
+                          int jlo, int jhi, int allow_j, uint32_t* written)
+{
+    long lo = 0, hi = 0;
+    int in_loop = 0;
+    if (start < 0 || len < 0 || (long)start + len > nins) return -2;
+    for (int p = start; p < start + len; ++p) {
+        const uint32_t* w = ins + (size_t)CL_INS * p;
+        int op = (int)(w[0] & 255u), d = (int)((w[0] >> 8) & 255u), a = (int)((w[0] >> 16) & 255u),
+            b = (int)(w[0] >> 24);
+        int32_t i1 = (int32_t)w[1], i2 = (int32_t)w[2];
+        int base = -1, size = n;
+        long kbase = 0;
+        uint32_t reads = 0;
+        switch (op) {
+        case CL_LDX: base = a; break;
+        case CL_LDC: if (i2 < 0 || i2 >= ncst) return -2; break;
+        case CL_LDI: if (i2 < 0 || i2 + 1 >= ncst) return -2; break;
+        case CL_LDK: case CL_LDKI: base = a; kbase = i2; size = -1; break;
+        case CL_TIMESK: case CL_PLUSK:
+            base = b; kbase = i2; size = -1;
+            if (a >= nreg) return -2;
+            reads = 1u << a;
+            break;
+        case CL_ADD: case CL_MINUS: case CL_MUL: case CL_DIV:
+            if (a >= nreg || b >= nreg) return -2;
+            reads = (1u << a) | (1u << b);
+            break;
+        case CL_TIMES: case CL_PLUS: if (i2 < 0 || i2 >= ncst) return -2; /* fall through */
+        case CL_SQR: case CL_SQRT: case CL_EXP: case CL_SIN: case CL_COS: case CL_MOV:
+            if (a >= nreg) return -2;
+            reads = 1u << a;
+            break;
+        case CL_LOOP:
+            if (in_loop || i1 < 0 || i1 >= i2 || i2 > n) return -2;
+            in_loop = 1; lo = i1; hi = i2;
+            continue;
+        case CL_ENDLOOP:
+            if (!in_loop) return -2;
+            in_loop = 0;
+            continue;
+        default:
+            return -2;
+        }
+        if (d >= nreg || (reads & ~*written)) return -2;   /* a register is written before it is read */
+        if (base >= 0) {
+            long mn, mx;
+            if (base == 0) { mn = mx = i1; }
+            else if (base == 1) { if (!in_loop) return -2; mn = lo + i1; mx = hi - 1 + i1; }
+            else if (base == 2) { if (!allow_j) return -2; mn = jlo + i1; mx = jhi - 1 + i1; }
+            else return -2;
+            if (mn < 0) return -2;
+            if (size > 0) {
+                if (mx >= size) return -2;
+            } else {
+                long per = (op == CL_LDKI) ? 2 : 1;
+                if (kbase < 0 || kbase + per * mx + per - 1 >= ncst) return -2;
+            }
+        }
+        *written |= 1u << d;
+    }
+    return in_loop ? -2 : 0;
+}
+
+static int cl_parse(const oc_spec* sp, consts* c)
+{
+    const double* cf = sp->coef;
+    int64_t nc = sp->ncoef;
+    if (!cf || nc < CL_HEADER) return -2;
+    for (int k = 0; k < CL_HEADER; ++k) if (!cl_hi_zero(cf[k])) return -2;
+    uint32_t h[CL_HEADER];
+    for (int k = 0; k < CL_HEADER; ++k) h[k] = cl_u32(cf[k]);
+    if (h[H_MAGIC] != CL_MAGIC || (int)h[H_N] != sp->n) return -2;
+    if (h[H_NREG] < 1 || h[H_NREG] > CL_MAXREG || h[H_NINS] > (1u << 20) || h[H_NCST] > (1u << 26)) return -2;
+    if (h[H_NSEC] > (uint32_t)sp->n) return -2;
+    int64_t nw = CL_HEADER + (int64_t)CL_SEC * h[H_NSEC] + (int64_t)CL_INS * h[H_NINS];
+    if (nc < nw + (int64_t)h[H_NCST]) return -2;
+    uint32_t* w = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)nw);
+    if (!w) return -1;
+    for (int64_t k = 0; k < nw; ++k) {
+        if (!cl_hi_zero(cf[k])) { free(w); return -2; }
+        w[k] = cl_u32(cf[k]);
+    }
+    c->clw = w;
+    c->clc = cf + nw;
+    const int n = sp->n, nreg = (int)h[H_NREG], nins = (int)h[H_NINS], ncst = (int)h[H_NCST];
+    const uint32_t* ins = w + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    uint32_t wv = 0, wp = 0;
+    if (h[H_VL] < 1 || h[H_RES] >= (uint32_t)nreg) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_VS], (int)h[H_VL], n, ncst, nreg, 0, 0, 0, &wv)) return -2;
+    if (!(wv & (1u << h[H_RES]))) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_PS], (int)h[H_PL], n, ncst, nreg, 0, 0, 0, &wp)) return -2;
+    if (h[H_SKIP] != CL_NONE && h[H_SKIP] >= (uint32_t)ncst) return -2;
+    int prev_hi = 0;
+    for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
+        const uint32_t* q = w + CL_HEADER + (size_t)CL_SEC * s;
+        int lo = (int)q[0], hi = (int)q[1], st = (int)q[2], ln = (int)q[3], r = (int)q[4];
+        int32_t chk = (int32_t)q[5];
+        uint32_t rs = q[6];
+        if (lo < prev_hi || lo >= hi || hi > n) return -2;   /* sections ascend and do not overlap */
+        prev_hi = hi;
+        if (r >= nreg || (rs != CL_NONE && rs >= (uint32_t)nreg)) return -2;
+        if ((long)lo + chk < 0 || (long)hi - 1 + chk >= n) return -2;
+        uint32_t ws = wp;
+        if (cl_check_range(ins, nins, st, ln, n, ncst, nreg, lo, hi, 1, &ws)) return -2;
+        if (!(ws & (1u << r)) || (rs != CL_NONE && !(ws & (1u << rs)))) return -2;
+    }
+    return 0;
+}
+
+/* Runs instructions start .. start+len-1; j is the gradient coordinate. */
+static void cl_exec(const consts* c, int start, int len, const iv* X, iv* R, long j)
+{
+    const uint32_t* h = c->clw;
+    const uint32_t* ins = h + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    const double* K = c->clc;
+    long i = 0, hi = 0;
+    int body = 0;
+    for (int p = start; p < start + len; ++p) {
+        const uint32_t* w = ins + (size_t)CL_INS * p;
+        const int op = (int)(w[0] & 255u), d = (int)((w[0] >> 8) & 255u), a = (int)((w[0] >> 16) & 255u),
+                  b = (int)(w[0] >> 24);
+        const int32_t i1 = (int32_t)w[1], i2 = (int32_t)w[2];
+        switch (op) {
+        case CL_LDX: R[d] = X[cl_idx(a, i1, i, j)]; break;
+        case CL_LDC: R[d] = mk(K[i2], K[i2]); break;
+        case CL_LDI: R[d] = mk(K[i2], K[i2 + 1]); break;
+        case CL_LDK: { double v = K[i2 + cl_idx(a, i1, i, j)]; R[d] = mk(v, v); break; }
+        case CL_LDKI: { long k = i2 + 2 * cl_idx(a, i1, i, j); R[d] = mk(K[k], K[k + 1]); break; }
+        case CL_ADD: R[d] = ia_add(R[a], R[b]); break;
+        case CL_MINUS: R[d] = ia_minus(R[a], R[b]); break;
+        case CL_MUL: R[d] = ia_mul(R[a], R[b]); break;
+        case CL_DIV: R[d] = ia_div(R[a], R[b]); break;
+        case CL_TIMES: R[d] = ia_times(R[a], K[i2]); break;
+        case CL_PLUS: R[d] = ia_plus(R[a], K[i2]); break;
+        case CL_TIMESK: R[d] = ia_times(R[a], K[i2 + cl_idx(b, i1, i, j)]); break;
+        case CL_PLUSK: R[d] = ia_plus(R[a], K[i2 + cl_idx(b, i1, i, j)]); break;
+        case CL_SQR: R[d] = ia_sqr(R[a]); break;
+        case CL_SQRT: R[d] = ia_sqrt(R[a]); break;
+        case CL_EXP: R[d] = ia_exp(R[a]); break;
+        case CL_SIN: R[d] = ia_sin(R[a]); break;
+        case CL_COS: R[d] = ia_cos(R[a]); break;
+        case CL_MOV: R[d] = R[a]; break;
+        case CL_LOOP: i = i1; hi = i2; body = p + 1; break;
+        case CL_ENDLOOP: if (++i < hi) p = body - 1; break;
+        }
+    }
+}
+
+static iv cl_value(const consts* c, const iv* X)
+{
+    const uint32_t* h = c->clw;
+    iv R[CL_MAXREG];
+    for (int k = 0; k < CL_MAXREG; ++k) R[k] = mk(0.0, 0.0);
+    cl_exec(c, (int)h[H_VS], (int)h[H_VL], X, R, 0);
+    return R[h[H_RES]];
+}
+
+/* generalized KKT test over every coordinate; 1 = rule out */
+static int cl_deriv(const oc_spec* sp, const consts* c, const iv* X)
+{
+    const uint32_t* h = c->clw;
+    const double* dom = sp->domain;
+    const int n = sp->n;
+    if (h[H_NSEC] == 0) return 0;
+    if (h[H_SKIP] != CL_NONE) {
+        const double v = c->clc[h[H_SKIP]];
+        int all = 1;
+        for (int k = 0; k < n; ++k) if (X[k].lo > v || X[k].hi < v) { all = 0; break; }
+        if (all) return 0;
+    }
+    iv R[CL_MAXREG];
+    for (int k = 0; k < CL_MAXREG; ++k) R[k] = mk(0.0, 0.0);
+    cl_exec(c, (int)h[H_PS], (int)h[H_PL], X, R, 0);
+    for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
+        const uint32_t* q = h + CL_HEADER + (size_t)CL_SEC * s;
+        for (long j = q[0]; j < (long)q[1]; ++j) {
+            cl_exec(c, (int)q[2], (int)q[3], X, R, j);
+            if (q[6] != CL_NONE) {
+                const iv t = R[q[6]];
+                if (t.lo == -INFINITY || t.hi == INFINITY) continue;
+            }
+            const long k = j + (int32_t)q[5];
+            const iv d = R[q[4]];
+            if (d.lo > 0 && X[k].lo != dom[2 * k]) return 1;
+            if (d.hi < 0 && X[k].hi != dom[2 * k + 1]) return 1;
+        }
+    }
+    return 0;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -694,6 +921,8 @@ static iv f_value(const oc_spec* sp, const consts* c, const iv* X)
         s = ia_plus(ia_mul(s, c->inv_d), 1.0);
         return ia_add(s, pr);
     }
+    case FAM_CODELIST:
+        return cl_value(c, X);
     }
     return mk(NAN, NAN);
 }
@@ -711,6 +940,8 @@ static int f_deriv(const oc_spec* sp, const consts* c, const iv* X)
     int n = sp->n;
     const double* dom = sp->domain;
     switch (sp->family) {
+    case FAM_CODELIST:
+        return cl_deriv(sp, c, X);
     case FAM_COSQUAD:                   /* rastrigin50.py:340-372 */
         for (int j = 0; j < n; ++j) {
             iv d = ia_times(X[j], c->a2[j]);
@@ -1082,7 +1313,13 @@ OC_API int oc_solve(const oc_spec* sp, int mode, oc_result* res, double* boxes_o
         int64_t it_done = iter;
         iter++;
 
-        /* Step 4: selection (ackley50.py:1269-1370) */
+        /* Step 4: selection (ackley50.py:1269-1370).  The parent table grows
+         * first: the child box below points into it. */
+        if (iter >= pcap) {
+            pcap *= 2;
+            parents = (double*)realloc(parents, sizeof(double) * 2 * n * pcap);
+            pcyc = (int32_t*)realloc(pcyc, sizeof(int32_t) * pcap);
+        }
         int found = 0, terminate = 0;
         while (!found) {
             if (L == 0) { terminate = 1; break; }
@@ -1109,11 +1346,6 @@ OC_API int oc_solve(const oc_spec* sp, int mode, oc_result* res, double* boxes_o
                 continue;
             }
             found = 1;
-            if (iter >= pcap) {
-                pcap *= 2;
-                parents = (double*)realloc(parents, sizeof(double) * 2 * n * pcap);
-                pcyc = (int32_t*)realloc(pcyc, sizeof(int32_t) * pcap);
-            }
             for (int i = 0; i < n; ++i) { iv x = child_iv(&ch, i); parents[2 * n * iter + 2 * i] = x.lo; parents[2 * n * iter + 2 * i + 1] = x.hi; }
             pcyc[iter] = (ccyc == max_cyc) ? 1 : ccyc + g;
             cur = iter;

@@ -29,6 +29,12 @@ Only the imports and function definitions of each script are executed; its
 top-level statements (the whole 50-variable B&B run) are skipped.  The result-box
 merging vectors come from the same execution of ``rosenbrock50.py``'s host
 functions ``combine`` / ``connectivity``.
+
+``--codelist`` writes ``codelist_vectors.npz`` instead: the value, sample and
+derivative code lists of the seven scripts without a built-in family (Levy,
+Salomon, Styblinski, Belegundu, Breiman, Fu, Zabinsky), which pin the code-list
+interpreter.  Their scalar multiplications use the sign-aware ``times`` (two of
+them pass -0.1 and -1).
 """
 from __future__ import annotations
 
@@ -36,6 +42,7 @@ import ast
 import math
 import os
 import sys
+import time
 import types
 from fractions import Fraction
 
@@ -292,5 +299,74 @@ def combine_cases(ref_root: str) -> dict:
             "combine_root_offsets": np.array(roff, dtype=np.int64), "combine_roots": flat(roots)}
 
 
+CODELIST_SCRIPTS = {
+    # name: (script, ia module name, function prefix, domain, centre of the small parent box)
+    # (its width is 1 % of the domain, or SMALL_WIDTH[name])
+    "levy": ("GPUGO_1.1/6-Levy/levy50.py", "IALevy", "Levy", (-10.0, 10.0), -3.0),
+    "salomon": ("GPUGO_1.1/8-Salomon/salomon50.py", "IASalomon", "salomon", (-100.0, 110.0), 30.0),
+    "corrupted": ("GPUGO_1.1/9-Styblinski/corrupted50.py", "IACorrupted", "corrupted", (-10.0, 11.0), 0.0),
+    "deflected": ("GPUGO_1.1/2-Belegundu/deflected50.py", "IADeflected", "deflected", (-10.0, 11.0), 5.0),
+    "cosine": ("GPUGO_1.1/3-Breiman/cosine50.py", "IACosine", "cosine", (-1.0, 2.0), 0.0),
+    "trigonometric": ("GPUGO_1.1/4-Fu/trigonometric50.py", "IATrigonometric", "trigonometric", (-10.0, 10.0), 0.9),
+    "sinusoidal": ("GPUGO_1.1/10-Zabinsky/sinusoidal50.py", "IASinusoidal", "sinusoidal", (0.0, math.pi),
+                   2.0 * math.pi / 3),
+}
+CODELIST_PER_PARENT = 40
+SMALL_WIDTH = {"salomon": 1e-8}   # the Salomon gradient excludes 0 only on very small boxes
+
+
+def codelist_main(ref_root: str, only: list[str] | None = None):
+    oracle.build()
+    sys.modules["numba"] = make_numba_stub()
+    rng = np.random.default_rng(0x636C6973)
+    dst = os.path.join(HERE, "codelist_vectors.npz")
+    out = dict(np.load(dst)) if (only and os.path.exists(dst)) else {}
+    for name, (rel, ia_name, pre, dom, centre) in CODELIST_SCRIPTS.items():
+        sub = np.random.default_rng(rng.integers(1 << 62))   # per script, so one can be regenerated alone
+        if only and name not in only:
+            continue
+        ia_mod = load_updated_ia(ref_root, True)
+        ns = load_script(ref_root, rel, ia_name, ia_mod)
+        value, sample, deriv = ns[pre + "Value_IA"], ns[pre + "Sample_IA"], ns[pre + "Derivative_IA"]
+        complete = ns["completeRegion"]
+        lo, hi = dom
+        root = np.tile([lo, hi], N).astype(np.float64)
+        c1 = complete(root, int(sub.integers(0, WID ** GROUP)), 1)
+        c1 = np.asarray(c1, dtype=np.float64)
+        small = np.empty(2 * N)
+        for i in range(N):
+            w = float(sub.uniform(0.5, 2.0)) * SMALL_WIDTH.get(name, 1e-2) * (hi - lo)
+            off = float(sub.uniform(-0.4, 0.4)) * w
+            small[2 * i] = max(lo, centre - w + off)
+            small[2 * i + 1] = min(hi, centre + w + off)
+        parents = [(root, 1), (c1, 11), (small, 41)]
+        pidx, cycs, codes, lbs, samps, dflags = [], [], [], [], [], []
+        t0 = time.time()
+        for k, (pbox, cyc) in enumerate(parents):
+            pos = [int(v) for v in sub.integers(0, WID ** GROUP, CODELIST_PER_PARENT - 2)] + [0, WID ** GROUP - 1]
+            for q in pos:
+                lb, _ = value(pbox, q, 1e300, 0, cyc)
+                lbs.append(float(lb))
+                samps.append(float(sample(pbox, q, SAMPLES, cyc)))
+                dflags.append(int(deriv(pbox, q, 0, cyc)))
+                pidx.append(k); cycs.append(cyc); codes.append(q)
+        out[name + "_domain"] = np.tile(np.array(dom, dtype=np.float64), N)
+        out[name + "_parents"] = np.stack([pb for pb, _ in parents])
+        out[name + "_parent_idx"] = np.array(pidx, dtype=np.int64)
+        out[name + "_cyc"] = np.array(cycs, dtype=np.int64)
+        out[name + "_code"] = np.array(codes, dtype=np.int64)
+        out[name + "_lb"] = np.array(lbs)
+        out[name + "_samp"] = np.array(samps)
+        out[name + "_dflag"] = np.array(dflags, dtype=np.int64)
+        print(name, "cases", len(codes), f"{time.time() - t0:.0f} s", flush=True)
+    np.savez_compressed(dst, **out)
+    print("wrote", dst)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--codelist" in sys.argv:
+        codelist_main(root, args[1:] or None)
+    else:
+        main(root)

@@ -1,0 +1,261 @@
+"""Objective code lists (family CODELIST): front end, the oracle's interpreter
+pinned to the reference's own code lists, and the product's input checks.
+
+The golden vectors (tests/golden/codelist_vectors.npz, made by
+tests/golden/make_golden.py --codelist) are the outputs of the reference's
+value, sample and derivative functions of its seven benchmarks without a
+built-in family, run as plain Python.  Two entries are not reproduced, each a
+bug of the reference's list (see gpugo_gb300/objectives.py): Belegundu's
+derivative and Breiman's sample.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+from gpugo_gb300 import codelist as CL
+from gpugo_gb300 import objectives as O
+from gpugo_gb300 import problems as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CL_GOLD = os.path.join(HERE, "golden", "codelist_vectors.npz")
+NOT_REPRODUCED = {("deflected", "dflag"), ("cosine", "samp")}
+
+
+def _bits(a):
+    return np.asarray(a, dtype=np.float64).view(np.uint64)
+
+
+def _gold_problem(z, name):
+    f, g, dom = O.REFERENCE[name](50)
+    coef = CL.compile_objective(f, 50, g).coef
+    return P.Problem(P.CODELIST, 50, z[name + "_domain"], coef, wid=4, group=10, samples=10)
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE))
+def test_oracle_matches_reference_code_lists(oracle_lib, name):
+    z = np.load(CL_GOLD)
+    p = _gold_problem(z, name)
+    par, pidx, cyc, code = z[name + "_parents"], z[name + "_parent_idx"], z[name + "_cyc"], z[name + "_code"]
+    n_pruned = 0
+    for k in range(len(par)):
+        sel = pidx == k
+        cy = int(cyc[sel][0])
+        assert np.all(cyc[sel] == cy)
+        lb, samp, _, dflag = oracle_lib.eval_children(p, par[k], cy, code[sel].astype(np.uint64), 1e300)
+        assert np.array_equal(_bits(lb), _bits(z[name + "_lb"][sel])), name
+        if (name, "samp") not in NOT_REPRODUCED:
+            assert np.array_equal(_bits(samp), _bits(z[name + "_samp"][sel])), name
+        else:
+            # the restated sample list is the value list: every sample bounds f from above
+            assert np.all(samp >= lb)
+        if (name, "dflag") not in NOT_REPRODUCED:
+            assert np.array_equal(dflag, z[name + "_dflag"][sel]), name
+        n_pruned += int(np.sum(z[name + "_dflag"][sel]))
+    assert n_pruned > 0, "the vectors exercise the derivative test"
+
+
+@pytest.mark.parametrize("family", [P.COSQUAD, P.CHAINED, P.EXPSQRT, P.PRODCOS])
+def test_builtin_families_restated_as_code_lists(oracle_lib, family):
+    """The four built-in families written as code lists give the same bits."""
+    rng = np.random.default_rng(family)
+    for n in (2, 3, 5, 9, 17):
+        p = P.instance(family, n, int(rng.integers(1 << 30)))
+        q = O.as_codelist(p)
+        lo, hi = p.domain[0::2], p.domain[1::2]
+        for t in range(4):
+            pbox = p.domain.copy()
+            if t:
+                w = (hi - lo) * 10.0 ** rng.uniform(-6, -1, n)
+                c = np.minimum(rng.uniform(lo, hi), hi - w) if t < 3 else -0.6 * w
+                pbox[0::2], pbox[1::2] = c, c + w
+            for cyc in sorted({1, 1 + p.group * ((n - 1) // p.group)}):
+                m = p.wid ** min(p.group, n - cyc + 1)
+                codes = rng.integers(0, m, 64).astype(np.uint64)
+                a = oracle_lib.eval_children(p, pbox, cyc, codes, 1e300)
+                b = oracle_lib.eval_children(q, pbox, cyc, codes, 1e300)
+                for x, y in zip(a, b):
+                    assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8)), (family, n, t)
+
+
+@pytest.mark.parametrize("family,n", [(P.COSQUAD, 5), (P.CHAINED, 4), (P.EXPSQRT, 5), (P.PRODCOS, 6)])
+def test_builtin_as_code_list_solve_trace(oracle_lib, family, n):
+    p = P.instance(family, n, 100 + family, 1e-6)
+    q = O.as_codelist(p)
+    a = oracle_lib.solve(p, box_cap=64, trace_cap=20000)
+    b = oracle_lib.solve(q, box_cap=64, trace_cap=20000)
+    assert (a.lb, a.ub, a.iterations, a.n_boxes) == (b.lb, b.ub, b.iterations, b.n_boxes)
+    for k in a.trace:
+        assert np.array_equal(a.trace[k], b.trace[k]), k
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE))
+def test_reference_objectives_certify_on_the_oracle(oracle_lib, name):
+    """Every restated benchmark certifies at n = 4 with its known minimum inside."""
+    p = O.problem(name, 4, tol=1e-6)
+    p.max_iter = 5000
+    r = oracle_lib.solve(p, box_cap=64)
+    assert r.ub - r.lb <= 1e-6 and r.lb <= r.ub
+    fmin = {"levy": 0.0, "salomon": 0.0, "corrupted": -16.0, "deflected": -1.0, "cosine": -0.4,
+            "trigonometric": 1.0, "sinusoidal": -3.5}[name]
+    assert r.lb <= fmin + 1e-12 and fmin - 1e-6 <= r.ub
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE) + ["cosquad", "chained", "expsqrt", "prodcos"])
+def test_gradient_lists_are_gradients_of_the_value_lists(oracle_lib, name):
+    """Where the central-difference gradient of the value list has a clear sign,
+    the derivative list rules out a tiny box around the point (a list that is
+    not the gradient of the value list, like the reference's Belegundu one,
+    fails this)."""
+    n = 5
+    if name in O.REFERENCE:
+        f, g, dom = O.REFERENCE[name](n)
+        coef = CL.compile_objective(f, n, g).coef
+        domain = np.tile(dom, n)
+    else:
+        fam = {"cosquad": P.COSQUAD, "chained": P.CHAINED, "expsqrt": P.EXPSQRT, "prodcos": P.PRODCOS}[name]
+        base = P.instance(fam, n, 7)
+        coef, domain = O.as_codelist(base).coef, base.domain
+    p = P.Problem(P.CODELIST, n, domain, coef, wid=2, group=1, samples=2)
+    rng = np.random.default_rng(11)
+    lo, hi = domain[0::2], domain[1::2]
+    tested = 0
+    for _ in range(40):
+        x = rng.uniform(lo + 0.1 * (hi - lo), hi - 0.1 * (hi - lo))
+        h = 1e-6 * (hi - lo)
+        grad = np.array([(CL.point_value(coef, x + h * e) - CL.point_value(coef, x - h * e)) / (2 * h[k])
+                         for k, e in enumerate(np.eye(n))])
+        scale = max(1.0, abs(CL.point_value(coef, x)))
+        if np.max(np.abs(grad)) < 1e-3 * scale:
+            continue
+        w = 1e-10 * (hi - lo)
+        pbox = np.empty(2 * n)
+        pbox[0::2], pbox[1::2] = x - w, x + w
+        _, _, _, dflag = oracle_lib.eval_children(p, pbox, 1, np.array([0], dtype=np.uint64), 1e300)
+        assert dflag[0] == 1, (name, x, grad)
+        tested += 1
+    assert tested >= 10
+
+
+def test_point_value_matches_plain_formulas():
+    rng = np.random.default_rng(3)
+    n = 6
+    for _ in range(5):
+        x = rng.uniform(-2, 2, n)
+        f, _, _ = O.levy(n)
+        c = CL.compile_objective(f, n).coef
+        # the reference's code list: (pi/n)[10 sin^2(pi/4 x1 + 3pi/4) + sum (x_i/4 - 1/4)^2 (1 + 10 sin^2(...)) + ...]
+        ref = (math.pi / n) * (10 * math.sin(math.pi / 4 * x[0] + 3 * math.pi / 4) ** 2
+                               + sum((x[i - 1] / 4 - 0.25) ** 2 * (10 * math.sin(math.pi / 4 * x[i] + 3 * math.pi / 4) ** 2 + 1)
+                                     for i in range(1, n))
+                               + (x[-1] / 4 - 0.25) ** 2)
+        assert CL.point_value(c, x) == pytest.approx(ref, rel=1e-12)
+        r = math.sqrt(np.sum(x * x))
+        f, _, _ = O.salomon(n)
+        assert CL.point_value(CL.compile_objective(f, n).coef, x) == pytest.approx(
+            1 - math.cos(2 * math.pi * r) + 0.1 * r, rel=1e-12)
+        for fam in (P.COSQUAD, P.CHAINED, P.EXPSQRT, P.PRODCOS):
+            p = P.instance(fam, n, 5)
+            assert O.as_codelist(p).evaluate(x) == pytest.approx(p.evaluate(x), rel=1e-12, abs=1e-12)
+
+
+def test_compile_rejects_bad_expressions():
+    X, Sum = CL.X, CL.Sum
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(X[5], 5)                              # coordinate out of range
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(Sum(lambda i: X[i + 1]), 5)           # i+1 leaves the coordinates
+    with pytest.raises(CL.CodeListError):
+        X[0] ** 3                                                  # only powers 2 and 0.5
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(X[0], 3, CL.Gradient([CL.Section(lambda j: X[j], 0, 2),
+                                                   CL.Section(lambda j: X[j], 1, 3)]))   # overlap
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(X[0], 3, CL.Gradient([CL.Section(lambda j: X[j - 1], 0, 3)]))  # j-1 < 0
+    # t0 + (t1 + (... + t16)): the left operand is evaluated first, so all 17
+    # terms are live before the innermost add -- more than 16 registers
+    terms = [CL.sin(X[k] * float(k + 1)) for k in range(17)]
+    left = terms[0]
+    for t in terms[1:]:
+        left = left + t
+    CL.compile_objective(left, 17)            # left to right: two live values
+    nested = terms[-1]
+    for t in reversed(terms[:-1]):
+        nested = t + nested
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(nested, 17)
+
+
+def _mutations(coef):
+    """Arrays that break one rule each; every one must be rejected."""
+    p = CL.parse(coef)
+    w = coef.view(np.uint64)
+    I = CL.HEADER + CL.SEC_WORDS * len(p["sections"])
+    out = {}
+
+    def put(name, k, v):
+        c = coef.copy()
+        c.view(np.uint64)[k] = v
+        out[name] = c
+
+    put("magic", 0, 0x12345678)
+    put("n", 1, int(w[1]) + 1)
+    put("registers", 2, 17)
+    put("result register", 11, int(w[2]))
+    put("high bits", 3, int(w[3]) | (1 << 40))
+    put("truncated", 4, int(w[4]) + 100)
+    # instruction 0 reads X at an absolute index past the end
+    ins = p["instructions"]
+    k = next(t for t, s in enumerate(ins) if s[0] == CL.LDX and s[2] == CL.BASE_ABS) if any(
+        s[0] == CL.LDX and s[2] == CL.BASE_ABS for s in ins) else None
+    if k is not None:
+        put("ldx index", I + CL.INS_WORDS * k + 1, p["n"])
+    k = next(t for t, s in enumerate(ins) if s[0] == CL.LDC)
+    put("constant index", I + CL.INS_WORDS * k + 2, len(p["consts"]))
+    k = next(t for t, s in enumerate(ins) if s[0] == CL.ADD)
+    op, d, a, b, _, _ = ins[k]
+    put("register index", I + CL.INS_WORDS * k, op | (d << 8) | (a << 16) | (15 << 24))  # never written
+    put("opcode", I + CL.INS_WORDS * k, 99 | (d << 8))
+    k = next(t for t, s in enumerate(ins) if s[0] == CL.LOOP)
+    put("loop range", I + CL.INS_WORDS * k + 2, p["n"] + 1)
+    put("nested loop", I + CL.INS_WORDS * (k + 1), CL.LOOP)
+    if p["sections"]:
+        put("section range", CL.HEADER + 1, p["n"] + 1)
+        put("check offset", CL.HEADER + 5, (-1) & 0xFFFFFFFF)
+    return out
+
+
+def test_oracle_and_library_reject_malformed_code_lists(oracle_lib):
+    from gpugo_gb300 import _lib
+    f, g, dom = O.levy(6)
+    good = CL.compile_objective(f, 6, g).coef
+    p = P.Problem(P.CODELIST, 6, np.tile(dom, 6), good, wid=2, group=2)
+    L = None
+    try:
+        L = _lib.load()
+    except ImportError:
+        pass
+
+    def lib_accepts(q):
+        from gpugo_gb300 import _spec
+        s, keep = _spec(q)
+        out = ctypes.c_int64(0)
+        return L.gpugo_instance_bytes(ctypes.byref(s), ctypes.byref(out)) == 0
+
+    oracle_lib.eval_children(p, p.domain, 1, np.array([0], dtype=np.uint64), 1e300)
+    if L is not None:
+        assert lib_accepts(p)
+    for name, bad in _mutations(good).items():
+        q = P.Problem(P.CODELIST, 6, p.domain, bad, wid=2, group=2)
+        with pytest.raises(ValueError):
+            oracle_lib.eval_children(q, q.domain, 1, np.array([0], dtype=np.uint64), 1e300)
+        if L is not None:
+            assert not lib_accepts(q), name
+
+
+def test_disassembly_names_every_instruction():
+    f, g, _ = O.sinusoidal(4)
+    text = CL.compile_objective(f, 4, g).disassemble()
+    assert "for i in 0..3:" in text and "section j in 0..3" in text and "div(" in text
