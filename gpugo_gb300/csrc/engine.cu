@@ -793,6 +793,7 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 // warp: its sample points spread over the lanes, then its KKT coordinates.
 // Returns true when the child survives.  Every lane returns the same value.
 // pfx (may be null): the instance's shared sample prefixes.
+template <bool CL>
 __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
                                const double* aux, const double* pfx) {
   const int lane = threadIdx.x & 31;
@@ -818,7 +819,7 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
     have_pre = true;
   } else {
     for (int j = lane; j < D.S; j += 32) {
-      double v = samp_one(D, T, C, pc, j, ub, pfx);
+      double v = samp_one<CL>(D, T, C, pc, j, ub, pfx);
       if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
     }
   }
@@ -855,11 +856,15 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
     P.u.lo = shfl_d(P.u.lo, 0); P.u.hi = shfl_d(P.u.hi, 0);
   }
   int pruned = 0;
-  if (D.family == FAM_CODELIST) {
-    pruned = cl_deriv(D, T, C, pc, lane, 32);
-  } else if (!skip) {
-    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
+  bool done = false;
+  if constexpr (CL) {
+    if (D.family == FAM_CODELIST) {
+      pruned = cl_deriv(D, T, C, pc, lane, 32);
+      done = true;
+    }
   }
+  if (!done && !skip)
+    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
   return !__any_sync(0xffffffffu, pruned);
 }
 
@@ -896,9 +901,12 @@ __device__ __noinline__ int thread_candidate_cl(const KArgs& a, int s, const dou
 // the other and every sample value below the running UB lowers it (the minimum
 // over all of them is the same value the per-child minimum would give).
 // returns bit 0: the child survives, bit 1: its samples were evaluated
+template <bool CL>
 __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned long long code, double lb,
                                 const double* aux, const double* pfx) {
-  if (a.desc[s].family == FAM_CODELIST) return thread_candidate_cl(a, s, T, code, lb);
+  if constexpr (CL) {
+    if (a.desc[s].family == FAM_CODELIST) return thread_candidate_cl(a, s, T, code, lb);
+  }
   const Desc& D = a.desc[s];
   State& st = a.st[s];
   ChildCtx C;
@@ -987,6 +995,7 @@ __device__ __forceinline__ void append_survivor(const KArgs& a, int s, unsigned 
 
 // Pass 1: every child's lower bound (uniform cost, static interleave over warps);
 // children whose LB is not above the UB go to the candidate queue.
+template <bool CL>
 __device__ void phase_bound(const KArgs& a) {
   bstamp(a, 2);
   extern __shared__ double s_tab[];
@@ -1016,7 +1025,7 @@ __device__ void phase_bound(const KArgs& a) {
       C.c0 = st.cyc - 1;
       C.gsz = group_size(D.n, D.group, st.cyc);
       const unsigned long long pc = pack_code(D, C.gsz, code);
-      lb = child_lb(D, T, C, pc, aux, ord_val(st.ub_start));
+      lb = child_lb<CL>(D, T, C, pc, aux, ord_val(st.ub_start));
       cand = !flt(ord_val(st.ub_start), lb);
     }
     unsigned int cm = __ballot_sync(0xffffffffu, cand);
@@ -1070,7 +1079,7 @@ __device__ void phase_bound(const KArgs& a) {
         double ca[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) ca[q] = shfl_d(aux[q], b);
-        bool kk = warp_candidate(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
+        bool kk = warp_candidate<CL>(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
         if (lane == b) keep = kk;
       }
       if (keep) append_survivor(a, s, code, lb);
@@ -1181,6 +1190,7 @@ __device__ __forceinline__ void instance_ready(const KArgs& a, int s) {
   __syncwarp();
 }
 
+template <bool CL>
 __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ double s_tab[];
   __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
@@ -1260,7 +1270,7 @@ __device__ void phase_candidates(const KArgs& a) {
 #pragma unroll
           for (int t = 0; t < 2; ++t) aux[t] = __longlong_as_double((long long)en[2 + t]);
           const double* T = (s == si) ? s_tab : a.desc[s].tab;
-          int rr = thread_candidate(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
+          int rr = thread_candidate<CL>(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
           keep = rr & 1;
           sampled = rr & 2;
           if (keep) append_survivor(a, s, code, lb);
@@ -1314,7 +1324,7 @@ __device__ void phase_candidates(const KArgs& a) {
         ca[0] = shfl_d(aux[0], b);
         ca[1] = shfl_d(aux[1], b);
         const double* T = (cs == si) ? s_tab : a.desc[cs].tab;
-        const bool keep = warp_candidate(a, cs, T, cc, cl, ca, pfx_on ? T + a.desc[cs].t_off[T_PFX] : nullptr);
+        const bool keep = warp_candidate<CL>(a, cs, T, cc, cl, ca, pfx_on ? T + a.desc[cs].t_off[T_PFX] : nullptr);
         if (keep && lane == 0) append_survivor(a, cs, cc, cl);
       }
       __syncwarp();
@@ -1477,6 +1487,8 @@ __device__ __forceinline__ void stamp(const KArgs& a, long long it, int k) {
   }
 }
 
+// CL: the build that runs code-list instances (used while one is resident)
+template <bool CL>
 __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   TailLists tl{&a};
   TailAfterChildren tc{&a};
@@ -1491,13 +1503,13 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
     phase_tables(a);
     if (!grid_barrier(a, NoTail{})) return;
     stamp(a, it, 1);
-    phase_bound(a);
+    phase_bound<CL>(a);
     if (!grid_barrier(a, tp)) return;
     if (a.ctl->seed_on) {
       phase_seed(a);
       if (!grid_barrier(a, NoTail{})) return;
     }
-    phase_candidates(a);
+    phase_candidates<CL>(a);
     if (!grid_barrier(a, tc)) return;
     stamp(a, it, 2);
     if (a.ctl->nBig > 0) {
@@ -2424,8 +2436,13 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     E->nsm = p.multiProcessorCount;
     if (!p.cooperativeLaunch) { rc = GPUGO_ERR_CUDA; break; }
     int occ = 0;
-    if ((rc = cuda_err(cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TAB_BYTES)))) break;
-    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel, E->threads, SMEM_TAB_BYTES)))) break;
+    // both builds of the persistent kernel must fit the same cooperative grid
+    int occ_cl = 0;
+    if ((rc = cuda_err(cudaFuncSetAttribute(solve_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TAB_BYTES)))) break;
+    if ((rc = cuda_err(cudaFuncSetAttribute(solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_TAB_BYTES)))) break;
+    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, solve_kernel<false>, E->threads, SMEM_TAB_BYTES)))) break;
+    if ((rc = cuda_err(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cl, solve_kernel<true>, E->threads, SMEM_TAB_BYTES)))) break;
+    occ = std::min(occ, occ_cl);
     if (occ < 1) { rc = GPUGO_ERR_CUDA; break; }
     if (cfg->blocks_per_sm > 0) occ = std::min(occ, cfg->blocks_per_sm);
     // an engine for a handful of solves is latency-bound: one block per SM halves
@@ -2766,8 +2783,11 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.bstamp_iters = E->bstamp_iters;
   a.cur_it = 0;
   void* args[] = {&a};
+  bool any_cl = false;   // the build with the code-list interpreter only while one is resident
+  for (int s = 0; s < E->max_slots && !any_cl; ++s) any_cl = E->slots[s].used && E->slots[s].spec.family == GPUGO_CODELIST;
+  const void* kern = any_cl ? (const void*)solve_kernel<true> : (const void*)solve_kernel<false>;
   CK(cudaEventRecord(E->ev0, st));
-  CK(cudaLaunchCooperativeKernel((void*)solve_kernel, dim3(E->blocks), dim3(E->threads), args, SMEM_TAB_BYTES, st));
+  CK(cudaLaunchCooperativeKernel(kern, dim3(E->blocks), dim3(E->threads), args, SMEM_TAB_BYTES, st));
   CK(cudaEventRecord(E->ev1, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;

@@ -493,6 +493,9 @@ __device__ __forceinline__ long long eidx(const Desc& D, ChildCtx C, unsigned lo
 // only compares it with cut).
 // Two independent reductions over the coordinates share one loop; each keeps
 // the reference's left-to-right order.
+// CL = false leaves the code-list case out (the persistent kernel is built
+// twice, and the copy without code lists runs whenever none is resident).
+template <bool CL = true>
 __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx C, unsigned long long pc,
                                         double* aux = nullptr, double cut = INF_D) {
   const int n = D.n, w = D.wid;
@@ -539,7 +542,8 @@ __device__ __noinline__ double child_lb(const Desc& D, const double* T, ChildCtx
       return __dadd_rd(__dadd_rd(mulk_lo(s_lo, k[0], k[1]), 1.0), pr.lo);
     }
     case FAM_CODELIST:
-      return cl_value(D, T, C, pc, -1).lo;
+      if constexpr (CL) return cl_value(D, T, C, pc, -1).lo;
+      break;
   }
   return 0.0;
 }
@@ -711,9 +715,12 @@ __device__ __forceinline__ SAcc samp_prefix(const Desc& D, const double* T, Chil
 }
 
 // upper bound of f at sample point j of the child (one pass of the sample code list)
+template <bool CL = true>
 __device__ __noinline__ double samp_one(const Desc& D, const double* T, ChildCtx C, unsigned long long pc, int j,
                                         double cut = INF_D, const double* pfx = nullptr) {
-  if (D.family == FAM_CODELIST) return cl_value(D, T, C, pc, j).hi;
+  if constexpr (CL) {
+    if (D.family == FAM_CODELIST) return cl_value(D, T, C, pc, j).hi;
+  }
   double v;
   samp_multi<1>(D, T, C, pc, j, &v, cut, pfx);
   return v;
