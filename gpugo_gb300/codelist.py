@@ -29,13 +29,26 @@ values and every copy keeps it bit for bit:
     [0] 0x314C4347  [1] n  [2] registers  [3] instructions  [4] constants
     [5] value start [6] value length  [7] gradient prologue start [8] length
     [9] sections    [10] skip constant (0xFFFFFFFF: none)  [11] value result register
-    [12 + 8s ...]   section s: lo, hi, start, length, gradient register, check
+    [12] term tables  [13..15] 0
+    [16 + 8s ...]   section s: lo, hi, start, length, gradient register, check
                     offset, skip register (0xFFFFFFFF: none; the test is skipped
                     when that register has an infinite end), 0
+    [U + 12t ...]   term table t: lo, hi, kind (0 sum, 1 product), offsets (0..2),
+                    offset 0, offset 1, 0, body start, body length, body result
+                    register, 0, 0
     [I + 4t ...]    instruction t: op | dst << 8 | a << 16 | b << 24, imm1, imm2, 0
     [C ...]         constants (plain doubles)
 
-with I = 12 + 8 sections and C = I + 4 instructions.
+with U = 16 + 8 sections, I = U + 12 tables and C = I + 4 instructions.
+
+Term tables.  A Sum or Prod whose body reads the coordinates only as X[i + o]
+(at most two offsets o) and otherwise only coefficients and constants is a
+*table reduction* (instruction TRED): the body is a separate piece of code with
+its own registers, and the device evaluates it once per iteration for every
+coordinate i, every digit of the coordinates i + o and every sample pass into a
+table; a child then adds (multiplies) its entries.  The result is the one the
+loop gives: the same operations on the same inputs, accumulated in the same
+order.  Other bodies run as a loop (LOOP .. ENDLOOP) in the child's code.
 """
 from __future__ import annotations
 
@@ -48,18 +61,21 @@ import numpy as np
 
 MAGIC = 0x314C4347
 MAX_REGS = 16
-HEADER = 12
+HEADER = 16
 SEC_WORDS = 8
+TAB_WORDS = 12
 INS_WORDS = 4
+MAX_TABLES = 8
+MAX_TABLE_OFFSETS = 2
 NO_SKIP = 0xFFFFFFFF
 
 # opcodes (the device interpreter and the oracle use the same numbers)
 LDX, LDC, LDI, LDK, LDKI, ADD, MINUS, MUL, DIV, TIMES, PLUS, TIMESK, PLUSK, SQR, SQRT, EXP, SIN, COS, MOV, \
-    LOOP, ENDLOOP = range(1, 22)
+    LOOP, ENDLOOP, TRED = range(1, 23)
 OP_NAMES = {v: k for k, v in dict(
     LDX=LDX, LDC=LDC, LDI=LDI, LDK=LDK, LDKI=LDKI, ADD=ADD, MINUS=MINUS, MUL=MUL, DIV=DIV, TIMES=TIMES, PLUS=PLUS,
     TIMESK=TIMESK, PLUSK=PLUSK, SQR=SQR, SQRT=SQRT, EXP=EXP, SIN=SIN, COS=COS, MOV=MOV, LOOP=LOOP,
-    ENDLOOP=ENDLOOP).items()}
+    ENDLOOP=ENDLOOP, TRED=TRED).items()}
 # index bases of LDX / LDK / LDKI / TIMESK / PLUSK
 BASE_ABS, BASE_I, BASE_J = 0, 1, 2
 NO_REG = 0xFFFFFFFF
@@ -348,6 +364,23 @@ class _Ctx:
     arrays: dict = field(default_factory=dict)
     ins: list = field(default_factory=list)
     nval: int = 0
+    tables: list = field(default_factory=list)
+    table_ix: dict = field(default_factory=dict)
+    use_tables: bool = True
+
+    def table(self, kind: int, lo: int, hi: int, offs: list, body: "Expr") -> int:
+        """Index of the term table of this reduction (compiled on first use)."""
+        key = (kind, lo, hi, body.key)
+        if key in self.table_ix:
+            return self.table_ix[key]
+        sub = _Ctx(self.n)
+        sub.consts, sub.const_ix, sub.arrays = self.consts, self.const_ix, self.arrays
+        em = _Emitter(sub)
+        r = em.emit(body, (lo, hi))
+        nreg, reg = _allocate(sub.ins, {r: len(sub.ins) - 1})
+        self.tables.append(dict(kind=kind, lo=lo, hi=hi, offs=offs, ins=sub.ins, reg=reg[r], nreg=nreg))
+        self.table_ix[key] = len(self.tables) - 1
+        return self.table_ix[key]
 
     def const(self, bits: int) -> int:
         if bits not in self.const_ix:
@@ -373,6 +406,23 @@ class _Ctx:
     def new_val(self) -> int:
         self.nval += 1
         return self.nval - 1
+
+
+def _table_offsets(e, acc: set) -> bool:
+    """True when the body reads coordinates only as X[i + o] (collected in acc)
+    and holds no reduction and nothing of the gradient coordinate."""
+    if not isinstance(e, Expr):
+        return True
+    if e.op == "x":
+        if e.args[0] != BASE_I:
+            return False
+        acc.add(e.args[1])
+        return True
+    if e.op in ("ldk", "ldki"):
+        return e.args[0] != BASE_J
+    if e.op in ("sum", "prod"):
+        return False
+    return all(_table_offsets(a, acc) for a in e.args if isinstance(a, Expr))
 
 
 def _depends(e, base: int, memo: dict) -> bool:
@@ -470,6 +520,13 @@ class _Emitter:
             if lo == hi:
                 self.done[key] = acc0
                 return acc0
+            offs: set = set()
+            if ctx.use_tables and _table_offsets(body, offs) and len(offs) <= MAX_TABLE_OFFSETS and (
+                    len(ctx.tables) < MAX_TABLES or (0 if op == "sum" else 1, lo, hi, body.key) in ctx.table_ix):
+                t = ctx.table(0 if op == "sum" else 1, lo, hi, sorted(offs), body)
+                ctx.ins.append(_Ins(TRED, v, acc0, 0, t, 0, (acc0,), v))
+                self.done[key] = v
+                return v
             # loop-invariant parts of the body first
             self._hoist(body, (lo, hi))
             ctx.ins.append(_Ins(MOV, v, acc0, 0, 0, 0, (acc0,), v))
@@ -573,7 +630,7 @@ def _allocate(ins: list[_Ins], keep_until: dict[int, int]) -> int:
         t.dst = reg[t.writes]
         if t.op in (ADD, MINUS, MUL, DIV):
             t.a, t.b = reg[t.a], reg[t.b]
-        elif t.op in (TIMES, PLUS, TIMESK, PLUSK, SQR, SQRT, EXP, SIN, COS, MOV):
+        elif t.op in (TIMES, PLUS, TIMESK, PLUSK, SQR, SQRT, EXP, SIN, COS, MOV, TRED):
             t.a = reg[t.a]
     return nreg, reg
 
@@ -589,14 +646,15 @@ class CompiledCodeList:
         return disassemble(self.coef)
 
 
-def compile_objective(f: Expr, n: int, gradient: Gradient | None = None) -> CompiledCodeList:
+def compile_objective(f: Expr, n: int, gradient: Gradient | None = None, tables: bool = True) -> CompiledCodeList:
     """Compile the value expression (and optionally the gradient code list) for
-    dimension n into a ``GPUGO_CODELIST`` coefficient array."""
+    dimension n into a ``GPUGO_CODELIST`` coefficient array.  ``tables=False``
+    runs every reduction as a loop (same results, for checks)."""
     if not isinstance(f, Expr):
         raise CodeListError("the objective must be an expression")
     if n < 1:
         raise CodeListError("n must be positive")
-    ctx = _Ctx(n)
+    ctx = _Ctx(n, use_tables=tables)
     em = _Emitter(ctx)
     res = em.emit(f, None)
     val_len = len(ctx.ins)
@@ -660,7 +718,9 @@ def compile_objective(f: Expr, n: int, gradient: Gradient | None = None) -> Comp
             rs = gem.emit(sk, None) if sk is not None else None
             gem.done = saved
             sections.append([lo, hi, start, len(ctx.ins) - start, r, s.check, rs])
-        end = len(ctx.ins) - 1
+        # the sections run once per coordinate: prologue values stay live past
+        # the last section instruction
+        end = len(ctx.ins)
         for v in pro_vals:
             keep[v] = max(keep.get(v, -1), end)
         for sec in sections:
@@ -677,15 +737,25 @@ def compile_objective(f: Expr, n: int, gradient: Gradient | None = None) -> Comp
         for sec in sections:
             sec[4] = reg_g[sec[4]]
             sec[6] = NO_REG if sec[6] is None else reg_g[sec[6]]
-    nreg = max(nreg_v, nreg_g, 1)
-    coef = _pack(n, nreg, ctx.ins, ctx.consts, reg_v[res], val_len, pro_start, pro_len, sections, skip)
-    return CompiledCodeList(coef, n, nreg, len(ctx.ins))
+    # term-table bodies follow the value and gradient code
+    tabs = []
+    all_ins = list(ctx.ins)
+    for t in ctx.tables:
+        tabs.append([t["lo"], t["hi"], t["kind"], len(t["offs"])] + (t["offs"] + [0, 0])[:2] +
+                    [0, len(all_ins), len(t["ins"]), t["reg"]])
+        all_ins += t["ins"]
+    nreg = max([nreg_v, nreg_g, 1] + [t["nreg"] for t in ctx.tables])
+    coef = _pack(n, nreg, all_ins, ctx.consts, reg_v[res], val_len, pro_start, pro_len, sections, skip, tabs)
+    return CompiledCodeList(coef, n, nreg, len(all_ins))
 
 
-def _pack(n, nreg, ins, consts, res_reg, val_len, pro_start, pro_len, sections, skip) -> np.ndarray:
-    words = [MAGIC, n, nreg, len(ins), len(consts), 0, val_len, pro_start, pro_len, len(sections), skip, res_reg]
+def _pack(n, nreg, ins, consts, res_reg, val_len, pro_start, pro_len, sections, skip, tabs) -> np.ndarray:
+    words = [MAGIC, n, nreg, len(ins), len(consts), 0, val_len, pro_start, pro_len, len(sections), skip, res_reg,
+             len(tabs), 0, 0, 0]
     for lo, hi, start, ln, r, chk, rs in sections:
         words += [lo, hi, start, ln, r, chk & 0xFFFFFFFF, rs, 0]
+    for lo, hi, kind, noff, o0, o1, _, start, ln, r in tabs:
+        words += [lo, hi, kind, noff, o0 & 0xFFFFFFFF, o1 & 0xFFFFFFFF, 0, start, ln, r, 0, 0]
     for t in ins:
         words += [t.op | (t.dst << 8) | (t.a << 16) | (t.b << 24), t.imm1 & 0xFFFFFFFF, t.imm2 & 0xFFFFFFFF, 0]
     w = np.array(words, dtype=np.uint64)
@@ -698,28 +768,33 @@ def _words(coef: np.ndarray) -> np.ndarray:
 
 
 def parse(coef: np.ndarray) -> dict:
-    """Header, sections, instructions and constants of a compiled array."""
+    """Header, sections, term tables, instructions and constants of a compiled array."""
     w = _words(coef)
     if w.size < HEADER or int(w[0]) != MAGIC:
         raise CodeListError("not a code list")
-    n, nreg, nins, ncst, vs, vl, ps, pl, nsec, skip, res = (int(x) for x in w[1:12])
-    i0 = HEADER + SEC_WORDS * nsec
+    n, nreg, nins, ncst, vs, vl, ps, pl, nsec, skip, res, ntab = (int(x) for x in w[1:13])
+    s32 = lambda u: u - (1 << 32) if u >= 1 << 31 else u
+    u0 = HEADER + SEC_WORDS * nsec
+    i0 = u0 + TAB_WORDS * ntab
     c0 = i0 + INS_WORDS * nins
     if w.size < c0 + ncst:
         raise CodeListError("code list truncated")
     secs = []
-    for s in range(nsec):
-        lo, hi, st, ln, r, chk, fl = (int(x) for x in w[HEADER + SEC_WORDS * s:HEADER + SEC_WORDS * s + 7])
-        secs.append(dict(lo=lo, hi=hi, start=st, len=ln, reg=r, check=chk - (1 << 32) if chk >= 1 << 31 else chk,
-                         skip_reg=fl))
+    for k in range(nsec):
+        lo, hi, st, ln, r, chk, sk = (int(x) for x in w[HEADER + SEC_WORDS * k:HEADER + SEC_WORDS * k + 7])
+        secs.append(dict(lo=lo, hi=hi, start=st, len=ln, reg=r, check=s32(chk), skip_reg=sk))
+    tabs = []
+    for k in range(ntab):
+        q = [int(x) for x in w[u0 + TAB_WORDS * k:u0 + TAB_WORDS * (k + 1)]]
+        tabs.append(dict(lo=q[0], hi=q[1], kind=q[2], offs=[s32(q[4]), s32(q[5])][:q[3]], start=q[7], len=q[8],
+                         reg=q[9]))
     ins = []
     for t in range(nins):
         a0, a1, a2 = (int(x) for x in w[i0 + INS_WORDS * t:i0 + INS_WORDS * t + 3])
-        s32 = lambda u: u - (1 << 32) if u >= 1 << 31 else u
         ins.append((a0 & 255, (a0 >> 8) & 255, (a0 >> 16) & 255, (a0 >> 24) & 255, s32(a1), s32(a2)))
     consts = np.ascontiguousarray(coef, dtype=np.float64)[c0:c0 + ncst].copy()
-    return dict(n=n, nreg=nreg, value=(vs, vl), result=res, prologue=(ps, pl), sections=secs, skip=skip,
-                instructions=ins, consts=consts)
+    return dict(n=n, nreg=nreg, value=(vs, vl), result=res, prologue=(ps, pl), sections=secs, tables=tabs,
+                skip=skip, instructions=ins, consts=consts)
 
 
 def disassemble(coef: np.ndarray) -> str:
@@ -749,6 +824,9 @@ def disassemble(coef: np.ndarray) -> str:
             s = f"for i in {i1}..{i2 - 1}:"
         elif op == ENDLOOP:
             s = "end"
+        elif op == TRED:
+            tb = p["tables"][i1]
+            s = f"r{d} = {'sum' if tb['kind'] == 0 else 'prod'}(r{a}, table {i1})"
         else:
             s = f"r{d} = {name.lower()}(r{a})"
         out.append(f"{t:4d}  {s}")
@@ -761,6 +839,9 @@ def disassemble(coef: np.ndarray) -> str:
                    f"gradient r{s['reg']}, KKT bounds of j{s['check']:+d}{sk}")
     if p["skip"] != NO_SKIP:
         out.append(f"skip the gradient test when every coordinate contains {float(p['consts'][p['skip']])!r}")
+    for k, t in enumerate(p["tables"]):
+        out.append(f"table {k}: {'sum' if t['kind'] == 0 else 'product'} over i in {t['lo']}..{t['hi'] - 1} of "
+                   f"code {t['start']}..{t['start'] + t['len'] - 1} (r{t['reg']}), reads X[i{t['offs']}]")
     return "\n".join(out)
 
 
@@ -773,61 +854,73 @@ def point_value(coef: np.ndarray, x: Sequence[float]) -> float:
     if x.size != n:
         raise CodeListError("point of the wrong dimension")
     c = p["consts"]
-    R = [0.0] * max(p["nreg"], 1)
     ins = p["instructions"]
+
+    def run(start, length, R, i0=0):
+        pc, i, hi, body = start, i0, 0, 0
+
+        def idx(b, o):
+            return (0 if b == BASE_ABS else i) + o
+
+        while pc < start + length:
+            op, d, a, b, i1, i2 = ins[pc]
+            if op == LDX:
+                R[d] = float(x[idx(a, i1)])
+            elif op == LDC:
+                R[d] = float(c[i2])
+            elif op == LDI:
+                R[d] = 0.5 * (float(c[i2]) + float(c[i2 + 1]))
+            elif op == LDK:
+                R[d] = float(c[i2 + idx(a, i1)])
+            elif op == LDKI:
+                k = i2 + 2 * idx(a, i1)
+                R[d] = 0.5 * (float(c[k]) + float(c[k + 1]))
+            elif op == ADD:
+                R[d] = R[a] + R[b]
+            elif op == MINUS:
+                R[d] = R[a] - R[b]
+            elif op == MUL:
+                R[d] = R[a] * R[b]
+            elif op == DIV:
+                R[d] = R[a] / R[b] if R[b] != 0 else math.copysign(math.inf, R[a])
+            elif op == TIMES:
+                R[d] = R[a] * float(c[i2])
+            elif op == PLUS:
+                R[d] = R[a] + float(c[i2])
+            elif op == TIMESK:
+                R[d] = R[a] * float(c[i2 + idx(b, i1)])
+            elif op == PLUSK:
+                R[d] = R[a] + float(c[i2 + idx(b, i1)])
+            elif op == SQR:
+                R[d] = R[a] * R[a]
+            elif op == SQRT:
+                R[d] = math.sqrt(max(R[a], 0.0))
+            elif op == EXP:
+                R[d] = math.exp(R[a]) if R[a] < 709 else math.inf
+            elif op == SIN:
+                R[d] = math.sin(R[a])
+            elif op == COS:
+                R[d] = math.cos(R[a])
+            elif op == MOV:
+                R[d] = R[a]
+            elif op == LOOP:
+                i, hi, body = i1, i2, pc + 1
+            elif op == ENDLOOP:
+                i += 1
+                if i < hi:
+                    pc = body
+                    continue
+            elif op == TRED:
+                t = p["tables"][i1]
+                acc = R[a]
+                for k in range(t["lo"], t["hi"]):
+                    R2 = [0.0] * max(p["nreg"], 1)
+                    run(t["start"], t["len"], R2, k)
+                    acc = acc + R2[t["reg"]] if t["kind"] == 0 else acc * R2[t["reg"]]
+                R[d] = acc
+            pc += 1
+
+    R = [0.0] * max(p["nreg"], 1)
     vs, vl = p["value"]
-    pc, i, hi, body = vs, 0, 0, 0
-
-    def idx(b, o):
-        return (0 if b == BASE_ABS else i) + o
-
-    while pc < vs + vl:
-        op, d, a, b, i1, i2 = ins[pc]
-        if op == LDX:
-            R[d] = float(x[idx(a, i1)])
-        elif op == LDC:
-            R[d] = float(c[i2])
-        elif op == LDI:
-            R[d] = 0.5 * (float(c[i2]) + float(c[i2 + 1]))
-        elif op == LDK:
-            R[d] = float(c[i2 + idx(a, i1)])
-        elif op == LDKI:
-            k = i2 + 2 * idx(a, i1)
-            R[d] = 0.5 * (float(c[k]) + float(c[k + 1]))
-        elif op == ADD:
-            R[d] = R[a] + R[b]
-        elif op == MINUS:
-            R[d] = R[a] - R[b]
-        elif op == MUL:
-            R[d] = R[a] * R[b]
-        elif op == DIV:
-            R[d] = R[a] / R[b] if R[b] != 0 else math.copysign(math.inf, R[a])
-        elif op == TIMES:
-            R[d] = R[a] * float(c[i2])
-        elif op == PLUS:
-            R[d] = R[a] + float(c[i2])
-        elif op == TIMESK:
-            R[d] = R[a] * float(c[i2 + idx(b, i1)])
-        elif op == PLUSK:
-            R[d] = R[a] + float(c[i2 + idx(b, i1)])
-        elif op == SQR:
-            R[d] = R[a] * R[a]
-        elif op == SQRT:
-            R[d] = math.sqrt(max(R[a], 0.0))
-        elif op == EXP:
-            R[d] = math.exp(R[a]) if R[a] < 709 else math.inf
-        elif op == SIN:
-            R[d] = math.sin(R[a])
-        elif op == COS:
-            R[d] = math.cos(R[a])
-        elif op == MOV:
-            R[d] = R[a]
-        elif op == LOOP:
-            i, hi, body = i1, i2, pc + 1
-        elif op == ENDLOOP:
-            i += 1
-            if i < hi:
-                pc = body
-                continue
-        pc += 1
+    run(vs, vl, R)
     return R[p["result"]]

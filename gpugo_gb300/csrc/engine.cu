@@ -435,6 +435,7 @@ __device__ __forceinline__ int find_seg(const long long* pref, int n, long long 
 // phase A: term tables; items are dealt round-robin over the blocks so that the
 // FP64 work of a single instance spreads over every SM
 // ---------------------------------------------------------------------------
+template <bool CL>
 __device__ void phase_tables(const KArgs& a) {
   bstamp(a, 0);
   const long long tot = a.ctl->totA;
@@ -453,7 +454,7 @@ __device__ void phase_tables(const KArgs& a) {
     int s = a.idsA[k];
     const Desc& D = a.desc[s];
     const State& st = a.st[s];
-    build_item(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k]);
+    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k]);
   }
   __syncthreads();
   bstamp(a, 1);
@@ -1500,7 +1501,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
     a.cur_it = it;
     stamp(a, it, 0);
-    phase_tables(a);
+    phase_tables<CL>(a);
     if (!grid_barrier(a, NoTail{})) return;
     stamp(a, it, 1);
     phase_bound<CL>(a);
@@ -1894,12 +1895,14 @@ int ilog2_exact(int w) {
 // can form over the range of its loop or gradient section (coordinates,
 // constants, registers), and that every register is written before it is read.
 // The device interpreter relies on this and checks nothing itself.
+// tb: the words of a term table when the code is its body (X read only as
+// X[i + o] for the table's offsets o; no loops, no reductions).
 static int cl_check_code(const double* cf, int64_t I, int nins, int start, int len, int n, int64_t ncst, int nreg,
-                         int jlo, int jhi, bool allow_j, uint32_t* written) {
+                         int jlo, int jhi, bool allow_j, uint32_t* written, const uint32_t* tb, int ntab) {
   if (start < 0 || len < 0 || (int64_t)start + len > nins) return GPUGO_ERR_INVALID;
   auto word = [&](int64_t k) { uint64_t u; memcpy(&u, cf + k, 8); return (uint32_t)u; };
-  bool in_loop = false;
-  int64_t lo = 0, hi = 0;
+  bool in_loop = tb != nullptr;
+  int64_t lo = tb ? tb[CLT_LO] : 0, hi = tb ? tb[CLT_HI] : 0;
   for (int p = start; p < start + len; ++p) {
     const int64_t q = I + (int64_t)CL_INS * p;
     const uint32_t w0 = word(q);
@@ -1927,14 +1930,23 @@ static int cl_check_code(const double* cf, int64_t I, int nins, int start, int l
         reads = 1u << a;
         break;
       case CL_LOOP:
-        if (in_loop || i1 < 0 || i1 >= i2 || i2 > n) return GPUGO_ERR_INVALID;
+        if (tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return GPUGO_ERR_INVALID;
         in_loop = true; lo = i1; hi = i2;
         continue;
       case CL_ENDLOOP:
-        if (!in_loop) return GPUGO_ERR_INVALID;
+        if (tb || !in_loop) return GPUGO_ERR_INVALID;
         in_loop = false;
         continue;
+      case CL_TRED:
+        if (tb || i1 < 0 || i1 >= ntab || a >= nreg) return GPUGO_ERR_INVALID;
+        reads = 1u << a;
+        break;
       default:
+        return GPUGO_ERR_INVALID;
+    }
+    if (tb && op == CL_LDX) {   // only X[i + o], o one of the table's offsets
+      const uint32_t no = tb[CLT_NOFF];
+      if (a != 1 || !((no > 0 && i1 == (int32_t)tb[CLT_OFF0]) || (no > 1 && i1 == (int32_t)tb[CLT_OFF1])))
         return GPUGO_ERR_INVALID;
     }
     if (d >= nreg || (reads & ~*written)) return GPUGO_ERR_INVALID;
@@ -1953,7 +1965,7 @@ static int cl_check_code(const double* cf, int64_t I, int nins, int start, int l
     }
     *written |= 1u << d;
   }
-  return in_loop ? GPUGO_ERR_INVALID : GPUGO_OK;
+  return (in_loop && !tb) ? GPUGO_ERR_INVALID : GPUGO_OK;
 }
 
 int validate_codelist(const gpugo_spec* s) {
@@ -1969,19 +1981,40 @@ int validate_codelist(const gpugo_spec* s) {
   if (h[CLH_MAGIC] != CL_MAGIC || (int)h[CLH_N] != s->n) return GPUGO_ERR_INVALID;
   if (h[CLH_NREG] < 1 || h[CLH_NREG] > CL_MAXREG || h[CLH_NINS] > (1u << 20) || h[CLH_NCST] > (1u << 26))
     return GPUGO_ERR_INVALID;
-  if (h[CLH_NSEC] > (uint32_t)s->n) return GPUGO_ERR_INVALID;
-  const int64_t I = CL_HEADER + (int64_t)CL_SEC * h[CLH_NSEC];
+  if (h[CLH_NSEC] > (uint32_t)s->n || h[CLH_NTAB] > CL_MAXTAB) return GPUGO_ERR_INVALID;
+  const int64_t U = CL_HEADER + (int64_t)CL_SEC * h[CLH_NSEC];
+  const int64_t I = U + (int64_t)CL_TAB * h[CLH_NTAB];
   const int64_t C = I + (int64_t)CL_INS * h[CLH_NINS];
   if (s->ncoef < C + (int64_t)h[CLH_NCST]) return GPUGO_ERR_INVALID;
   for (int64_t k = CL_HEADER; k < C; ++k) { uint32_t t; if (!word(k, &t)) return GPUGO_ERR_INVALID; }
-  const int n = s->n, nreg = (int)h[CLH_NREG], nins = (int)h[CLH_NINS];
+  const int n = s->n, nreg = (int)h[CLH_NREG], nins = (int)h[CLH_NINS], ntab = (int)h[CLH_NTAB];
   const int64_t ncst = h[CLH_NCST];
+  for (int t = 0; t < ntab; ++t) {
+    uint32_t tb[CL_TAB];
+    for (int k = 0; k < CL_TAB; ++k) word(U + (int64_t)CL_TAB * t + k, &tb[k]);
+    const uint32_t no = tb[CLT_NOFF];
+    if (tb[CLT_LO] >= tb[CLT_HI] || tb[CLT_HI] > (uint32_t)n || tb[CLT_KIND] > 1 || no > 2) return GPUGO_ERR_INVALID;
+    for (uint32_t k = 0; k < no; ++k) {
+      const int64_t o = (int32_t)tb[CLT_OFF0 + k];
+      if ((int64_t)tb[CLT_LO] + o < 0 || (int64_t)tb[CLT_HI] - 1 + o >= n) return GPUGO_ERR_INVALID;
+    }
+    if (no == 2 && tb[CLT_OFF0] == tb[CLT_OFF1]) return GPUGO_ERR_INVALID;
+    double cells = 1.0;
+    for (uint32_t k = 0; k < no; ++k) cells *= s->wid;
+    if (cells > 4096.0 || tb[CLT_REG] >= (uint32_t)nreg) return GPUGO_ERR_INVALID;
+    uint32_t wt = 0;
+    if (cl_check_code(cf, I, nins, (int)tb[CLT_START], (int)tb[CLT_LEN], n, ncst, nreg, 0, 0, false, &wt, tb, ntab))
+      return GPUGO_ERR_INVALID;
+    if (!(wt & (1u << tb[CLT_REG]))) return GPUGO_ERR_INVALID;
+  }
   uint32_t wv = 0;
   if (h[CLH_VL] < 1 || h[CLH_RES] >= (uint32_t)nreg) return GPUGO_ERR_INVALID;
-  if (cl_check_code(cf, I, nins, (int)h[CLH_VS], (int)h[CLH_VL], n, ncst, nreg, 0, 0, false, &wv)) return GPUGO_ERR_INVALID;
+  if (cl_check_code(cf, I, nins, (int)h[CLH_VS], (int)h[CLH_VL], n, ncst, nreg, 0, 0, false, &wv, nullptr, ntab))
+    return GPUGO_ERR_INVALID;
   if (!(wv & (1u << h[CLH_RES]))) return GPUGO_ERR_INVALID;
   uint32_t wp = 0;
-  if (cl_check_code(cf, I, nins, (int)h[CLH_PS], (int)h[CLH_PL], n, ncst, nreg, 0, 0, false, &wp)) return GPUGO_ERR_INVALID;
+  if (cl_check_code(cf, I, nins, (int)h[CLH_PS], (int)h[CLH_PL], n, ncst, nreg, 0, 0, false, &wp, nullptr, ntab))
+    return GPUGO_ERR_INVALID;
   if (h[CLH_SKIP] != CL_NONE && h[CLH_SKIP] >= (uint32_t)ncst) return GPUGO_ERR_INVALID;
   int prev_hi = 0;
   for (uint32_t q = 0; q < h[CLH_NSEC]; ++q) {
@@ -1994,7 +2027,8 @@ int validate_codelist(const gpugo_spec* s) {
     if (w[4] >= (uint32_t)nreg || (w[6] != CL_NONE && w[6] >= (uint32_t)nreg)) return GPUGO_ERR_INVALID;
     if ((int64_t)lo + chk < 0 || (int64_t)hi - 1 + chk >= n) return GPUGO_ERR_INVALID;
     uint32_t ws = wp;
-    if (cl_check_code(cf, I, nins, (int)w[2], (int)w[3], n, ncst, nreg, lo, hi, true, &ws)) return GPUGO_ERR_INVALID;
+    if (cl_check_code(cf, I, nins, (int)w[2], (int)w[3], n, ncst, nreg, lo, hi, true, &ws, nullptr, ntab))
+      return GPUGO_ERR_INVALID;
     if (!(ws & (1u << w[4])) || (w[6] != CL_NONE && !(ws & (1u << w[6])))) return GPUGO_ERR_INVALID;
   }
   return GPUGO_OK;
@@ -2032,6 +2066,7 @@ int validate(const gpugo_spec* s) {
 
 struct Layout {
   int64_t cst, tab, t_off[T_NOFF], a_items;
+  int64_t cl_toff[CL_MAXTAB];
   int64_t pool_cap, parent_cap, tiles_cap, ubc_cap, out_cap, trace_cap;
   int64_t bytes;
   // byte offsets
@@ -2067,10 +2102,24 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
       put(T_LO, (n - 1) * w * w); put(T_SHI, (n - 1) * w * w * S); put(T_PRB, (n * w * w * w + 7) / 8);
       L->a_items = (n - 1) * w * w * (S + 1) + n * w * w * w;
       break;
-    case GPUGO_CODELIST:
+    case GPUGO_CODELIST: {
       put(T_LO, 2 * n * w); put(T_SHI, n * w * S);
       L->a_items = n * w * (S + 1);
+      // term tables: [S + 1 passes][hi - lo][w^offsets] intervals each
+      auto word = [&](int64_t k) { uint64_t u; memcpy(&u, s->coef + k, 8); return (uint32_t)u; };
+      const int64_t U = CL_HEADER + (int64_t)CL_SEC * word(CLH_NSEC);
+      const int ntab = (int)word(CLH_NTAB);
+      for (int t = 0; t < ntab; ++t) {
+        const int64_t q = U + (int64_t)CL_TAB * t;
+        int64_t cells = 1;
+        for (uint32_t k = 0; k < word(q + CLT_NOFF); ++k) cells *= w;
+        const int64_t items = (S + 1) * (int64_t)(word(q + CLT_HI) - word(q + CLT_LO)) * cells;
+        L->cl_toff[t] = o;
+        o += 2 * items;
+        L->a_items += items;
+      }
       break;
+    }
     case GPUGO_EXPSQRT:
       put(T_SQ, 2 * n * w); put(T_CS, 2 * n * w); put(T_XI, 2 * n * w); put(T_SN, 2 * n * w);
       put(T_ZB, (n * w + 7) / 8); put(T_SQS, 2 * n * w * S); put(T_CSS, 2 * n * w * S);
@@ -2138,6 +2187,7 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->tiles_cap = L.tiles_cap; D->ubc_cap = L.ubc_cap; D->a_items = L.a_items;
   D->tab_doubles = L.tab;
   for (int i = 0; i < T_NOFF; ++i) D->t_off[i] = L.t_off[i];
+  for (int i = 0; i < CL_MAXTAB; ++i) D->cl_toff[i] = L.cl_toff[i];
   D->dom = (const double*)(base + L.o_dom);
   D->coef = (const double*)(base + L.o_coef);
   D->cst = (double*)(base + L.o_cst);

@@ -51,6 +51,7 @@ struct Desc {
   long long a_items;                 // table-build work items per iteration
   long long tab_doubles;             // table region size (doubles)
   long long t_off[T_NOFF];           // table offsets (doubles)
+  long long cl_toff[8];              // code lists: offsets of the term tables (doubles)
   const double* dom;                 // [2n]
   const double* coef;
   double* cst;                       // derived constants
@@ -393,8 +394,11 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
   }
 }
 
+template <bool CL = true>
 __device__ __forceinline__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
-  if (D.family == FAM_CODELIST) { cl_build_item(D, pbox, pw, cyc, t); return; }
+  if constexpr (CL) {
+    if (D.family == FAM_CODELIST) { cl_build_item(D, pbox, pw, cyc, t); return; }
+  }
   if (D.a_items < (1LL << 31)) build_item_t<unsigned>(D, pbox, pw, cyc, (unsigned)t);
   else build_item_t<unsigned long long>(D, pbox, pw, cyc, (unsigned long long)t);
 }

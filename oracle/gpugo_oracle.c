@@ -667,13 +667,15 @@ static inline double sample_pt(iv x, int S, int j)
 /* ------------------------------------------------------------------------- */
 enum {
     CL_LDX = 1, CL_LDC, CL_LDI, CL_LDK, CL_LDKI, CL_ADD, CL_MINUS, CL_MUL, CL_DIV, CL_TIMES, CL_PLUS,
-    CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP
+    CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP, CL_TRED
 };
-enum { CL_MAGIC = 0x314C4347u, CL_HEADER = 12, CL_SEC = 8, CL_INS = 4, CL_MAXREG = 16 };
+enum { CL_MAGIC = 0x314C4347u, CL_HEADER = 16, CL_SEC = 8, CL_TAB = 12, CL_INS = 4, CL_MAXREG = 16, CL_MAXTAB = 8 };
 #define CL_NONE 0xFFFFFFFFu
 
 /* header words */
-enum { H_MAGIC, H_N, H_NREG, H_NINS, H_NCST, H_VS, H_VL, H_PS, H_PL, H_NSEC, H_SKIP, H_RES };
+enum { H_MAGIC, H_N, H_NREG, H_NINS, H_NCST, H_VS, H_VL, H_PS, H_PL, H_NSEC, H_SKIP, H_RES, H_NTAB };
+/* term-table words: a reduction whose body is evaluated per coordinate (TRED) */
+enum { T_LO_, T_HI_, T_KIND, T_NOFF, T_OFF0, T_OFF1, T_PAD, T_START, T_LEN, T_REG };
 
 static inline uint32_t cl_u32(double d) { uint64_t u = d2u(d); return (uint32_t)u; }
 static inline int cl_hi_zero(double d) { return (d2u(d) >> 32) == 0; }
@@ -685,12 +687,15 @@ static inline long cl_idx(int base, int32_t off, long i, long j)
 }
 
 /* Checks every instruction once, over the ranges its indexes can take, so that
- * the interpreter never reads outside the coordinates, constants or registers. */
+ * the interpreter never reads outside the coordinates, constants or registers.
+ * tb (a table body, or NULL): X is read only as X[i + o] for the table's
+ * offsets o, i in [lo, hi); no loops and no nested reductions. */
 static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int n, int ncst, int nreg,
-                          int jlo, int jhi, int allow_j, uint32_t* written)
+                          int jlo, int jhi, int allow_j, uint32_t* written, const uint32_t* tb, int ntab)
 {
     long lo = 0, hi = 0;
     int in_loop = 0;
+    if (tb) { in_loop = 1; lo = tb[T_LO_]; hi = tb[T_HI_]; }
     if (start < 0 || len < 0 || (long)start + len > nins) return -2;
     for (int p = start; p < start + len; ++p) {
         const uint32_t* w = ins + (size_t)CL_INS * p;
@@ -720,15 +725,23 @@ static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int
             reads = 1u << a;
             break;
         case CL_LOOP:
-            if (in_loop || i1 < 0 || i1 >= i2 || i2 > n) return -2;
+            if (tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return -2;
             in_loop = 1; lo = i1; hi = i2;
             continue;
         case CL_ENDLOOP:
-            if (!in_loop) return -2;
+            if (tb || !in_loop) return -2;
             in_loop = 0;
             continue;
+        case CL_TRED:
+            if (tb || i1 < 0 || i1 >= ntab || a >= nreg) return -2;
+            reads = 1u << a;
+            break;
         default:
             return -2;
+        }
+        if (tb && op == CL_LDX) {   /* only X[i + o], o one of the table's offsets */
+            uint32_t no = tb[T_NOFF];
+            if (a != 1 || !((no > 0 && i1 == (int32_t)tb[T_OFF0]) || (no > 1 && i1 == (int32_t)tb[T_OFF1]))) return -2;
         }
         if (d >= nreg || (reads & ~*written)) return -2;   /* a register is written before it is read */
         if (base >= 0) {
@@ -747,7 +760,7 @@ static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int
         }
         *written |= 1u << d;
     }
-    return in_loop ? -2 : 0;
+    return (in_loop && !tb) ? -2 : 0;
 }
 
 static int cl_parse(const oc_spec* sp, consts* c)
@@ -760,8 +773,8 @@ static int cl_parse(const oc_spec* sp, consts* c)
     for (int k = 0; k < CL_HEADER; ++k) h[k] = cl_u32(cf[k]);
     if (h[H_MAGIC] != CL_MAGIC || (int)h[H_N] != sp->n) return -2;
     if (h[H_NREG] < 1 || h[H_NREG] > CL_MAXREG || h[H_NINS] > (1u << 20) || h[H_NCST] > (1u << 26)) return -2;
-    if (h[H_NSEC] > (uint32_t)sp->n) return -2;
-    int64_t nw = CL_HEADER + (int64_t)CL_SEC * h[H_NSEC] + (int64_t)CL_INS * h[H_NINS];
+    if (h[H_NSEC] > (uint32_t)sp->n || h[H_NTAB] > CL_MAXTAB) return -2;
+    int64_t nw = CL_HEADER + (int64_t)CL_SEC * h[H_NSEC] + (int64_t)CL_TAB * h[H_NTAB] + (int64_t)CL_INS * h[H_NINS];
     if (nc < nw + (int64_t)h[H_NCST]) return -2;
     uint32_t* w = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)nw);
     if (!w) return -1;
@@ -771,13 +784,28 @@ static int cl_parse(const oc_spec* sp, consts* c)
     }
     c->clw = w;
     c->clc = cf + nw;
-    const int n = sp->n, nreg = (int)h[H_NREG], nins = (int)h[H_NINS], ncst = (int)h[H_NCST];
-    const uint32_t* ins = w + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    const int n = sp->n, nreg = (int)h[H_NREG], nins = (int)h[H_NINS], ncst = (int)h[H_NCST], ntab = (int)h[H_NTAB];
+    const uint32_t* tabs = w + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    const uint32_t* ins = tabs + (size_t)CL_TAB * ntab;
+    for (int t = 0; t < ntab; ++t) {
+        const uint32_t* tb = tabs + (size_t)CL_TAB * t;
+        const uint32_t no = tb[T_NOFF];
+        if (tb[T_LO_] >= tb[T_HI_] || tb[T_HI_] > (uint32_t)n || tb[T_KIND] > 1 || no > 2) return -2;
+        for (uint32_t k = 0; k < no; ++k) {
+            const long o = (int32_t)tb[T_OFF0 + k];
+            if ((long)tb[T_LO_] + o < 0 || (long)tb[T_HI_] - 1 + o >= n) return -2;
+        }
+        if (no == 2 && tb[T_OFF0] == tb[T_OFF1]) return -2;
+        uint32_t wt = 0;
+        if (tb[T_REG] >= (uint32_t)nreg) return -2;
+        if (cl_check_range(ins, nins, (int)tb[T_START], (int)tb[T_LEN], n, ncst, nreg, 0, 0, 0, &wt, tb, ntab)) return -2;
+        if (!(wt & (1u << tb[T_REG]))) return -2;
+    }
     uint32_t wv = 0, wp = 0;
     if (h[H_VL] < 1 || h[H_RES] >= (uint32_t)nreg) return -2;
-    if (cl_check_range(ins, nins, (int)h[H_VS], (int)h[H_VL], n, ncst, nreg, 0, 0, 0, &wv)) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_VS], (int)h[H_VL], n, ncst, nreg, 0, 0, 0, &wv, NULL, ntab)) return -2;
     if (!(wv & (1u << h[H_RES]))) return -2;
-    if (cl_check_range(ins, nins, (int)h[H_PS], (int)h[H_PL], n, ncst, nreg, 0, 0, 0, &wp)) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_PS], (int)h[H_PL], n, ncst, nreg, 0, 0, 0, &wp, NULL, ntab)) return -2;
     if (h[H_SKIP] != CL_NONE && h[H_SKIP] >= (uint32_t)ncst) return -2;
     int prev_hi = 0;
     for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
@@ -790,19 +818,21 @@ static int cl_parse(const oc_spec* sp, consts* c)
         if (r >= nreg || (rs != CL_NONE && rs >= (uint32_t)nreg)) return -2;
         if ((long)lo + chk < 0 || (long)hi - 1 + chk >= n) return -2;
         uint32_t ws = wp;
-        if (cl_check_range(ins, nins, st, ln, n, ncst, nreg, lo, hi, 1, &ws)) return -2;
+        if (cl_check_range(ins, nins, st, ln, n, ncst, nreg, lo, hi, 1, &ws, NULL, ntab)) return -2;
         if (!(ws & (1u << r)) || (rs != CL_NONE && !(ws & (1u << rs)))) return -2;
     }
     return 0;
 }
 
-/* Runs instructions start .. start+len-1; j is the gradient coordinate. */
-static void cl_exec(const consts* c, int start, int len, const iv* X, iv* R, long j)
+/* Runs instructions start .. start+len-1; j is the gradient coordinate, i0 the
+ * loop index of a table body. */
+static void cl_exec(const consts* c, int start, int len, const iv* X, iv* R, long j, long i0)
 {
     const uint32_t* h = c->clw;
-    const uint32_t* ins = h + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    const uint32_t* tabs = h + CL_HEADER + (size_t)CL_SEC * h[H_NSEC];
+    const uint32_t* ins = tabs + (size_t)CL_TAB * h[H_NTAB];
     const double* K = c->clc;
-    long i = 0, hi = 0;
+    long i = i0, hi = 0;
     int body = 0;
     for (int p = start; p < start + len; ++p) {
         const uint32_t* w = ins + (size_t)CL_INS * p;
@@ -831,6 +861,19 @@ static void cl_exec(const consts* c, int start, int len, const iv* X, iv* R, lon
         case CL_MOV: R[d] = R[a]; break;
         case CL_LOOP: i = i1; hi = i2; body = p + 1; break;
         case CL_ENDLOOP: if (++i < hi) p = body - 1; break;
+        case CL_TRED: {
+            /* the loop the table stands for: acc op= body(k) for k in [lo, hi) */
+            const uint32_t* tb = tabs + (size_t)CL_TAB * i1;
+            iv acc = R[a];
+            for (long k = tb[T_LO_]; k < (long)tb[T_HI_]; ++k) {
+                iv R2[CL_MAXREG];
+                for (int q = 0; q < CL_MAXREG; ++q) R2[q] = mk(0.0, 0.0);
+                cl_exec(c, (int)tb[T_START], (int)tb[T_LEN], X, R2, j, k);
+                acc = tb[T_KIND] ? ia_mul(acc, R2[tb[T_REG]]) : ia_add(acc, R2[tb[T_REG]]);
+            }
+            R[d] = acc;
+            break;
+        }
         }
     }
 }
@@ -840,7 +883,7 @@ static iv cl_value(const consts* c, const iv* X)
     const uint32_t* h = c->clw;
     iv R[CL_MAXREG];
     for (int k = 0; k < CL_MAXREG; ++k) R[k] = mk(0.0, 0.0);
-    cl_exec(c, (int)h[H_VS], (int)h[H_VL], X, R, 0);
+    cl_exec(c, (int)h[H_VS], (int)h[H_VL], X, R, 0, 0);
     return R[h[H_RES]];
 }
 
@@ -859,11 +902,11 @@ static int cl_deriv(const oc_spec* sp, const consts* c, const iv* X)
     }
     iv R[CL_MAXREG];
     for (int k = 0; k < CL_MAXREG; ++k) R[k] = mk(0.0, 0.0);
-    cl_exec(c, (int)h[H_PS], (int)h[H_PL], X, R, 0);
+    cl_exec(c, (int)h[H_PS], (int)h[H_PL], X, R, 0, 0);
     for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
         const uint32_t* q = h + CL_HEADER + (size_t)CL_SEC * s;
         for (long j = q[0]; j < (long)q[1]; ++j) {
-            cl_exec(c, (int)q[2], (int)q[3], X, R, j);
+            cl_exec(c, (int)q[2], (int)q[3], X, R, j, 0);
             if (q[6] != CL_NONE) {
                 const iv t = R[q[6]];
                 if (t.lo == -INFINITY || t.hi == INFINITY) continue;

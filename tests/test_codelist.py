@@ -188,17 +188,18 @@ def test_compile_rejects_bad_expressions():
         CL.compile_objective(nested, 17)
 
 
-def _mutations(coef):
+def _mutations(coef, tag):
     """Arrays that break one rule each; every one must be rejected."""
     p = CL.parse(coef)
     w = coef.view(np.uint64)
-    I = CL.HEADER + CL.SEC_WORDS * len(p["sections"])
+    U = CL.HEADER + CL.SEC_WORDS * len(p["sections"])
+    I = U + CL.TAB_WORDS * len(p["tables"])
     out = {}
 
     def put(name, k, v):
         c = coef.copy()
         c.view(np.uint64)[k] = v
-        out[name] = c
+        out[tag + ": " + name] = c
 
     put("magic", 0, 0x12345678)
     put("n", 1, int(w[1]) + 1)
@@ -206,21 +207,31 @@ def _mutations(coef):
     put("result register", 11, int(w[2]))
     put("high bits", 3, int(w[3]) | (1 << 40))
     put("truncated", 4, int(w[4]) + 100)
-    # instruction 0 reads X at an absolute index past the end
+    put("table count", 12, 9)
     ins = p["instructions"]
-    k = next(t for t, s in enumerate(ins) if s[0] == CL.LDX and s[2] == CL.BASE_ABS) if any(
-        s[0] == CL.LDX and s[2] == CL.BASE_ABS for s in ins) else None
-    if k is not None:
-        put("ldx index", I + CL.INS_WORDS * k + 1, p["n"])
+    ks = [t for t, s in enumerate(ins) if s[0] == CL.LDX and s[2] == CL.BASE_ABS]
+    if ks:
+        put("ldx index", I + CL.INS_WORDS * ks[0] + 1, p["n"])
     k = next(t for t, s in enumerate(ins) if s[0] == CL.LDC)
     put("constant index", I + CL.INS_WORDS * k + 2, len(p["consts"]))
     k = next(t for t, s in enumerate(ins) if s[0] == CL.ADD)
     op, d, a, b, _, _ = ins[k]
-    put("register index", I + CL.INS_WORDS * k, op | (d << 8) | (a << 16) | (15 << 24))  # never written
+    put("unwritten register", I + CL.INS_WORDS * k, op | (d << 8) | (a << 16) | (15 << 24))
     put("opcode", I + CL.INS_WORDS * k, 99 | (d << 8))
-    k = next(t for t, s in enumerate(ins) if s[0] == CL.LOOP)
-    put("loop range", I + CL.INS_WORDS * k + 2, p["n"] + 1)
-    put("nested loop", I + CL.INS_WORDS * (k + 1), CL.LOOP)
+    loops = [t for t, s in enumerate(ins) if s[0] == CL.LOOP]
+    if loops:
+        put("loop range", I + CL.INS_WORDS * loops[0] + 2, p["n"] + 1)
+        put("nested loop", I + CL.INS_WORDS * (loops[0] + 1), CL.LOOP)
+    if p["tables"]:
+        t0 = p["tables"][0]
+        put("table range", U + 1, p["n"] + 1)
+        put("table offset", U + 4, (t0["offs"][0] + p["n"]) & 0xFFFFFFFF if t0["offs"] else 0)
+        put("table kind", U + 2, 2)
+        put("table register", U + 9, 16)
+        body_ldx = [t for t in range(t0["start"], t0["start"] + t0["len"]) if ins[t][0] == CL.LDX]
+        put("table body reads another coordinate", I + CL.INS_WORDS * body_ldx[0] + 1, 7)
+        treds = [t for t, s in enumerate(ins) if s[0] == CL.TRED]
+        put("tred table index", I + CL.INS_WORDS * treds[0] + 1, len(p["tables"]))
     if p["sections"]:
         put("section range", CL.HEADER + 1, p["n"] + 1)
         put("check offset", CL.HEADER + 5, (-1) & 0xFFFFFFFF)
@@ -231,6 +242,7 @@ def test_oracle_and_library_reject_malformed_code_lists(oracle_lib):
     from gpugo_gb300 import _lib
     f, g, dom = O.levy(6)
     good = CL.compile_objective(f, 6, g).coef
+    loops = CL.compile_objective(f, 6, g, tables=False).coef
     p = P.Problem(P.CODELIST, 6, np.tile(dom, 6), good, wid=2, group=2)
     L = None
     try:
@@ -247,7 +259,9 @@ def test_oracle_and_library_reject_malformed_code_lists(oracle_lib):
     oracle_lib.eval_children(p, p.domain, 1, np.array([0], dtype=np.uint64), 1e300)
     if L is not None:
         assert lib_accepts(p)
-    for name, bad in _mutations(good).items():
+    bads = {**_mutations(good, "tables"), **_mutations(loops, "loops")}
+    assert any("table body" in k for k in bads) and any("nested loop" in k for k in bads)
+    for name, bad in bads.items():
         q = P.Problem(P.CODELIST, 6, p.domain, bad, wid=2, group=2)
         with pytest.raises(ValueError):
             oracle_lib.eval_children(q, q.domain, 1, np.array([0], dtype=np.uint64), 1e300)
@@ -258,4 +272,71 @@ def test_oracle_and_library_reject_malformed_code_lists(oracle_lib):
 def test_disassembly_names_every_instruction():
     f, g, _ = O.sinusoidal(4)
     text = CL.compile_objective(f, 4, g).disassemble()
-    assert "for i in 0..3:" in text and "section j in 0..3" in text and "div(" in text
+    assert "prod(r" in text and "table 1: product over i in 0..3" in text
+    assert "section j in 0..3" in text and "div(" in text
+    text = CL.compile_objective(f, 4, g, tables=False).disassemble()
+    assert "for i in 0..3:" in text and "table" not in text
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE))
+def test_term_tables_and_loops_agree_on_the_oracle(oracle_lib, name):
+    """A reduction compiled to a term table (TRED) and the same reduction as a
+    loop are one code list to the oracle: same bits."""
+    f, g, dom = O.REFERENCE[name](7)
+    a = P.Problem(P.CODELIST, 7, np.tile(dom, 7), CL.compile_objective(f, 7, g).coef, wid=3, group=4, samples=3)
+    b = P.Problem(P.CODELIST, 7, np.tile(dom, 7), CL.compile_objective(f, 7, g, tables=False).coef, wid=3,
+                  group=4, samples=3)
+    assert CL.parse(a.coef)["tables"] and not CL.parse(b.coef)["tables"]
+    codes = np.arange(81, dtype=np.uint64)
+    for cyc in (1, 5):
+        x = oracle_lib.eval_children(a, a.domain, cyc, codes[:3 ** (4 if cyc == 1 else 3)], 1e300)
+        y = oracle_lib.eval_children(b, b.domain, cyc, codes[:3 ** (4 if cyc == 1 else 3)], 1e300)
+        for u, v in zip(x, y):
+            assert np.array_equal(np.asarray(u).view(np.uint8), np.asarray(v).view(np.uint8))
+
+
+def _per_coordinate_gradients(grad, n):
+    """One gradient list per coordinate j, holding only j's section."""
+    out = []
+    for j in range(n):
+        for s in grad.sections:
+            lo = s.lo + n if s.lo < 0 else s.lo
+            hi = n if s.hi is None else (s.hi + n if s.hi < 0 else s.hi)
+            if lo <= j < hi:
+                out.append(CL.Gradient([CL.Section(s.expr, j, j + 1, s.check, s.skip_infinite)],
+                                       skip_if_contains=grad.skip_if_contains))
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE) + ["expsqrt", "prodcos", "chained"])
+def test_gradient_test_is_the_or_of_its_coordinates(oracle_lib, name):
+    """The derivative test over all coordinates rules a box out exactly when one
+    coordinate's test alone does (values computed once per box, such as the
+    Salomon radius, must survive every coordinate's section)."""
+    n = 6
+    if name in O.REFERENCE:
+        f, grad, dom = O.REFERENCE[name](n)
+        domain = np.tile(dom, n)
+    else:
+        fam = {"expsqrt": P.EXPSQRT, "prodcos": P.PRODCOS, "chained": P.CHAINED}[name]
+        base = P.instance(fam, n, 3)
+        f, grad = O.BUILTIN[fam](n, base.coef)
+        domain = base.domain
+    full = P.Problem(P.CODELIST, n, domain, CL.compile_objective(f, n, grad).coef, wid=2, group=1, samples=2)
+    singles = [P.Problem(P.CODELIST, n, domain, CL.compile_objective(f, n, g).coef, wid=2, group=1, samples=2)
+               for g in _per_coordinate_gradients(grad, n)]
+    rng = np.random.default_rng(17)
+    lo, hi = domain[0::2], domain[1::2]
+    seen = 0
+    for _ in range(60):
+        x = rng.uniform(lo, hi)
+        w = (hi - lo) * 10.0 ** rng.uniform(-7, -2, n)
+        # most coordinates straddle the point where their gradient changes sign less often
+        pbox = np.empty(2 * n)
+        pbox[0::2], pbox[1::2] = np.maximum(lo, x - w), np.minimum(hi, x + w)
+        code = np.array([0], dtype=np.uint64)
+        d_full = oracle_lib.eval_children(full, pbox, 1, code, 1e300)[3][0]
+        d_any = max(oracle_lib.eval_children(q, pbox, 1, code, 1e300)[3][0] for q in singles)
+        assert d_full == d_any, (name, pbox)
+        seen += d_full
+    assert seen > 0

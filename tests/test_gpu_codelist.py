@@ -121,6 +121,21 @@ def test_engine_mixed_batch(oracle_lib, mode, big):
             assert _same(rg.trace[k], ro.trace[k]), (p.tag, k)
 
 
+@pytest.mark.parametrize("name,n", [("levy", 9), ("sinusoidal", 6), ("salomon", 8), ("trigonometric", 7)])
+def test_term_tables_and_loops_same_solve(name, n):
+    """Reductions read from term tables give the solve the loop form gives."""
+    f, g, dom = O.REFERENCE[name](n)
+    base = O.problem(name, n, tol=1e-6)
+    loops = P.Problem(P.CODELIST, n, base.domain, CL.compile_objective(f, n, g, tables=False).coef, wid=base.wid,
+                      group=base.group, samples=base.samples, gap_tol=1e-6)
+    a = G.solve(base, box_cap=16, trace_cap=100000)
+    b = G.solve(loops, box_cap=16, trace_cap=100000)
+    assert (a.lb, a.ub, a.iterations, a.pool_size) == (b.lb, b.ub, b.iterations, b.pool_size)
+    for k in a.trace:
+        assert _same(a.trace[k], b.trace[k]), k
+    print(f"\n{name}{n}: tables {a.device_ms:.3f} ms, loops {b.device_ms:.3f} ms, {a.iterations} iterations")
+
+
 def test_malformed_code_list_is_rejected():
     f, g, dom = O.levy(5)
     coef = CL.compile_objective(f, 5, g).coef.copy()
