@@ -120,6 +120,7 @@ struct KArgs {
   long long cand_cap;
   int cand_mode;              // GPUGO_CAND_AUTO / _WARP / _LANE
   int max_slots;
+  int fam_hi;                 // highest family number resident (work lists are grouped up to it)
   long long max_iters;        // iterations in this launch (<= 0: until idle)
   unsigned long long timeout_ns;
   unsigned long long* stamps; // optional: %globaltimer at each barrier release
@@ -303,7 +304,7 @@ __device__ void build_lists(const KArgs& a) {
   block_exclusive_scan(cE, &tE);
   long long oR = block_exclusive_scan(cR, &tR);
   long long baseA = 0, baseSA = 0, baseSB = 0;
-  for (int f = grouped ? 1 : 0; f <= (grouped ? FAM_CODELIST : 0); ++f) {
+  for (int f = grouped ? 1 : 0; f <= (grouped ? a.fam_hi : 0); ++f) {
     long long cA = 0, sA = 0, sB = 0;
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
@@ -1119,6 +1120,7 @@ __device__ void prefill_ready(const KArgs& a) {
 // again in pass 2; the UB stays the minimum over the same set of sample values.
 // The same warp stores the instance's shared sample prefixes (samp_prefix), which
 // pass 2 then starts every candidate's sample passes from.
+template <bool CL>
 __device__ void phase_seed(const KArgs& a) {
   extern __shared__ double s_tab[];
   const int si = stage_tables(a);
@@ -1131,8 +1133,11 @@ __device__ void phase_seed(const KArgs& a) {
     const Desc& D = a.desc[s];
     State& st = a.st[s];
     const unsigned long long sk = st.seed_key;
-    // code lists have no seed pass: it only lowers the UB earlier in the iteration
-    if (sk == ~0ULL || D.family == FAM_CODELIST) continue;
+    if (sk == ~0ULL) continue;
+    if constexpr (CL) {
+      // code lists have no seed pass: it only lowers the UB earlier in the iteration
+      if (D.family == FAM_CODELIST) continue;
+    }
     const unsigned long long code = sk & 0xffffffffULL;
     const double* T = (s == si) ? s_tab : D.tab;
     ChildCtx C;
@@ -1507,7 +1512,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
     phase_bound<CL>(a);
     if (!grid_barrier(a, tp)) return;
     if (a.ctl->seed_on) {
-      phase_seed(a);
+      phase_seed<CL>(a);
       if (!grid_barrier(a, NoTail{})) return;
     }
     phase_candidates<CL>(a);
@@ -2826,6 +2831,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.cand_mode = E->cand_mode;
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;
+  a.fam_hi = FAM_PRODCOS;
   a.timeout_ns = (unsigned long long)(E->timeout_s * 1e9);
   a.stamps = E->d_stamps;
   a.stamp_cap = E->stamp_cap;
@@ -2836,6 +2842,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   bool any_cl = false;   // the build with the code-list interpreter only while one is resident
   for (int s = 0; s < E->max_slots && !any_cl; ++s) any_cl = E->slots[s].used && E->slots[s].spec.family == GPUGO_CODELIST;
   const void* kern = any_cl ? (const void*)solve_kernel<true> : (const void*)solve_kernel<false>;
+  if (any_cl) a.fam_hi = FAM_CODELIST;
   CK(cudaEventRecord(E->ev0, st));
   CK(cudaLaunchCooperativeKernel(kern, dim3(E->blocks), dim3(E->threads), args, SMEM_TAB_BYTES, st));
   CK(cudaEventRecord(E->ev1, st));

@@ -51,7 +51,6 @@ struct Desc {
   long long a_items;                 // table-build work items per iteration
   long long tab_doubles;             // table region size (doubles)
   long long t_off[T_NOFF];           // table offsets (doubles)
-  long long cl_toff[8];              // code lists: offsets of the term tables (doubles)
   const double* dom;                 // [2n]
   const double* coef;
   double* cst;                       // derived constants
@@ -70,6 +69,9 @@ struct Desc {
   long long* tr_surv;
   long long* tr_pool;
   long long* tr_sel;
+  // code lists: offsets of the term tables (doubles); last, so that the fields
+  // every iteration reads keep their cache lines
+  long long cl_toff[8];
 };
 
 // ---------------------------------------------------------------------------
@@ -570,8 +572,8 @@ __device__ __forceinline__ SAcc sacc_init(const Desc& D) {
 // coordinates before the split group, whose digit is 0 in every child) are the
 // same for all children of the parent
 __device__ __forceinline__ int samp_terms(const Desc& D) { return D.family == FAM_CHAINED ? D.n - 1 : D.n; }
+// (built-in families only: code lists have no seed pass and no sample prefixes)
 __device__ __forceinline__ int samp_shared(const Desc& D, ChildCtx C) {
-  if (D.family == FAM_CODELIST) return 0;   // no shared prefix: the list is not a plain reduction
   return D.family == FAM_CHAINED ? (C.c0 > 0 ? C.c0 - 1 : 0) : C.c0;
 }
 
