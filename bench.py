@@ -473,7 +473,7 @@ def main():
     ap.add_argument("--workload", default="cfg2",
                     choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "listpass", "codelist"],
                     help="cfg2 is the benchmark line; the others print their own records")
-    ap.add_argument("--count", type=int, default=1024)
+    ap.add_argument("--count", type=int, default=None, help="instances (cfg4: 1024) or requests (cfg5: 4096)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
@@ -481,6 +481,8 @@ def main():
                     help="cfg4/cfg5: skip the autotuner (block size, candidates per warp, fan-out)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.count is None:
+        args.count = 4096 if args.workload == "cfg5" else 1024
     ws, rank, local = dist_env()
     if args.workload != "cfg2" and args.impl == "gpugo":
         fn = {"cfg1": run_single, "cfg3": run_single, "cfg4": run_batched, "cfg5": run_serving,
