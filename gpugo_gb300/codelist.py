@@ -342,6 +342,190 @@ class Gradient:
 
 
 # ---------------------------------------------------------------------------
+# automatic gradient
+# ---------------------------------------------------------------------------
+_ONE = None   # set below (Const(1.0)); None stands for an exact zero
+
+
+def _is_one(e) -> bool:
+    return e is not None and e.key == _ONE.key
+
+
+def _add(u, v):
+    if u is None:
+        return v
+    if v is None:
+        return u
+    return Expr("add", (u, v))
+
+
+def _sub(u, v):
+    if v is None:
+        return u
+    if u is None:
+        return Expr("times", (v, -1.0))
+    return Expr("minus", (u, v))
+
+
+def _mul(u, v):
+    if u is None or v is None:
+        return None
+    if _is_one(u):
+        return v
+    if _is_one(v):
+        return u
+    return Expr("mul", (u, v))
+
+
+def _times(u, c: float):
+    if u is None:
+        return None
+    if _is_one(u):
+        return Const(c)
+    return Expr("times", (u, c))
+
+
+def _diff(e: Expr, wrt_key, memo: dict):
+    """d e / d (the node with key wrt_key), None for an exact zero.  Reductions
+    and coordinates other than wrt are constants here."""
+    k = e.key
+    if k == wrt_key:
+        return _ONE
+    if k in memo:
+        return memo[k]
+    op, a = e.op, e.args
+    if op in ("x", "ldc", "ldi", "ldk", "ldki", "sum", "prod"):
+        r = None
+    elif op in ("add", "minus"):
+        da, db = _diff(a[0], wrt_key, memo), _diff(a[1], wrt_key, memo)
+        r = _add(da, db) if op == "add" else _sub(da, db)
+    elif op == "mul":
+        r = _add(_mul(_diff(a[0], wrt_key, memo), a[1]), _mul(a[0], _diff(a[1], wrt_key, memo)))
+    elif op == "div":
+        da, db = _diff(a[0], wrt_key, memo), _diff(a[1], wrt_key, memo)
+        # (da - (a / b) db) / b
+        num = _sub(da, _mul(e, db))
+        r = None if num is None else Expr("div", (num, a[1]))
+    elif op == "times":
+        r = _times(_diff(a[0], wrt_key, memo), a[1])
+    elif op == "plus" or op == "plusk":
+        r = _diff(a[0], wrt_key, memo)
+    elif op == "timesk":
+        da = _diff(a[0], wrt_key, memo)
+        r = None if da is None else (a[1] if _is_one(da) else Expr("timesk", (da, a[1])))
+    elif op == "sqr":
+        r = _times(_mul(a[0], _diff(a[0], wrt_key, memo)), 2.0)
+    elif op == "sqrt":
+        da = _diff(a[0], wrt_key, memo)
+        r = None if da is None else _times(Expr("div", (da, e)), 0.5)
+    elif op == "exp":
+        r = _mul(e, _diff(a[0], wrt_key, memo))
+    elif op == "sin":
+        r = _mul(Expr("cos", (a[0],)), _diff(a[0], wrt_key, memo))
+    elif op == "cos":
+        r = _times(_mul(Expr("sin", (a[0],)), _diff(a[0], wrt_key, memo)), -1.0)
+    else:
+        raise CodeListError(f"no derivative rule for {op}")
+    memo[k] = r
+    return r
+
+
+def _leaves(e: Expr, out: dict):
+    """Reductions and fixed coordinates of the value expression (outside bodies)."""
+    if not isinstance(e, Expr):
+        return
+    if e.op in ("sum", "prod"):
+        out[e.key] = e
+        return
+    if e.op == "x":
+        if e.args[0] != BASE_ABS:
+            raise CodeListError("the value expression reads X[i] outside a Sum/Prod")
+        out[e.key] = e
+        return
+    for a in e.args:
+        if isinstance(a, Expr):
+            _leaves(a, out)
+
+
+def _shift(e, o: int, memo: dict):
+    """The body expression with the loop index i replaced by j - o (memo is per o)."""
+    if not isinstance(e, Expr):
+        return e
+    if e.key in memo:
+        return memo[e.key]
+    if e.op == "x":
+        base, off = e.args
+        r = Expr("x", (BASE_J, off - o)) if base == BASE_I else e
+    elif e.op in ("ldk", "ldki"):
+        base, off, arr = e.args
+        r = arr[Index(BASE_J, off - o)] if base == BASE_I else e
+    else:
+        args = tuple(_shift(a, o, memo) for a in e.args)
+        r = CoefRef.__new__(CoefRef) if isinstance(e, CoefRef) else Expr.__new__(Expr)
+        Expr.__init__(r, e.op, args)
+    memo[e.key] = r
+    return r
+
+
+def auto_gradient(f: Expr, n: int) -> Gradient:
+    """The gradient code list of a value expression, by symbolic differentiation.
+
+    d f / d x_j = sum over reductions R of (d f / d R) (d R / d x_j) plus, for a
+    fixed coordinate X[k], d f / d X[k] when j = k.  For R = Sum_i t(i):
+    d R / d x_j = sum over the offsets o of t of (d t / d X[i+o]) at i = j - o,
+    for j - o in R's range; for a product, (R / t(j - o)) (d t / d X[i+o]).
+    The coordinates where the set of terms changes split [0, n) into sections.
+    Every rule is exact, so the interval evaluation encloses the gradient; a
+    division by an interval containing zero (a product's term, a square root at
+    zero) gives an unbounded gradient and the test keeps the box."""
+    global _ONE
+    if _ONE is None:
+        _ONE = Const(1.0)
+    leaves: dict = {}
+    _leaves(f, leaves)
+    adj = {k: _diff(f, k, {}) for k in leaves}
+    # contributions: (j range, expression builder)
+    parts = []
+    for k, L in leaves.items():
+        if adj[k] is None:
+            continue
+        if L.op == "x":
+            c = L.args[1] + n if L.args[1] < 0 else L.args[1]
+            if not 0 <= c < n:
+                raise CodeListError(f"coordinate {L.args[1]} outside 0..{n - 1}")
+            parts.append((c, c + 1, adj[k]))
+            continue
+        body, lo, hi, init = L.args
+        hi = n if hi is None else (hi + n if hi < 0 else hi)
+        lo = lo + n if lo < 0 else lo
+        offs: set = set()
+        if not _table_offsets(body, offs):
+            raise CodeListError("automatic gradient: a Sum/Prod body may read the coordinates only as X[i + o]")
+        for o in sorted(offs):
+            dt = _diff(body, Expr("x", (BASE_I, o)).key, {})
+            if dt is None:
+                continue
+            memo: dict = {}
+            dj = _shift(dt, o, memo)
+            if L.op == "prod":
+                dj = _mul(Expr("div", (L, _shift(body, o, memo))), dj)
+            parts.append((lo + o, hi + o, _mul(adj[k], dj)))
+    cuts = sorted({0, n} | {max(0, min(n, p[0])) for p in parts} | {max(0, min(n, p[1])) for p in parts})
+    sections = []
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        if a >= b:
+            continue
+        terms = [e for lo, hi, e in parts if lo <= a and b <= hi]
+        if not terms:
+            continue
+        g = terms[0]
+        for t in terms[1:]:
+            g = Expr("add", (g, t))
+        sections.append(Section(lambda j, g=g: g, a, b))
+    return Gradient(sections)
+
+
+# ---------------------------------------------------------------------------
 # compiler
 # ---------------------------------------------------------------------------
 @dataclass
@@ -646,14 +830,20 @@ class CompiledCodeList:
         return disassemble(self.coef)
 
 
-def compile_objective(f: Expr, n: int, gradient: Gradient | None = None, tables: bool = True) -> CompiledCodeList:
+def compile_objective(f: Expr, n: int, gradient: Gradient | str | None = None,
+                      tables: bool = True) -> CompiledCodeList:
     """Compile the value expression (and optionally the gradient code list) for
-    dimension n into a ``GPUGO_CODELIST`` coefficient array.  ``tables=False``
+    dimension n into a ``GPUGO_CODELIST`` coefficient array.  ``gradient="auto"``
+    derives the gradient symbolically (:func:`auto_gradient`); ``tables=False``
     runs every reduction as a loop (same results, for checks)."""
     if not isinstance(f, Expr):
         raise CodeListError("the objective must be an expression")
     if n < 1:
         raise CodeListError("n must be positive")
+    if isinstance(gradient, str):
+        if gradient != "auto":
+            raise CodeListError("gradient must be a Gradient, \"auto\" or None")
+        gradient = auto_gradient(f, n)
     ctx = _Ctx(n, use_tables=tables)
     em = _Emitter(ctx)
     res = em.emit(f, None)

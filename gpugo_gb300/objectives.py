@@ -232,12 +232,15 @@ BUILTIN = {1: cosquad, 2: chained, 3: expsqrt, 4: prodcos}
 # problems
 # ---------------------------------------------------------------------------
 def problem(name: str, n: int, tol: float = 1e-6, split: tuple[int, int] | None = None, samples: int = 10,
-            domain: tuple[float, float] | None = None, with_gradient: bool = True) -> Problem:
-    """One of the reference benchmarks as a CODELIST problem of dimension n."""
+            domain: tuple[float, float] | None = None, with_gradient: bool | str = True) -> Problem:
+    """One of the reference benchmarks as a CODELIST problem of dimension n
+    (``with_gradient``: True the restated derivative list, "auto" the derived
+    one, False none)."""
     from .problems import default_split
     f, grad, dom = REFERENCE[name](n)
     dom = domain or dom
-    coef = compile_objective(f, n, grad if with_gradient else None).coef
+    g = grad if with_gradient is True else ("auto" if with_gradient == "auto" else None)
+    coef = compile_objective(f, n, g).coef
     wid, group = split or default_split(n)
     return Problem(CODELIST, n, np.tile(np.array(dom, dtype=np.float64), n), coef, wid=wid, group=group,
                    samples=samples, stop_mode=STOP_GAP, gap_tol=tol, tag=f"{name}{n}")

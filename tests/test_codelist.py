@@ -103,21 +103,23 @@ def test_reference_objectives_certify_on_the_oracle(oracle_lib, name):
     assert r.lb <= fmin + 1e-12 and fmin - 1e-6 <= r.ub
 
 
+@pytest.mark.parametrize("mode", ["written", "auto"])
 @pytest.mark.parametrize("name", sorted(O.REFERENCE) + ["cosquad", "chained", "expsqrt", "prodcos"])
-def test_gradient_lists_are_gradients_of_the_value_lists(oracle_lib, name):
+def test_gradient_lists_are_gradients_of_the_value_lists(oracle_lib, name, mode):
     """Where the central-difference gradient of the value list has a clear sign,
-    the derivative list rules out a tiny box around the point (a list that is
-    not the gradient of the value list, like the reference's Belegundu one,
-    fails this)."""
+    the derivative list (written out, or derived by the compiler) rules out a
+    tiny box around the point (a list that is not the gradient of the value
+    list, like the reference's Belegundu one, fails this)."""
     n = 5
     if name in O.REFERENCE:
         f, g, dom = O.REFERENCE[name](n)
-        coef = CL.compile_objective(f, n, g).coef
         domain = np.tile(dom, n)
     else:
         fam = {"cosquad": P.COSQUAD, "chained": P.CHAINED, "expsqrt": P.EXPSQRT, "prodcos": P.PRODCOS}[name]
         base = P.instance(fam, n, 7)
-        coef, domain = O.as_codelist(base).coef, base.domain
+        f, g = O.BUILTIN[fam](n, base.coef)
+        domain = base.domain
+    coef = CL.compile_objective(f, n, g if mode == "written" else "auto").coef
     p = P.Problem(P.CODELIST, n, domain, coef, wid=2, group=1, samples=2)
     rng = np.random.default_rng(11)
     lo, hi = domain[0::2], domain[1::2]
@@ -340,3 +342,50 @@ def test_gradient_test_is_the_or_of_its_coordinates(oracle_lib, name):
         assert d_full == d_any, (name, pbox)
         seen += d_full
     assert seen > 0
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE) + ["chained", "prodcos"])
+def test_auto_gradient_solves_certify(oracle_lib, name):
+    """Solves with the derived gradient certify and keep the known minimum."""
+    n = 6
+    if name in O.REFERENCE:
+        f, g, dom = O.REFERENCE[name](n)
+        domain = np.tile(dom, n)
+        fmin = {"levy": 0.0, "salomon": 0.0, "corrupted": -24.0, "deflected": -1.0, "cosine": -0.6,
+                "trigonometric": 1.0, "sinusoidal": -3.5}[name]
+    else:
+        fam = {"chained": P.CHAINED, "prodcos": P.PRODCOS}[name]
+        base = P.instance(fam, n, 9)
+        f, g = O.BUILTIN[fam](n, base.coef)
+        domain, fmin = base.domain, 0.0
+    wid, group = P.default_split(n)
+    res = {}
+    for tag, grad in (("written", g), ("auto", "auto"), ("none", None)):
+        p = P.Problem(P.CODELIST, n, domain, CL.compile_objective(f, n, grad).coef, wid=wid, group=group)
+        p.max_iter = 5000
+        res[tag] = oracle_lib.solve(p, box_cap=8, trace_cap=10000)
+        r = res[tag]
+        assert r.ub - r.lb <= 1e-6 and r.lb <= fmin + 1e-12 and fmin - 1e-6 <= r.ub, tag
+    # the derived test rules out boxes: never fewer survivors than no test at all
+    assert sum(res["auto"].trace["n_surv"]) <= sum(res["none"].trace["n_surv"])
+
+
+def test_auto_gradient_prunes_like_written_lists(oracle_lib):
+    """On the chained quartic (n = 20) the derived gradient removes most of what
+    the reference's factorised list removes."""
+    base = P.instance(P.CHAINED, 20, 320, 1e-6)
+    f, g = O.BUILTIN[P.CHAINED](20, base.coef)
+    surv = {}
+    for tag, grad in (("written", g), ("auto", "auto"), ("none", None)):
+        q = P.Problem(P.CODELIST, 20, base.domain, CL.compile_objective(f, 20, grad).coef, wid=base.wid,
+                      group=base.group)
+        surv[tag] = int(sum(oracle_lib.solve(q, box_cap=8, trace_cap=10000).trace["n_surv"]))
+    assert surv["written"] <= surv["auto"] < 0.6 * surv["none"]
+
+
+def test_auto_gradient_rejects_unsupported_bodies():
+    X = CL.X
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(CL.Sum(lambda i: X[i] * X[0]), 4, "auto")     # a fixed coordinate in a body
+    with pytest.raises(CL.CodeListError):
+        CL.compile_objective(X[0], 4, "derive")

@@ -136,6 +136,27 @@ def test_term_tables_and_loops_same_solve(name, n):
     print(f"\n{name}{n}: tables {a.device_ms:.3f} ms, loops {b.device_ms:.3f} ms, {a.iterations} iterations")
 
 
+AUTO = [("levy", 7), ("sinusoidal", 6), ("salomon", 9), ("chained", 12), ("prodcos", 10)]
+
+
+@pytest.mark.parametrize("name,n", AUTO, ids=[f"{a}{b}" for a, b in AUTO])
+def test_auto_gradient_solve_parity(oracle_lib, name, n):
+    """Gradients derived by the compiler, on the GPU against the oracle."""
+    if name in O.REFERENCE:
+        f, _, dom = O.REFERENCE[name](n)
+        domain = np.tile(dom, n)
+    else:
+        fam = {"chained": P.CHAINED, "prodcos": P.PRODCOS}[name]
+        base = P.instance(fam, n, 400 + n)
+        f, _ = O.BUILTIN[fam](n, base.coef)
+        domain = base.domain
+    wid, group = P.default_split(n)
+    p = P.Problem(P.CODELIST, n, domain, CL.compile_objective(f, n, "auto").coef, wid=wid, group=group, gap_tol=1e-6)
+    p.max_iter = 3000
+    rg, ro = _compare(p, oracle_lib)
+    assert rg.status == G.CERTIFIED
+
+
 def test_malformed_code_list_is_rejected():
     f, g, dom = O.levy(5)
     coef = CL.compile_objective(f, 5, g).coef.copy()
