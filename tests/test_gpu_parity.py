@@ -262,10 +262,16 @@ def test_bounded_wait_expires_cleanly():
     assert r.certified
 
 
+def _levy12_codelist():
+    from gpugo_gb300 import objectives as O
+    return O.problem("levy", 12, tol=1e-6)
+
+
 CKPT = [
     ("cfg2", lambda: P.config2()),
     ("expsqrt20", lambda: P.instance(P.EXPSQRT, 20, 18, 1e-6)),
     ("chained30", lambda: P.instance(P.CHAINED, 30, 22, 1e-6)),
+    ("levy12_codelist", _levy12_codelist),
 ]
 
 

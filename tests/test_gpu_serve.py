@@ -11,8 +11,14 @@ from gpugo_gb300.serve import serve
 pytestmark = pytest.mark.gpu
 
 
-def test_served_results_match_solo():
+@pytest.mark.parametrize("with_codelists", [False, True], ids=["builtin", "mixed"])
+def test_served_results_match_solo(with_codelists):
     probs = P.config4(count=18, seed=91, nmax=16) + [P.config1(), P.config2()]
+    if with_codelists:
+        from gpugo_gb300 import objectives as O
+        # code-list requests arrive between built-in ones: launches switch builds
+        probs = [q for pair in zip(probs[:7], [O.problem(n, 5) for n in sorted(O.REFERENCE)]) for q in pair]
+        probs += [O.as_codelist(P.config2())]
     for p in probs:
         p.max_iter = 2000
     stream = [(0.0002 * i, p) for i, p in enumerate(probs)]
