@@ -30,16 +30,17 @@ values and every copy keeps it bit for bit:
     [5] value start [6] value length  [7] gradient prologue start [8] length
     [9] sections    [10] skip constant (0xFFFFFFFF: none)  [11] value result register
     [12] term tables  [13..15] 0
-    [16 + 8s ...]   section s: lo, hi, start, length, gradient register, check
+    [16 + 12s ...]  section s: lo, hi, start, length, gradient register, check
                     offset, skip register (0xFFFFFFFF: none; the test is skipped
-                    when that register has an infinite end), 0
+                    when that register has an infinite end), tabled (0/1),
+                    offsets (0..3), offset 0, offset 1, offset 2
     [U + 12t ...]   term table t: lo, hi, kind (0 sum, 1 product), offsets (0..2),
                     offset 0, offset 1, 0, body start, body length, body result
                     register, 0, 0
     [I + 4t ...]    instruction t: op | dst << 8 | a << 16 | b << 24, imm1, imm2, 0
     [C ...]         constants (plain doubles)
 
-with U = 16 + 8 sections, I = U + 12 tables and C = I + 4 instructions.
+with U = 16 + 12 sections, I = U + 12 tables and C = I + 4 instructions.
 
 Term tables.  A Sum or Prod whose body reads the coordinates only as X[i + o]
 (at most two offsets o) and otherwise only coefficients and constants is a
@@ -49,6 +50,13 @@ coordinate i, every digit of the coordinates i + o and every sample pass into a
 table; a child then adds (multiplies) its entries.  The result is the one the
 loop gives: the same operations on the same inputs, accumulated in the same
 order.  Other bodies run as a loop (LOOP .. ENDLOOP) in the child's code.
+
+Tabled sections.  A gradient section whose expression reads the coordinates only
+as X[j + o] (at most three offsets, the KKT test's own coordinate included) and
+otherwise constants and coefficients is compiled self-contained (it reads no
+prologue register); the device evaluates its KKT test once per iteration for
+every coordinate j and digit combination of the coordinates j + o, and a
+candidate only looks its flags up.  The flag is the one the section's code gives.
 """
 from __future__ import annotations
 
@@ -62,7 +70,9 @@ import numpy as np
 MAGIC = 0x314C4347
 MAX_REGS = 16
 HEADER = 16
-SEC_WORDS = 8
+SEC_WORDS = 12
+MAX_TABLED_SECTIONS = 8
+MAX_SECTION_OFFSETS = 3
 TAB_WORDS = 12
 INS_WORDS = 4
 MAX_TABLES = 8
@@ -467,6 +477,25 @@ def _shift(e, o: int, memo: dict):
     return r
 
 
+def _rebase_abs(e, c: int, n: int, memo: dict):
+    """In a section of the single coordinate c, the fixed coordinate X[k] is X[j + k - c]."""
+    if not isinstance(e, Expr):
+        return e
+    if e.key in memo:
+        return memo[e.key]
+    if e.op == "x" and e.args[0] == BASE_ABS:
+        k = e.args[1] + n if e.args[1] < 0 else e.args[1]
+        r = Expr("x", (BASE_J, k - c))
+    elif e.op in ("x", "ldc", "ldi", "ldk", "ldki", "sum", "prod"):
+        r = e
+    else:
+        args = tuple(_rebase_abs(a, c, n, memo) for a in e.args)
+        r = CoefRef.__new__(CoefRef) if isinstance(e, CoefRef) else Expr.__new__(Expr)
+        Expr.__init__(r, e.op, args)
+    memo[e.key] = r
+    return r
+
+
 def auto_gradient(f: Expr, n: int) -> Gradient:
     """The gradient code list of a value expression, by symbolic differentiation.
 
@@ -521,6 +550,8 @@ def auto_gradient(f: Expr, n: int) -> Gradient:
         g = terms[0]
         for t in terms[1:]:
             g = Expr("add", (g, t))
+        if b - a == 1:
+            g = _rebase_abs(g, a, n, {})   # lets the section read its coordinates as X[j + o] (tabled)
         sections.append(Section(lambda j, g=g: g, a, b))
     return Gradient(sections)
 
@@ -590,6 +621,23 @@ class _Ctx:
     def new_val(self) -> int:
         self.nval += 1
         return self.nval - 1
+
+
+def _section_offsets(e, acc: set) -> bool:
+    """True when a gradient section reads coordinates only as X[j + o]
+    (collected in acc) and contains no reduction."""
+    if not isinstance(e, Expr):
+        return True
+    if e.op == "x":
+        if e.args[0] != BASE_J:
+            return False
+        acc.add(e.args[1])
+        return True
+    if e.op in ("ldk", "ldki"):
+        return e.args[0] != BASE_I
+    if e.op in ("sum", "prod"):
+        return False
+    return all(_section_offsets(a, acc) for a in e.args if isinstance(a, Expr))
 
 
 def _table_offsets(e, acc: set) -> bool:
@@ -871,9 +919,12 @@ def compile_objective(f: Expr, n: int, gradient: Gradient | str | None = None,
             sk = s.skip_infinite(_J) if s.skip_infinite is not None else None
             if sk is not None and not isinstance(sk, Expr):
                 raise CodeListError("skip_infinite must return an expression")
-            secs.append((lo, hi, s, e, sk))
+            offs: set = {s.check}
+            tabled = (tables and len(secs) < MAX_TABLED_SECTIONS and _section_offsets(e, offs)
+                      and (sk is None or _section_offsets(sk, offs)) and len(offs) <= MAX_SECTION_OFFSETS)
+            secs.append((lo, hi, s, e, sk, sorted(offs) if tabled else None))
         covered = np.zeros(n, dtype=int)
-        for lo, hi, _, _, _ in secs:
+        for lo, hi, _, _, _, _ in secs:
             covered[lo:hi] += 1
         if np.any(covered > 1):
             raise CodeListError("gradient sections overlap")
@@ -894,20 +945,23 @@ def compile_objective(f: Expr, n: int, gradient: Gradient | str | None = None,
                 if isinstance(a, Expr):
                     hoist(a)
 
-        for _, _, _, e, sk in secs:
+        for _, _, _, e, sk, toffs in secs:
+            if toffs is not None:
+                continue           # tabled sections are self-contained
             hoist(e)
             if sk is not None:
                 hoist(sk)
         pro_len = len(ctx.ins) - pro_start
-        for si, (lo, hi, s, e, sk) in enumerate(secs):
+        for si, (lo, hi, s, e, sk, toffs) in enumerate(secs):
             start = len(ctx.ins)
-            gem.section = si
-            gem.sec_range = (lo, hi)
-            saved = dict(gem.done)      # section-local values are not shared
-            r = gem.emit(e, None)
-            rs = gem.emit(sk, None) if sk is not None else None
-            gem.done = saved
-            sections.append([lo, hi, start, len(ctx.ins) - start, r, s.check, rs])
+            em_s = gem if toffs is None else _Emitter(ctx)   # tabled: nothing from the prologue
+            em_s.section = si
+            em_s.sec_range = (lo, hi)
+            saved = dict(em_s.done)      # section-local values are not shared
+            r = em_s.emit(e, None)
+            rs = em_s.emit(sk, None) if sk is not None else None
+            em_s.done = saved
+            sections.append([lo, hi, start, len(ctx.ins) - start, r, s.check, rs, toffs])
         # the sections run once per coordinate: prologue values stay live past
         # the last section instruction
         end = len(ctx.ins)
@@ -942,8 +996,10 @@ def compile_objective(f: Expr, n: int, gradient: Gradient | str | None = None,
 def _pack(n, nreg, ins, consts, res_reg, val_len, pro_start, pro_len, sections, skip, tabs) -> np.ndarray:
     words = [MAGIC, n, nreg, len(ins), len(consts), 0, val_len, pro_start, pro_len, len(sections), skip, res_reg,
              len(tabs), 0, 0, 0]
-    for lo, hi, start, ln, r, chk, rs in sections:
-        words += [lo, hi, start, ln, r, chk & 0xFFFFFFFF, rs, 0]
+    for lo, hi, start, ln, r, chk, rs, toffs in sections:
+        offs = (toffs or []) + [0, 0, 0]
+        words += [lo, hi, start, ln, r, chk & 0xFFFFFFFF, rs, 1 if toffs else 0, len(toffs or []),
+                  offs[0] & 0xFFFFFFFF, offs[1] & 0xFFFFFFFF, offs[2] & 0xFFFFFFFF]
     for lo, hi, kind, noff, o0, o1, _, start, ln, r in tabs:
         words += [lo, hi, kind, noff, o0 & 0xFFFFFFFF, o1 & 0xFFFFFFFF, 0, start, ln, r, 0, 0]
     for t in ins:
@@ -971,8 +1027,10 @@ def parse(coef: np.ndarray) -> dict:
         raise CodeListError("code list truncated")
     secs = []
     for k in range(nsec):
-        lo, hi, st, ln, r, chk, sk = (int(x) for x in w[HEADER + SEC_WORDS * k:HEADER + SEC_WORDS * k + 7])
-        secs.append(dict(lo=lo, hi=hi, start=st, len=ln, reg=r, check=s32(chk), skip_reg=sk))
+        lo, hi, st, ln, r, chk, sk, tb, no, o0, o1, o2 = (int(x) for x in w[HEADER + SEC_WORDS * k:
+                                                                           HEADER + SEC_WORDS * (k + 1)])
+        secs.append(dict(lo=lo, hi=hi, start=st, len=ln, reg=r, check=s32(chk), skip_reg=sk,
+                         tabled=[s32(o0), s32(o1), s32(o2)][:no] if tb else None))
     tabs = []
     for k in range(ntab):
         q = [int(x) for x in w[u0 + TAB_WORDS * k:u0 + TAB_WORDS * (k + 1)]]
@@ -1025,8 +1083,9 @@ def disassemble(coef: np.ndarray) -> str:
     out.append(f"value {vs}..{vs + vl - 1} (result r{p['result']}); gradient prologue {ps}..{ps + pl - 1}")
     for s in p["sections"]:
         sk = "" if s["skip_reg"] == NO_REG else f", no test when r{s['skip_reg']} has an infinite end"
+        tb = "" if s["tabled"] is None else f", tabled over X[j{s['tabled']}]"
         out.append(f"section j in {s['lo']}..{s['hi'] - 1}: code {s['start']}..{s['start'] + s['len'] - 1}, "
-                   f"gradient r{s['reg']}, KKT bounds of j{s['check']:+d}{sk}")
+                   f"gradient r{s['reg']}, KKT bounds of j{s['check']:+d}{sk}{tb}")
     if p["skip"] != NO_SKIP:
         out.append(f"skip the gradient test when every coordinate contains {float(p['consts'][p['skip']])!r}")
     for k, t in enumerate(p["tables"]):

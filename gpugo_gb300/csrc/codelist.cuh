@@ -24,11 +24,14 @@ enum {
   CL_LDX = 1, CL_LDC, CL_LDI, CL_LDK, CL_LDKI, CL_ADD, CL_MINUS, CL_MUL, CL_DIV, CL_TIMES, CL_PLUS,
   CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP, CL_TRED
 };
-enum { CL_HEADER = 16, CL_SEC = 8, CL_TAB = 12, CL_INS = 4, CL_MAXREG = 16, CL_MAXTAB = 8 };
+enum { CL_HEADER = 16, CL_SEC = 12, CL_TAB = 12, CL_INS = 4, CL_MAXREG = 16, CL_MAXTAB = 8 };
 enum { CLH_MAGIC, CLH_N, CLH_NREG, CLH_NINS, CLH_NCST, CLH_VS, CLH_VL, CLH_PS, CLH_PL, CLH_NSEC, CLH_SKIP, CLH_RES,
        CLH_NTAB };
 // term-table words
 enum { CLT_LO, CLT_HI, CLT_KIND, CLT_NOFF, CLT_OFF0, CLT_OFF1, CLT_PAD, CLT_START, CLT_LEN, CLT_REG };
+// gradient-section words
+enum { CLS_LO, CLS_HI, CLS_START, CLS_LEN, CLS_REG, CLS_CHK, CLS_SKIP, CLS_TABLED, CLS_NOFF, CLS_OFF0 };
+constexpr int CL_FLAG_TABLES = 8;   // Desc::cl_toff[8 + s]: KKT flags of tabled section s
 constexpr unsigned CL_NONE = 0xFFFFFFFFu;
 constexpr unsigned CL_MAGIC = 0x314C4347u;
 
@@ -152,9 +155,68 @@ __device__ __noinline__ void cl_exec(const Desc& D, const double* T, const XF& x
   }
 }
 
+// Coordinates j + o (o one of a tabled section's offsets) at the digits of one
+// flag-table entry, straight from the parent box.
+struct ClSecX {
+  const Desc* D;
+  const double* pbox;
+  const double* pw;
+  int c0, gsz, j, noff;
+  int off[3], dig[3];
+  __device__ __forceinline__ iv operator()(int k) const {
+    int d = dig[0];
+    for (int q = 1; q < noff; ++q)
+      if (k - j == off[q]) d = dig[q];
+    return child_iv(*D, pbox, pw, c0, gsz, k, d);
+  }
+};
+
+// Entry u of the iteration's KKT flag tables (tabled sections one after the
+// other): 1.0 when the section's test rules the box out, else 0.0.
+__device__ __noinline__ void cl_build_flag(const Desc& D, const double* pbox, const double* pw, int c0, int gsz,
+                                           long long u) {
+  const int w = D.wid;
+  const double* cf = D.coef;
+  const int nsec = (int)cl_word(cf, CLH_NSEC);
+  for (int s = 0; s < nsec && s < CL_FLAG_TABLES; ++s) {
+    const long long q = CL_HEADER + (long long)CL_SEC * s;
+    if (!cl_word(cf, q + CLS_TABLED)) continue;
+    const int lo = (int)cl_word(cf, q + CLS_LO), hi = (int)cl_word(cf, q + CLS_HI);
+    const int noff = (int)cl_word(cf, q + CLS_NOFF);
+    const int W = ipow(w, noff);
+    const long long cnt = (long long)(hi - lo) * W;
+    if (u >= cnt) { u -= cnt; continue; }
+    ClSecX xf;
+    xf.D = &D; xf.pbox = pbox; xf.pw = pw; xf.c0 = c0; xf.gsz = gsz; xf.noff = noff;
+    xf.j = lo + (int)(u / W);
+    int combo = (int)(u % W);
+    for (int k = noff - 1; k >= 0; --k) {
+      xf.off[k] = (int)cl_word(cf, q + CLS_OFF0 + k);
+      xf.dig[k] = combo % w;
+      combo /= w;
+      if (xf.dig[k] >= ndig(D, c0, gsz, xf.j + xf.off[k])) return;   // a digit this coordinate does not have
+    }
+    iv R[CL_MAXREG];
+    ChildCtx C0;
+    C0.c0 = c0;
+    C0.gsz = gsz;
+    cl_exec(D, D.tab, xf, (int)cl_word(cf, q + CLS_START), (int)cl_word(cf, q + CLS_LEN), xf.j, 0, R, C0, 0ULL, -1);
+    const unsigned rs = cl_word(cf, q + CLS_SKIP);
+    bool prune = true;
+    if (rs != CL_NONE) {
+      const iv t = R[rs];
+      if (feq(t.lo, -INF_D) || feq(t.hi, INF_D)) prune = false;   // corrupted50.py:418-421
+    }
+    const int k = xf.j + (int)cl_word(cf, q + CLS_CHK);
+    prune = prune && kkt_prune(R[cl_word(cf, q + CLS_REG)], xf(k), D.dom[2 * k], D.dom[2 * k + 1]);
+    D.tab[D.cl_toff[CL_FLAG_TABLES + s] + u] = prune ? 1.0 : 0.0;
+    return;
+  }
+}
+
 // Entry u of the iteration's term tables (all tables one after the other).
 __device__ __noinline__ void cl_build_term(const Desc& D, const double* pbox, const double* pw, int c0, int gsz,
-                                           long long u) {
+                                           long long u, long long* rest) {
   const int S = D.S, w = D.wid;
   const double* cf = D.coef;
   const int ntab = (int)cl_word(cf, CLH_NTAB);
@@ -181,8 +243,10 @@ __device__ __noinline__ void cl_build_term(const Desc& D, const double* pbox, co
     C0.gsz = gsz;
     cl_exec(D, D.tab, xf, (int)cl_word(cf, q + CLT_START), (int)cl_word(cf, q + CLT_LEN), 0, i, R, C0, 0ULL, js);
     stiv(D.tab + D.cl_toff[tt] + 2 * u, R[cl_word(cf, q + CLT_REG)]);
+    *rest = -1;
     return;
   }
+  *rest = u;   // past the term tables: an entry of the flag tables
 }
 
 // Table entries of one iteration: items [0, n w) are coordinate intervals,
@@ -210,7 +274,9 @@ __device__ __forceinline__ void cl_build_item(const Desc& D, const double* pbox,
     T[D.t_off[T_SHI] + u] = sample_pt(child_iv(D, pbox, pw, c0, gsz, i, d), S, js);
     return;
   }
-  cl_build_term(D, pbox, pw, c0, gsz, t - NW * (S + 1));
+  long long rest;
+  cl_build_term(D, pbox, pw, c0, gsz, t - NW * (S + 1), &rest);
+  if (rest >= 0) cl_build_flag(D, pbox, pw, c0, gsz, rest);
 }
 
 // interval of f over the child (js < 0) or at its sample point js
@@ -245,13 +311,25 @@ __device__ __noinline__ int cl_deriv(const Desc& D, const double* T, ChildCtx C,
   cl_exec(D, T, xf, (int)cl_word(cf, CLH_PS), (int)cl_word(cf, CLH_PL), 0, 0, R, C, pc, -1);
   for (int s = 0; s < nsec; ++s) {
     const long long q = CL_HEADER + (long long)CL_SEC * s;
-    const int lo = (int)cl_word(cf, q), hi = (int)cl_word(cf, q + 1);
-    const int st = (int)cl_word(cf, q + 2), ln = (int)cl_word(cf, q + 3);
-    const int rg = (int)cl_word(cf, q + 4), chk = (int)cl_word(cf, q + 5);
-    const unsigned rs = cl_word(cf, q + 6);
+    const int lo = (int)cl_word(cf, q + CLS_LO), hi = (int)cl_word(cf, q + CLS_HI);
+    const int st = (int)cl_word(cf, q + CLS_START), ln = (int)cl_word(cf, q + CLS_LEN);
+    const int rg = (int)cl_word(cf, q + CLS_REG), chk = (int)cl_word(cf, q + CLS_CHK);
+    const unsigned rs = cl_word(cf, q + CLS_SKIP);
     // first coordinate of this caller's stride in [lo, hi)
     int j = j0;
     if (j < lo) j += ((lo - j + jstep - 1) / jstep) * jstep;
+    if (cl_word(cf, q + CLS_TABLED)) {
+      // the flags of this section were computed for every digit combination
+      const int noff = (int)cl_word(cf, q + CLS_NOFF);
+      const int W = ipow(D.wid, noff);
+      const double* fl = T + D.cl_toff[CL_FLAG_TABLES + s];
+      for (; j < hi; j += jstep) {
+        int combo = 0;
+        for (int k = 0; k < noff; ++k) combo = combo * D.wid + digit(D, C.c0, C.gsz, pc, j + (int)cl_word(cf, q + CLS_OFF0 + k));
+        if (__double_as_longlong(fl[(long long)(j - lo) * W + combo]) != 0) return 1;   // 1.0, not 0.0
+      }
+      continue;
+    }
     for (; j < hi; j += jstep) {
       cl_exec(D, T, xf, st, ln, j, 0, R, C, pc, -1);
       if (rs != CL_NONE) {

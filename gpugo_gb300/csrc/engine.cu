@@ -1134,10 +1134,6 @@ __device__ void phase_seed(const KArgs& a) {
     State& st = a.st[s];
     const unsigned long long sk = st.seed_key;
     if (sk == ~0ULL) continue;
-    if constexpr (CL) {
-      // code lists have no seed pass: it only lowers the UB earlier in the iteration
-      if (D.family == FAM_CODELIST) continue;
-    }
     const unsigned long long code = sk & 0xffffffffULL;
     const double* T = (s == si) ? s_tab : D.tab;
     ChildCtx C;
@@ -1148,10 +1144,17 @@ __device__ void phase_seed(const KArgs& a) {
     const int sh = samp_shared(D, C);
     double bv = 0.0;
     int bj = J_NONE;
+    bool cl = false;
+    if constexpr (CL) cl = D.family == FAM_CODELIST;
     for (int j = lane; j < D.S; j += 32) {
-      SAcc r = (sh > 0) ? samp_prefix(D, T, C, j, D.tab + D.t_off[T_PFX]) : sacc_init(D);
-      samp_run<1>(D, T, C, pc, j, sh, samp_terms(D), &r);
-      double v = samp_value(D, r, cut);
+      double v;
+      if (cl) {
+        v = samp_one<CL>(D, T, C, pc, j);   // code lists: the value list at the sample point, no prefixes
+      } else {
+        SAcc r = (sh > 0) ? samp_prefix(D, T, C, j, D.tab + D.t_off[T_PFX]) : sacc_init(D);
+        samp_run<1>(D, T, C, pc, j, sh, samp_terms(D), &r);
+        v = samp_value(D, r, cut);
+      }
       if (samp_less(v, j, bv, bj)) { bv = v; bj = j; }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1901,9 +1904,11 @@ int ilog2_exact(int w) {
 // constants, registers), and that every register is written before it is read.
 // The device interpreter relies on this and checks nothing itself.
 // tb: the words of a term table when the code is its body (X read only as
-// X[i + o] for the table's offsets o; no loops, no reductions).
+// X[i + o] for the table's offsets o; no loops, no reductions); sec: the words
+// of a tabled gradient section (X read only as X[j + o] for its offsets).
 static int cl_check_code(const double* cf, int64_t I, int nins, int start, int len, int n, int64_t ncst, int nreg,
-                         int jlo, int jhi, bool allow_j, uint32_t* written, const uint32_t* tb, int ntab) {
+                         int jlo, int jhi, bool allow_j, uint32_t* written, const uint32_t* tb, int ntab,
+                         const uint32_t* sec = nullptr) {
   if (start < 0 || len < 0 || (int64_t)start + len > nins) return GPUGO_ERR_INVALID;
   auto word = [&](int64_t k) { uint64_t u; memcpy(&u, cf + k, 8); return (uint32_t)u; };
   bool in_loop = tb != nullptr;
@@ -1935,7 +1940,7 @@ static int cl_check_code(const double* cf, int64_t I, int nins, int start, int l
         reads = 1u << a;
         break;
       case CL_LOOP:
-        if (tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return GPUGO_ERR_INVALID;
+        if (sec || tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return GPUGO_ERR_INVALID;
         in_loop = true; lo = i1; hi = i2;
         continue;
       case CL_ENDLOOP:
@@ -1943,7 +1948,7 @@ static int cl_check_code(const double* cf, int64_t I, int nins, int start, int l
         in_loop = false;
         continue;
       case CL_TRED:
-        if (tb || i1 < 0 || i1 >= ntab || a >= nreg) return GPUGO_ERR_INVALID;
+        if (sec || tb || i1 < 0 || i1 >= ntab || a >= nreg) return GPUGO_ERR_INVALID;
         reads = 1u << a;
         break;
       default:
@@ -1953,6 +1958,11 @@ static int cl_check_code(const double* cf, int64_t I, int nins, int start, int l
       const uint32_t no = tb[CLT_NOFF];
       if (a != 1 || !((no > 0 && i1 == (int32_t)tb[CLT_OFF0]) || (no > 1 && i1 == (int32_t)tb[CLT_OFF1])))
         return GPUGO_ERR_INVALID;
+    }
+    if (sec && op == CL_LDX) {  // only X[j + o], o one of the section's offsets
+      bool hit = false;
+      for (uint32_t q = 0; q < sec[CLS_NOFF]; ++q) hit |= i1 == (int32_t)sec[CLS_OFF0 + q];
+      if (a != 2 || !hit) return GPUGO_ERR_INVALID;
     }
     if (d >= nreg || (reads & ~*written)) return GPUGO_ERR_INVALID;
     if (base >= 0) {
@@ -2023,16 +2033,33 @@ int validate_codelist(const gpugo_spec* s) {
   if (h[CLH_SKIP] != CL_NONE && h[CLH_SKIP] >= (uint32_t)ncst) return GPUGO_ERR_INVALID;
   int prev_hi = 0;
   for (uint32_t q = 0; q < h[CLH_NSEC]; ++q) {
-    uint32_t w[7];
-    for (int t = 0; t < 7; ++t) word(CL_HEADER + (int64_t)CL_SEC * q + t, &w[t]);
+    uint32_t w[CL_SEC];
+    for (int t = 0; t < CL_SEC; ++t) word(CL_HEADER + (int64_t)CL_SEC * q + t, &w[t]);
     const int lo = (int)w[0], hi = (int)w[1];
     const int32_t chk = (int32_t)w[5];
     if (lo < prev_hi || lo >= hi || hi > n) return GPUGO_ERR_INVALID;  // ascending, disjoint
     prev_hi = hi;
     if (w[4] >= (uint32_t)nreg || (w[6] != CL_NONE && w[6] >= (uint32_t)nreg)) return GPUGO_ERR_INVALID;
     if ((int64_t)lo + chk < 0 || (int64_t)hi - 1 + chk >= n) return GPUGO_ERR_INVALID;
-    uint32_t ws = wp;
-    if (cl_check_code(cf, I, nins, (int)w[2], (int)w[3], n, ncst, nreg, lo, hi, true, &ws, nullptr, ntab))
+    // a tabled section: its KKT flag per (j, digits of the coordinates j + o)
+    if (w[CLS_TABLED] > 1) return GPUGO_ERR_INVALID;
+    if (w[CLS_TABLED]) {
+      const uint32_t no = w[CLS_NOFF];
+      if (q >= (uint32_t)CL_FLAG_TABLES || no < 1 || no > 3) return GPUGO_ERR_INVALID;
+      bool has_chk = false;
+      double cells = 1.0;
+      for (uint32_t a = 0; a < no; ++a) {
+        const int64_t o = (int32_t)w[CLS_OFF0 + a];
+        if ((int64_t)lo + o < 0 || (int64_t)hi - 1 + o >= n) return GPUGO_ERR_INVALID;
+        for (uint32_t b = 0; b < a; ++b) if (w[CLS_OFF0 + b] == w[CLS_OFF0 + a]) return GPUGO_ERR_INVALID;
+        has_chk |= o == chk;
+        cells *= s->wid;
+      }
+      if (!has_chk || cells > 4096.0) return GPUGO_ERR_INVALID;
+    }
+    uint32_t ws = w[CLS_TABLED] ? 0u : wp;   // tabled sections read nothing from the prologue
+    if (cl_check_code(cf, I, nins, (int)w[2], (int)w[3], n, ncst, nreg, lo, hi, true, &ws, nullptr, ntab,
+                      w[CLS_TABLED] ? w : nullptr))
       return GPUGO_ERR_INVALID;
     if (!(ws & (1u << w[4])) || (w[6] != CL_NONE && !(ws & (1u << w[6])))) return GPUGO_ERR_INVALID;
   }
@@ -2071,7 +2098,7 @@ int validate(const gpugo_spec* s) {
 
 struct Layout {
   int64_t cst, tab, t_off[T_NOFF], a_items;
-  int64_t cl_toff[CL_MAXTAB];
+  int64_t cl_toff[2 * CL_FLAG_TABLES];
   int64_t pool_cap, parent_cap, tiles_cap, ubc_cap, out_cap, trace_cap;
   int64_t bytes;
   // byte offsets
@@ -2121,6 +2148,17 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
         const int64_t items = (S + 1) * (int64_t)(word(q + CLT_HI) - word(q + CLT_LO)) * cells;
         L->cl_toff[t] = o;
         o += 2 * items;
+        L->a_items += items;
+      }
+      // KKT flag tables of tabled sections: [hi - lo][w^offsets] doubles each
+      for (uint32_t q = 0; q < word(CLH_NSEC) && q < (uint32_t)CL_FLAG_TABLES; ++q) {
+        const int64_t b = CL_HEADER + (int64_t)CL_SEC * q;
+        if (!word(b + CLS_TABLED)) continue;
+        int64_t cells = 1;
+        for (uint32_t k = 0; k < word(b + CLS_NOFF); ++k) cells *= w;
+        const int64_t items = (int64_t)(word(b + CLS_HI) - word(b + CLS_LO)) * cells;
+        L->cl_toff[CL_FLAG_TABLES + q] = o;
+        o += items + (items & 1);
         L->a_items += items;
       }
       break;
@@ -2192,7 +2230,7 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->tiles_cap = L.tiles_cap; D->ubc_cap = L.ubc_cap; D->a_items = L.a_items;
   D->tab_doubles = L.tab;
   for (int i = 0; i < T_NOFF; ++i) D->t_off[i] = L.t_off[i];
-  for (int i = 0; i < CL_MAXTAB; ++i) D->cl_toff[i] = L.cl_toff[i];
+  for (int i = 0; i < 2 * CL_FLAG_TABLES; ++i) D->cl_toff[i] = L.cl_toff[i];
   D->dom = (const double*)(base + L.o_dom);
   D->coef = (const double*)(base + L.o_coef);
   D->cst = (double*)(base + L.o_cst);

@@ -71,7 +71,7 @@ struct Desc {
   long long* tr_sel;
   // code lists: offsets of the term tables (doubles); last, so that the fields
   // every iteration reads keep their cache lines
-  long long cl_toff[8];
+  long long cl_toff[16];   // [0, 8) term tables, [8, 16) KKT flags of tabled sections
 };
 
 // ---------------------------------------------------------------------------

@@ -669,7 +669,7 @@ enum {
     CL_LDX = 1, CL_LDC, CL_LDI, CL_LDK, CL_LDKI, CL_ADD, CL_MINUS, CL_MUL, CL_DIV, CL_TIMES, CL_PLUS,
     CL_TIMESK, CL_PLUSK, CL_SQR, CL_SQRT, CL_EXP, CL_SIN, CL_COS, CL_MOV, CL_LOOP, CL_ENDLOOP, CL_TRED
 };
-enum { CL_MAGIC = 0x314C4347u, CL_HEADER = 16, CL_SEC = 8, CL_TAB = 12, CL_INS = 4, CL_MAXREG = 16, CL_MAXTAB = 8 };
+enum { CL_MAGIC = 0x314C4347u, CL_HEADER = 16, CL_SEC = 12, CL_TAB = 12, CL_INS = 4, CL_MAXREG = 16, CL_MAXTAB = 8 };
 #define CL_NONE 0xFFFFFFFFu
 
 /* header words */
@@ -691,8 +691,11 @@ static inline long cl_idx(int base, int32_t off, long i, long j)
  * tb (a table body, or NULL): X is read only as X[i + o] for the table's
  * offsets o, i in [lo, hi); no loops and no nested reductions. */
 static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int n, int ncst, int nreg,
-                          int jlo, int jhi, int allow_j, uint32_t* written, const uint32_t* tb, int ntab)
+                          int jlo, int jhi, int allow_j, uint32_t* written, const uint32_t* tb, int ntab,
+                          const uint32_t* sec)
 {
+    /* sec (a tabled gradient section's words, or NULL): X read only as X[j + o]
+     * for the section's offsets o; no loops, no reductions */
     long lo = 0, hi = 0;
     int in_loop = 0;
     if (tb) { in_loop = 1; lo = tb[T_LO_]; hi = tb[T_HI_]; }
@@ -725,7 +728,7 @@ static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int
             reads = 1u << a;
             break;
         case CL_LOOP:
-            if (tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return -2;
+            if (sec || tb || in_loop || i1 < 0 || i1 >= i2 || i2 > n) return -2;
             in_loop = 1; lo = i1; hi = i2;
             continue;
         case CL_ENDLOOP:
@@ -733,7 +736,7 @@ static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int
             in_loop = 0;
             continue;
         case CL_TRED:
-            if (tb || i1 < 0 || i1 >= ntab || a >= nreg) return -2;
+            if (sec || tb || i1 < 0 || i1 >= ntab || a >= nreg) return -2;
             reads = 1u << a;
             break;
         default:
@@ -742,6 +745,11 @@ static int cl_check_range(const uint32_t* ins, int nins, int start, int len, int
         if (tb && op == CL_LDX) {   /* only X[i + o], o one of the table's offsets */
             uint32_t no = tb[T_NOFF];
             if (a != 1 || !((no > 0 && i1 == (int32_t)tb[T_OFF0]) || (no > 1 && i1 == (int32_t)tb[T_OFF1]))) return -2;
+        }
+        if (sec && op == CL_LDX) {  /* only X[j + o], o one of the section's offsets */
+            int hit = 0;
+            for (uint32_t q = 0; q < sec[8]; ++q) hit |= i1 == (int32_t)sec[9 + q];
+            if (a != 2 || !hit) return -2;
         }
         if (d >= nreg || (reads & ~*written)) return -2;   /* a register is written before it is read */
         if (base >= 0) {
@@ -798,14 +806,14 @@ static int cl_parse(const oc_spec* sp, consts* c)
         if (no == 2 && tb[T_OFF0] == tb[T_OFF1]) return -2;
         uint32_t wt = 0;
         if (tb[T_REG] >= (uint32_t)nreg) return -2;
-        if (cl_check_range(ins, nins, (int)tb[T_START], (int)tb[T_LEN], n, ncst, nreg, 0, 0, 0, &wt, tb, ntab)) return -2;
+        if (cl_check_range(ins, nins, (int)tb[T_START], (int)tb[T_LEN], n, ncst, nreg, 0, 0, 0, &wt, tb, ntab, NULL)) return -2;
         if (!(wt & (1u << tb[T_REG]))) return -2;
     }
     uint32_t wv = 0, wp = 0;
     if (h[H_VL] < 1 || h[H_RES] >= (uint32_t)nreg) return -2;
-    if (cl_check_range(ins, nins, (int)h[H_VS], (int)h[H_VL], n, ncst, nreg, 0, 0, 0, &wv, NULL, ntab)) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_VS], (int)h[H_VL], n, ncst, nreg, 0, 0, 0, &wv, NULL, ntab, NULL)) return -2;
     if (!(wv & (1u << h[H_RES]))) return -2;
-    if (cl_check_range(ins, nins, (int)h[H_PS], (int)h[H_PL], n, ncst, nreg, 0, 0, 0, &wp, NULL, ntab)) return -2;
+    if (cl_check_range(ins, nins, (int)h[H_PS], (int)h[H_PL], n, ncst, nreg, 0, 0, 0, &wp, NULL, ntab, NULL)) return -2;
     if (h[H_SKIP] != CL_NONE && h[H_SKIP] >= (uint32_t)ncst) return -2;
     int prev_hi = 0;
     for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
@@ -817,8 +825,21 @@ static int cl_parse(const oc_spec* sp, consts* c)
         prev_hi = hi;
         if (r >= nreg || (rs != CL_NONE && rs >= (uint32_t)nreg)) return -2;
         if ((long)lo + chk < 0 || (long)hi - 1 + chk >= n) return -2;
-        uint32_t ws = wp;
-        if (cl_check_range(ins, nins, st, ln, n, ncst, nreg, lo, hi, 1, &ws, NULL, ntab)) return -2;
+        /* a tabled section: its flag per (j, digits of X[j + o]) is what its code gives */
+        if (q[7] > 1) return -2;
+        if (q[7]) {
+            if (s >= 8 || q[8] < 1 || q[8] > 3) return -2;
+            int has_chk = 0;
+            for (uint32_t a = 0; a < q[8]; ++a) {
+                const long o = (int32_t)q[9 + a];
+                if ((long)lo + o < 0 || (long)hi - 1 + o >= n) return -2;
+                for (uint32_t b = 0; b < a; ++b) if (q[9 + b] == q[9 + a]) return -2;
+                has_chk |= o == chk;
+            }
+            if (!has_chk || pow((double)sp->wid, (double)q[8]) > 4096.0) return -2;
+        }
+        uint32_t ws = q[7] ? 0u : wp;   /* tabled sections read nothing from the prologue */
+        if (cl_check_range(ins, nins, st, ln, n, ncst, nreg, lo, hi, 1, &ws, NULL, ntab, q[7] ? q : NULL)) return -2;
         if (!(ws & (1u << r)) || (rs != CL_NONE && !(ws & (1u << rs)))) return -2;
     }
     return 0;

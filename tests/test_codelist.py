@@ -237,6 +237,18 @@ def _mutations(coef, tag):
     if p["sections"]:
         put("section range", CL.HEADER + 1, p["n"] + 1)
         put("check offset", CL.HEADER + 5, (-1) & 0xFFFFFFFF)
+    tabled = [k for k, sec in enumerate(p["sections"]) if sec["tabled"]]
+    if tabled:
+        q = CL.HEADER + CL.SEC_WORDS * tabled[-1]
+        put("tabled flag", q + 7, 2)
+        put("tabled offset count", q + 8, 4)
+        put("tabled offsets repeat", q + 10, int(w[q + 9]))
+        put("tabled offsets miss the check", q + 9, 5)
+        # a tabled section may not read the prologue: point its first read at a register it never writes
+        sec = p["sections"][tabled[-1]]
+        k = next(t for t in range(sec["start"], sec["start"] + sec["len"]) if ins[t][0] in (CL.TIMES, CL.PLUS, CL.SQR, CL.SIN))
+        op, d, a, b, _, _ = ins[k]
+        put("tabled section reads outside itself", I + CL.INS_WORDS * k, op | (d << 8) | (15 << 16) | (b << 24))
     return out
 
 
@@ -263,6 +275,7 @@ def test_oracle_and_library_reject_malformed_code_lists(oracle_lib):
         assert lib_accepts(p)
     bads = {**_mutations(good, "tables"), **_mutations(loops, "loops")}
     assert any("table body" in k for k in bads) and any("nested loop" in k for k in bads)
+    assert any("tabled section" in k for k in bads)
     for name, bad in bads.items():
         q = P.Problem(P.CODELIST, 6, p.domain, bad, wid=2, group=2)
         with pytest.raises(ValueError):
