@@ -13,7 +13,6 @@ reference's other benchmarks are in :mod:`gpugo_gb300.objectives`.
 from __future__ import annotations
 
 import ctypes
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

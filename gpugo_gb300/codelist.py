@@ -228,10 +228,6 @@ def _bits(v: float) -> int:
     return struct.unpack("<Q", struct.pack("<d", v))[0]
 
 
-def _unbits(b: int) -> float:
-    return struct.unpack("<d", struct.pack("<Q", b))[0]
-
-
 class _XIndexer:
     def __getitem__(self, k) -> Expr:
         base, off = _index(k)
