@@ -21,6 +21,7 @@
 // Every device-side wait is bounded by a %globaltimer budget.
 #include <cuda_runtime.h>
 #include <cooperative_groups.h>
+#include <nvtx3/nvToolsExt.h>   // header-only: ranges are free unless a profiler is attached
 
 #include <algorithm>
 #include <climits>
@@ -38,6 +39,15 @@
 #include "ia.cuh"
 #include "families.cuh"
 #include "../../include/gpugo.h"
+
+// Named ranges around the host entry points (admission, runs, result collection,
+// whole solves) for nsys / ncu --nvtx.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 namespace gg {
 
@@ -2431,6 +2441,7 @@ int gpugo_device_info(int32_t* sm_out, int32_t* num_sms_out) {
 
 int gpugo_combine(const double* boxes, int64_t nbox, int32_t n, double tol, double* roots_out, int64_t cap,
                   int64_t* nroots_out) {
+  NvtxRange nvtx_range("gpugo_combine");
   if (nbox < 0 || n < 1 || cap < 0 || !nroots_out || (nbox > 0 && !boxes) || (cap > 0 && !roots_out) ||
       !(tol >= 0.0))
     return GPUGO_ERR_INVALID;
@@ -2689,6 +2700,7 @@ extern "C" {
 
 int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* box_lb_out, int64_t cap,
                  double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+  NvtxRange nvtx_range("gpugo_submit");
   return admit(E, spec, boxes_out, box_lb_out, cap, xhat_out, trace, nullptr, {}, ticket_out);
 }
 
@@ -2711,6 +2723,7 @@ size_t pad8(size_t b) { return (b + 7) & ~size_t(7); }
 extern "C" {
 
 int gpugo_checkpoint(gpugo_engine* E, int64_t ticket, void* buf, int64_t cap, int64_t* bytes_out) {
+  NvtxRange nvtx_range("gpugo_checkpoint");
   if (!E || !bytes_out) return GPUGO_ERR_INVALID;
   int slot = -1;
   for (int s = 0; s < E->max_slots; ++s)
@@ -2773,6 +2786,7 @@ int gpugo_checkpoint(gpugo_engine* E, int64_t ticket, void* buf, int64_t cap, in
 
 int gpugo_restore(gpugo_engine* E, const void* buf, int64_t bytes, double* boxes_out, double* box_lb_out,
                   int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
+  NvtxRange nvtx_range("gpugo_restore");
   if (!E || !buf || bytes < (int64_t)sizeof(CkptHeader)) return GPUGO_ERR_INVALID;
   CkptHeader hd;
   memcpy(&hd, buf, sizeof(hd));
@@ -2824,6 +2838,7 @@ int gpugo_restore(gpugo_engine* E, const void* buf, int64_t bytes, double* boxes
 }
 
 int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
+  NvtxRange nvtx_range("gpugo_run");
   if (!E) return GPUGO_ERR_INVALID;
   cudaStream_t st = E->stream;
   if (!E->pending_init.empty()) {
@@ -2923,6 +2938,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
 }
 
 int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_done_out) {
+  NvtxRange nvtx_range("gpugo_poll");
   if (!E) return GPUGO_ERR_INVALID;
   std::vector<int> fin;
   for (int s = 0; s < E->max_slots && (int)fin.size() < max_done; ++s)
@@ -3122,6 +3138,7 @@ static int64_t g_single_bytes = 0;
 
 int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, double* box_lb_out, int64_t cap,
                 double* xhat_out, gpugo_trace* trace) {
+  NvtxRange nvtx_range("gpugo_solve");
   if (!res) return GPUGO_ERR_INVALID;
   int rc = validate(spec);
   if (rc) return rc;
@@ -3172,6 +3189,7 @@ int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, do
 
 int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes,
                         int64_t m, double ub, double* lb_out, double* samp_out, int32_t* flag_out) {
+  NvtxRange nvtx_range("gpugo_eval_children");
   int rc = validate(spec);
   if (rc) return rc;
   if (!parent_box || (!codes && m > 0) || m < 0 || cyc < 1 || cyc > spec->n) return GPUGO_ERR_INVALID;
