@@ -2079,7 +2079,7 @@ int validate_codelist(const gpugo_spec* s) {
 int validate(const gpugo_spec* s) {
   if (!s || !s->domain || !s->coef) return GPUGO_ERR_INVALID;
   if (s->family < 1 || s->family > 5) return GPUGO_ERR_INVALID;
-  if (s->n < 1 || s->n > 4096) return GPUGO_ERR_INVALID;
+  if (s->n < 1 || s->n > 16384) return GPUGO_ERR_INVALID;   // the reference goes up to 10 000 (levy10000.py)
   if (s->family == GPUGO_CHAINED && s->n < 2) return GPUGO_ERR_INVALID;
   if (s->wid < 2 || s->group < 1 || s->samples < 1 || s->samples > 255) return GPUGO_ERR_INVALID;
   if (s->stop_mode != GPUGO_STOP_WIDTH && s->stop_mode != GPUGO_STOP_GAP) return GPUGO_ERR_INVALID;

@@ -66,7 +66,7 @@ extern "C" {
 /* One problem: the constants of a reference script made explicit. */
 typedef struct gpugo_spec {
     int32_t family;        /* GPUGO_COSQUAD .. GPUGO_CODELIST */
-    int32_t n;             /* variables (reference: 50..10000, hard-coded per script) */
+    int32_t n;             /* variables, 1..16384 (reference: 50..10000, hard-coded per script) */
     int32_t wid;           /* parts per split coordinate (reference wid = 4, ackley50.py:527) */
     int32_t group;         /* coordinates split per iteration (reference cycleSize = 10, :530) */
     int32_t samples;       /* sample points per child (reference numSamples = 10, :1015) */

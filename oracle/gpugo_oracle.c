@@ -1094,7 +1094,7 @@ static void eval_child(const oc_spec* sp, const consts* c, const child_t* ch, iv
 
 static int validate(const oc_spec* sp)
 {
-    if (sp->n < 1 || sp->n > 4096) return -2;
+    if (sp->n < 1 || sp->n > 16384) return -2;
     if (sp->wid < 2 || sp->group < 1 || sp->samples < 1) return -2;
     if (!sp->domain) return -2;
     int g = sp->group < sp->n ? sp->group : sp->n;

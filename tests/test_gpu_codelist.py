@@ -164,3 +164,23 @@ def test_malformed_code_list_is_rejected():
     p = P.Problem(P.CODELIST, 5, np.tile(dom, 5), coef, wid=3, group=5)
     with pytest.raises(G.GpugoError):
         G.solve(p)
+
+
+def test_levy10000_reference_size(oracle_lib):
+    """The reference's largest script (levy10000.py: 10 000 variables, wid 4,
+    cycles of 10): children against the oracle at the first and the last cycle,
+    then two iterations of the loop (4^10 children each)."""
+    n = 10000
+    f, g, dom = O.levy(n)
+    p = P.Problem(P.CODELIST, n, np.tile(dom, n), CL.compile_objective(f, n, g).coef, wid=4, group=10,
+                  samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1000.0)
+    rng = np.random.default_rng(10)
+    for cyc in (1, n - 9):
+        codes = np.concatenate([rng.integers(0, 4 ** 10, 300), [0, 4 ** 10 - 1]]).astype(np.uint64)
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, p.domain, cyc, codes, 1e300)
+        lb_g, s_g, f_g = G.eval_children(p, p.domain, cyc, codes, 1e300)
+        assert _same(lb_g, lb_o) and _same(s_g, s_o) and np.array_equal(f_g, f_o)
+    p.max_iter = 2
+    r = G.solve(p, box_cap=4)
+    assert r.status == G.ITER_LIMIT and r.boxes_bounded == 2 * 4 ** 10 and r.lb <= r.ub
+    print(f"\nlevy10000: 2 iterations in {r.device_ms:.1f} ms, enclosure [{r.lb:.6g}, {r.ub:.6g}]")
