@@ -599,7 +599,10 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
       iv x = child_iv(D, pb, pw, ccyc - 1, gsz, i, digit(D, ccyc - 1, gsz, pc, i));
       nb[2 * i] = x.lo;
       nb[2 * i + 1] = x.hi;
-      nw[i] = part_width(D, x.lo, x.hi);
+      // a coordinate outside the split group keeps the parent's interval, so its
+      // part width is the parent's (same operation on the same operands)
+      const int k = i - (ccyc - 1);
+      nw[i] = (k >= 0 && k < gsz) ? part_width(D, x.lo, x.hi) : pw[i];
     }
   }
   __syncwarp();
