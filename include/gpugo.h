@@ -53,11 +53,17 @@ extern "C" {
  *   [0] 0x314C4347 [1] n [2] registers (<= 16) [3] instructions [4] constants
  *   [5] value start [6] value length [7] gradient prologue start [8] length
  *   [9] sections [10] skip constant (0xFFFFFFFF none) [11] value result register
- *   [12 + 8s] section: lo, hi, start, length, gradient register, check offset, skip register, 0
- *   [I + 4t]  instruction: op | dst << 8 | a << 16 | b << 24, imm1, imm2, 0   (I = 12 + 8 sections)
+ *   [12] term tables (<= 8) [13..15] 0
+ *   [16 + 12s] section: lo, hi, start, length, gradient register, check offset,
+ *              skip register, tabled, offsets, offset 0..2
+ *   [U + 12t]  term table: lo, hi, kind, offsets, offset 0, offset 1, 0, body start,
+ *              body length, body result register, 0, 0            (U = 16 + 12 sections)
+ *   [I + 4t]   instruction: op | dst << 8 | a << 16 | b << 24, imm1, imm2, 0
+ *                                                                  (I = U + 12 tables)
  *   [I + 4 instructions ...] constants (doubles)
  * The library checks every index an instruction can form against n, the
- * constants and the registers before it accepts the problem (GPUGO_ERR_INVALID). */
+ * constants and the registers, and that registers are written before they are
+ * read, before it accepts the problem (GPUGO_ERR_INVALID). */
 #define GPUGO_CODELIST 5
 
 #define GPUGO_STOP_WIDTH 0   /* reference rule: emit a box when width(x_1) < width_tol at the last cycle (ackley50.py:1306-1343) */
