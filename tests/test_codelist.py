@@ -402,3 +402,47 @@ def test_auto_gradient_rejects_unsupported_bodies():
         CL.compile_objective(CL.Sum(lambda i: X[i] * X[0]), 4, "auto")     # a fixed coordinate in a body
     with pytest.raises(CL.CodeListError):
         CL.compile_objective(X[0], 4, "derive")
+
+
+def _solve_codelist(oracle_lib, f, n, grad, lo, hi, split):
+    p = P.Problem(P.CODELIST, n, np.tile([lo, hi], n), CL.compile_objective(f, n, grad).coef, wid=split[0],
+                  group=split[1])
+    p.max_iter = 5000
+    return oracle_lib.solve(p, box_cap=8)
+
+
+def test_front_end_shapes(oracle_lib):
+    """Objectives outside the reference's shapes: fixed coordinates only, a
+    reduction whose start value reads a coordinate, a reduction used inside
+    another's body (evaluated once, before the loop), a product; each with
+    written and derived gradients; minima known in closed form."""
+    X, Sum, Prod, sqr, cos = CL.X, CL.Sum, CL.Prod, CL.sqr, CL.cos
+    cases = [
+        # (f, n, written gradient or None, minimum, domain)
+        (sqr(X[0] + (-1.0)) + sqr(X[1]) * 3.0, 2,
+         CL.Gradient([CL.Section(lambda j: (X[j] + (-1.0)) * 2.0, 0, 1), CL.Section(lambda j: X[j] * 6.0, 1, 2)]),
+         0.0, (-4.0, 5.0)),
+        (Sum(lambda i: sqr(X[i]), lo=1, init=sqr(X[0]) * 2.0), 4, None, 0.0, (-3.0, 2.0)),
+        (Sum(lambda i: sqr(X[i]) * Sum(lambda k: 1.0 + sqr(X[k]) * 0.0)), 3, None, 0.0, (-2.0, 3.0)),
+        (Prod(lambda i: sqr(X[i]) + 1.0) + (-1.0), 3, None, 0.0, (-2.0, 1.5)),
+        (Sum(lambda i: sqr(X[i]) - cos(X[i] * 3.0) * 2.0), 5, None, -10.0, (-4.0, 5.0)),
+    ]
+    for k, (f, n, g, fmin, (lo, hi)) in enumerate(cases):
+        split = P.default_split(n)
+        grads = ([g] if g is not None else []) + [None]
+        if k == 2:
+            # a reduction inside a body: the derived gradient does not cover it
+            with pytest.raises(CL.CodeListError):
+                CL.compile_objective(f, n, "auto")
+        else:
+            grads.append("auto")
+        for grad in grads:
+            r = _solve_codelist(oracle_lib, f, n, grad, lo, hi, split)
+            assert r.ub - r.lb <= 1e-6 and r.lb <= fmin + 1e-12 and fmin - 1e-6 <= r.ub, (k, grad)
+
+
+def test_auto_gradient_of_fixed_coordinates_is_tabled():
+    X, sqr = CL.X, CL.sqr
+    c = CL.compile_objective(sqr(X[0] + (-1.0)) + sqr(X[1]) * 3.0, 2, "auto")
+    secs = CL.parse(c.coef)["sections"]
+    assert len(secs) == 2 and all(s["tabled"] is not None for s in secs)
