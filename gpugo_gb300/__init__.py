@@ -65,6 +65,19 @@ class SolveResult:
     def gap(self) -> float:
         return self.ub - self.lb
 
+    def record(self, tag: str = "") -> dict:
+        """One structured log record of the solve (what the reference prints per
+        script: enclosure, iterations, time; plus the work counts), JSON-ready;
+        the survivors per iteration come from the trace when one was kept."""
+        out = {"tag": tag, "lb": self.lb, "ub": self.ub, "gap": self.gap, "status": self.status,
+               "certified": self.certified, "iterations": self.iterations, "boxes_bounded": self.boxes_bounded,
+               "samples_evaluated": self.samples_evaluated, "pool_size": self.pool_size, "n_boxes": self.n_boxes,
+               "device_ms": self.device_ms}
+        if self.trace:
+            out["survivors"] = [int(v) for v in self.trace["n_surv"]]
+            out["list_sizes"] = [int(v) for v in self.trace["pool"]]
+        return out
+
 
 def _alloc_out(p: Problem, cap: int, trace_cap: int):
     boxes = np.zeros((max(cap, 1), 2 * p.n))

@@ -55,3 +55,14 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(ImportError):
         _lib.load()
+
+
+def test_solve_record_is_json_ready():
+    import json
+    import numpy as np
+    import gpugo_gb300 as G
+    r = G.SolveResult(lb=-1.0, ub=-0.5, status=G.CERTIFIED, iterations=3, boxes_bounded=30, samples_evaluated=12,
+                      pool_size=2, n_boxes=2, boxes=np.zeros((2, 1, 2)), box_lbs=np.zeros(2), xhat=None,
+                      device_ms=0.25, trace={"n_surv": np.array([4, 2, 1]), "pool": np.array([4, 5, 2])})
+    rec = json.loads(json.dumps(r.record("t")))
+    assert rec["gap"] == 0.5 and rec["certified"] and rec["survivors"] == [4, 2, 1] and rec["list_sizes"] == [4, 5, 2]
