@@ -50,9 +50,12 @@ def test_static_matches_allocating_entry_point(lib):
     g = np.load(GOLD)
     ref = P.Problem(1, 50, g["rastrigin_domain"], g["rastrigin_coef"], wid=4, group=10, samples=10,
                     stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6)
+    from gpugo_gb300 import objectives as O
+    levy = O.problem("levy", 12, split=(4, 6))      # a code list: term and flag tables in the scratch
     cases = [
         (P.config2(), P.config2().domain, 1, rng.integers(0, 4 ** 8, 5000)),
         (ref, g["rastrigin_parents"][1], 11, rng.integers(0, 4 ** 10, 5000)),
+        (levy, levy.domain, 7, rng.integers(0, 4 ** 6, 3000)),
     ]
     for p, pbox, cyc, codes in cases:  # two calls in a row on the shared scratch
         rc0, lb0, s0, f0 = _call(lib, "gpugo_eval_children", p, pbox, cyc, codes, 1e300)
