@@ -296,7 +296,7 @@ def run_batched(args):
         # block size, candidates per warp and fan-out picked on a sample of the batch;
         # the plain loop then solves the same (re-split) problems
         t0 = time.perf_counter()
-        tuned = A.tune(probs, sample=min(128, args.count))
+        tuned = A.tune(probs, sample=min(512, args.count))
         tune_s = time.perf_counter() - t0
         probs = tuned.apply(probs)
         ecfg = tuned.engine

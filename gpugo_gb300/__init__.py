@@ -269,20 +269,26 @@ class Engine:
         _lib.check(self._L.gpugo_engine_free_bytes(self._h, ctypes.byref(out)), "gpugo_engine_free_bytes")
         return out.value
 
-    def solve_all(self, problems: list[Problem], iters_per_run: int = 0, box_cap: int = 16):
-        """Admit as many problems as fit, run, collect, refill; returns results in input order."""
+    def solve_all(self, problems: list[Problem], iters_per_run: int = 0, box_cap: int = 16,
+                  group_by_shape: bool = True):
+        """Admit as many problems as fit, run, collect, refill; returns results in input order.
+        ``group_by_shape`` admits them ordered by (family, n): slots, and so the
+        kernel's work lists, then hold neighbours of equal cost side by side."""
         results: list[SolveResult | None] = [None] * len(problems)
         tickets: dict[int, int] = {}
+        order = list(range(len(problems)))
+        if group_by_shape:
+            order.sort(key=lambda k: (problems[k].family, problems[k].n))
         nxt = 0
         while nxt < len(problems) or tickets:
             while nxt < len(problems):
-                t = self.submit(problems[nxt], box_cap=box_cap)
+                t = self.submit(problems[order[nxt]], box_cap=box_cap)
                 if t is None:
                     break
-                tickets[t] = nxt
+                tickets[t] = order[nxt]
                 nxt += 1
             if not tickets:
-                raise GpugoError(-7, f"problem {nxt} does not fit an empty engine")
+                raise GpugoError(-7, f"problem {order[nxt]} does not fit an empty engine")
             self.run(iters_per_run)
             for t, r in self.poll():
                 results[tickets.pop(t)] = r

@@ -102,7 +102,7 @@ def sample_problems(problems: Sequence[Problem], k: int) -> list[Problem]:
     return [problems[int(i * step)] for i in range(k)]
 
 
-def tune(problems: Sequence[Problem], sample: int = 128, configs: Sequence[EngineConfig] = ENGINE_CONFIGS,
+def tune(problems: Sequence[Problem], sample: int = 512, configs: Sequence[EngineConfig] = ENGINE_CONFIGS,
          fanout_options: Sequence[tuple[int, int]] = FANOUT_OPTIONS,
          n_classes: Sequence[tuple[int, int]] = N_CLASSES, per_class: int = 16,
          timer: Callable[[Sequence[Problem], EngineConfig], float] = time_engine) -> TuneResult:
