@@ -67,3 +67,22 @@ def test_admission_respects_slots_and_arrival_order():
         assert r.admitted >= r.arrival and r.finished > r.admitted
         assert r.result.tag == f"q{r.index}"
     assert rep.p99_ms >= rep.p50_ms > 0
+
+
+def test_solve_all_admits_by_shape_and_returns_input_order():
+    """Engine.solve_all (host logic, run on a fake engine): admission ordered by
+    (family, n), refills as slots free up, results in the caller's order."""
+    import gpugo_gb300 as G
+    probs = P.config4(count=40, seed=5, nmax=30)
+    for i, p in enumerate(probs):
+        p.tag = f"p{i}"
+    fake = FakeEngine(slots=7, iters=3)
+    res = G.Engine.solve_all(fake, probs, iters_per_run=1)
+    assert [r.tag for r in res] == [p.tag for p in probs]
+    shapes = [(p.family, p.n) for p in sorted(probs, key=lambda q: (q.family, q.n))]
+    by_tag = {p.tag: (p.family, p.n) for p in probs}
+    assert [by_tag[t] for t in fake.admit_order] == shapes
+    assert fake.max_resident == 7
+    fake2 = FakeEngine(slots=7, iters=3)
+    G.Engine.solve_all(fake2, probs, iters_per_run=1, group_by_shape=False)
+    assert fake2.admit_order == [p.tag for p in probs]
