@@ -465,6 +465,8 @@ def _shift(e, o: int, memo: dict):
     elif e.op in ("ldk", "ldki"):
         base, off, arr = e.args
         r = arr[Index(BASE_J, off - o)] if base == BASE_I else e
+    elif e.op in ("sum", "prod"):
+        r = e   # an inner reduction binds its own loop index
     else:
         args = tuple(_shift(a, o, memo) for a in e.args)
         r = CoefRef.__new__(CoefRef) if isinstance(e, CoefRef) else Expr.__new__(Expr)
@@ -492,6 +494,33 @@ def _rebase_abs(e, c: int, n: int, memo: dict):
     return r
 
 
+def _body_leaves(e, out: dict):
+    """Fixed coordinates and (loop-invariant) reductions inside a reduction's body."""
+    if not isinstance(e, Expr):
+        return
+    if e.op in ("sum", "prod") or (e.op == "x" and e.args[0] == BASE_ABS):
+        out[e.key] = e
+        return
+    for a in e.args:
+        if isinstance(a, Expr):
+            _body_leaves(a, out)
+
+
+def _xi_offsets(e, acc: set):
+    """Offsets o of the X[i + o] a body reads (outside its inner reductions)."""
+    if not isinstance(e, Expr) or e.op in ("sum", "prod"):
+        return
+    if e.op == "x":
+        if e.args[0] == BASE_I:
+            acc.add(e.args[1])
+        elif e.args[0] == BASE_J:
+            raise CodeListError("the value expression reads the gradient coordinate j")
+        return
+    for a in e.args:
+        if isinstance(a, Expr):
+            _xi_offsets(a, acc)
+
+
 def auto_gradient(f: Expr, n: int) -> Gradient:
     """The gradient code list of a value expression, by symbolic differentiation.
 
@@ -499,33 +528,54 @@ def auto_gradient(f: Expr, n: int) -> Gradient:
     fixed coordinate X[k], d f / d X[k] when j = k.  For R = Sum_i t(i):
     d R / d x_j = sum over the offsets o of t of (d t / d X[i+o]) at i = j - o,
     for j - o in R's range; for a product, (R / t(j - o)) (d t / d X[i+o]).
-    The coordinates where the set of terms changes split [0, n) into sections.
-    Every rule is exact, so the interval evaluation encloses the gradient; a
-    division by an interval containing zero (a product's term, a square root at
-    zero) gives an unbounded gradient and the test keeps the box."""
+    A fixed coordinate or another reduction L inside t is reached through R with
+    d R / d L = Sum_i d t(i) / d L (for a product Sum_i (R / t(i)) d t(i) / d L),
+    a reduction over R's range evaluated once per box; such leaves go through a
+    worklist with their accumulated adjoints.  The coordinates where the set of
+    terms changes split [0, n) into sections.  Every rule is exact, so the
+    interval evaluation encloses the gradient; a division by an interval
+    containing zero (a product's term, a square root at zero) gives an unbounded
+    gradient and the test keeps the box."""
     global _ONE
     if _ONE is None:
         _ONE = Const(1.0)
     leaves: dict = {}
     _leaves(f, leaves)
-    adj = {k: _diff(f, k, {}) for k in leaves}
-    # contributions: (j range, expression builder)
+    # worklist of (leaf, adjoint); the adjoints of a leaf reached along several
+    # paths add up (every path's term is kept: the sum of the exact terms)
+    work = [(L, _diff(f, k, {})) for k, L in leaves.items()]
     parts = []
-    for k, L in leaves.items():
-        if adj[k] is None:
+    steps = 0
+    while work:
+        L, adj = work.pop(0)
+        steps += 1
+        if steps > 10000:
+            raise CodeListError("automatic gradient: the expression is too deeply nested")
+        if adj is None:
             continue
         if L.op == "x":
             c = L.args[1] + n if L.args[1] < 0 else L.args[1]
             if not 0 <= c < n:
                 raise CodeListError(f"coordinate {L.args[1]} outside 0..{n - 1}")
-            parts.append((c, c + 1, adj[k]))
+            parts.append((c, c + 1, adj))
             continue
         body, lo, hi, init = L.args
         hi = n if hi is None else (hi + n if hi < 0 else hi)
         lo = lo + n if lo < 0 else lo
+        if lo >= hi:
+            continue
+        # a start value that reads the coordinates: d R / d init is 1 for a sum,
+        # R / init for a product
+        init_leaves: dict = {}
+        if isinstance(init, Expr):
+            _leaves(init, init_leaves)
+        for k2, L2 in init_leaves.items():
+            d_init = _diff(init, k2, {})
+            if L.op == "prod":
+                d_init = _mul(Expr("div", (L, init)), d_init)
+            work.append((L2, _mul(adj, d_init)))
         offs: set = set()
-        if not _table_offsets(body, offs):
-            raise CodeListError("automatic gradient: a Sum/Prod body may read the coordinates only as X[i + o]")
+        _xi_offsets(body, offs)
         for o in sorted(offs):
             dt = _diff(body, Expr("x", (BASE_I, o)).key, {})
             if dt is None:
@@ -534,7 +584,16 @@ def auto_gradient(f: Expr, n: int) -> Gradient:
             dj = _shift(dt, o, memo)
             if L.op == "prod":
                 dj = _mul(Expr("div", (L, _shift(body, o, memo))), dj)
-            parts.append((lo + o, hi + o, _mul(adj[k], dj)))
+            parts.append((lo + o, hi + o, _mul(adj, dj)))
+        inner: dict = {}
+        _body_leaves(body, inner)
+        for k2, L2 in inner.items():
+            dt = _diff(body, k2, {})
+            if dt is None:
+                continue
+            term = dt if L.op == "sum" else _mul(Expr("div", (L, body)), dt)
+            red = Expr("sum", (term, lo, hi, Const(0.0)))
+            work.append((L2, _mul(adj, red)))
     cuts = sorted({0, n} | {max(0, min(n, p[0])) for p in parts} | {max(0, min(n, p[1])) for p in parts})
     sections = []
     for a, b in zip(cuts[:-1], cuts[1:]):

@@ -396,12 +396,44 @@ def test_auto_gradient_prunes_like_written_lists(oracle_lib):
     assert surv["written"] <= surv["auto"] < 0.6 * surv["none"]
 
 
-def test_auto_gradient_rejects_unsupported_bodies():
-    X = CL.X
+def test_auto_gradient_rejects_a_bad_mode():
     with pytest.raises(CL.CodeListError):
-        CL.compile_objective(CL.Sum(lambda i: X[i] * X[0]), 4, "auto")     # a fixed coordinate in a body
-    with pytest.raises(CL.CodeListError):
-        CL.compile_objective(X[0], 4, "derive")
+        CL.compile_objective(CL.X[0], 4, "derive")
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_auto_gradient_through_bodies_with_box_constants(oracle_lib, case):
+    """Bodies that read a fixed coordinate, a reduction inside a body, a start
+    value that reads a coordinate, products: the derived test prunes only boxes
+    with a fixed-sign gradient component, and prunes some."""
+    X, Sum, Prod, sqr, cos, sin = CL.X, CL.Sum, CL.Prod, CL.sqr, CL.cos, CL.sin
+    n = 4
+    f = [Sum(lambda i: sqr(X[i] + (-0.3)) * (sqr(X[0]) + 1.0)),
+         Sum(lambda i: sqr(X[i]) * Sum(lambda k: sqr(X[k]) * 0.1 + 1.0)),
+         Sum(lambda i: sqr(X[i] + 0.2), lo=1, init=sqr(X[0] + (-0.7)) * 2.0),
+         Prod(lambda i: sqr(X[i]) + 1.0, init=sqr(X[1]) + 0.5),
+         Sum(lambda i: sin(X[i] * X[-1]) + sqr(X[i]) * 0.5)][case]
+    coef = CL.compile_objective(f, n, "auto").coef
+    p = P.Problem(P.CODELIST, n, np.tile([-2.0, 2.5], n), coef, wid=2, group=1, samples=2)
+    rng = np.random.default_rng(case)
+    pruned = 0
+    for _ in range(60):
+        x = rng.uniform(-1.8, 2.3, n)
+        w = 10.0 ** rng.uniform(-6, -2, n)
+        pbox = np.empty(2 * n)
+        pbox[0::2], pbox[1::2] = x - w, x + w
+        d = oracle_lib.eval_children(p, pbox, 1, np.array([0, 1], dtype=np.uint64), 1e300)[3]
+        for k, code in enumerate((0, 1)):
+            if not d[k]:
+                continue
+            pruned += 1
+            box = oracle_lib.child_box(p, pbox, 1, code).reshape(n, 2)
+            pts = box[:, 0] + (box[:, 1] - box[:, 0]) * (0.05 + 0.9 * rng.random((5, n)))
+            h = 1e-7
+            g = np.array([[(CL.point_value(coef, y + h * e) - CL.point_value(coef, y - h * e)) / (2 * h)
+                           for e in np.eye(n)] for y in pts])
+            assert any(np.all(g[:, j] > -1e-6) or np.all(g[:, j] < 1e-6) for j in range(n))
+    assert pruned > 0
 
 
 def _solve_codelist(oracle_lib, f, n, grad, lo, hi, split):
@@ -429,13 +461,7 @@ def test_front_end_shapes(oracle_lib):
     ]
     for k, (f, n, g, fmin, (lo, hi)) in enumerate(cases):
         split = P.default_split(n)
-        grads = ([g] if g is not None else []) + [None]
-        if k == 2:
-            # a reduction inside a body: the derived gradient does not cover it
-            with pytest.raises(CL.CodeListError):
-                CL.compile_objective(f, n, "auto")
-        else:
-            grads.append("auto")
+        grads = ([g] if g is not None else []) + [None, "auto"]
         for grad in grads:
             r = _solve_codelist(oracle_lib, f, n, grad, lo, hi, split)
             assert r.ub - r.lb <= 1e-6 and r.lb <= fmin + 1e-12 and fmin - 1e-6 <= r.ub, (k, grad)

@@ -61,6 +61,11 @@ def _objective(rng, n):
         return np.random.default_rng(seed)
 
     f = Sum(body, hi=hi)
+    extra = rng.random()
+    if extra < 0.25:        # a fixed coordinate inside the body
+        f = Sum(lambda i: body(i) * (sqr(X[0]) * 0.1 + 1.0), hi=hi)
+    elif extra < 0.5:       # a (loop-invariant) reduction inside the body
+        f = Sum(lambda i: body(i) + sqr(X[i]) * Sum(lambda k: cos(X[k]) * 0.1), hi=hi)
     if rng.random() < 0.5:
         f = f + sqr(X[0] + (-0.5)) * 0.5
     if rng.random() < 0.3:
