@@ -41,7 +41,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp"
+    # ptxas compiles the module's functions on all cores (the same code per
+    # function: only the optimisation passes run in parallel)
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-shared",
+           "-Xptxas", "--split-compile=0",
            "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
            "-o", tmp] + [os.path.join(CSRC, f) for f in SOURCES]
     if verbose:
