@@ -66,3 +66,35 @@ def test_solve_record_is_json_ready():
                       device_ms=0.25, trace={"n_surv": np.array([4, 2, 1]), "pool": np.array([4, 5, 2])})
     rec = json.loads(json.dumps(r.record("t")))
     assert rec["gap"] == 0.5 and rec["certified"] and rec["survivors"] == [4, 2, 1] and rec["list_sizes"] == [4, 5, 2]
+
+
+def test_spec_validation_on_the_host(lib):
+    """gpugo_instance_bytes validates a problem without touching the device:
+    the dimension limit (16384, above the reference's largest script), split
+    limits, and that a code list is compiled for the problem's n."""
+    import numpy as np
+    import gpugo_gb300 as G
+    from gpugo_gb300 import objectives as O
+    from gpugo_gb300 import problems as P
+
+    def accepts(p):
+        s, keep = G._spec(p)
+        out = ctypes.c_int64(0)
+        rc = lib.gpugo_instance_bytes(ctypes.byref(s), ctypes.byref(out))
+        return rc == 0, out.value
+
+    def cosquad(n):
+        return P.Problem(P.COSQUAD, n, np.tile([-1.0, 1.0], n), np.ones(3 * n), wid=3, group=4)
+
+    ok, nbytes = accepts(cosquad(16384))
+    assert ok and nbytes > 0
+    assert not accepts(cosquad(16385))[0]
+    p = cosquad(40)
+    p.wid, p.group = 2, 33          # 2^33 children per iteration (the group is capped by n)
+    assert not accepts(p)[0]
+    p.wid, p.group = 2, 32          # 2^32: the largest split
+    assert accepts(p)[0]
+    lv = O.problem("levy", 6)
+    assert accepts(lv)[0]
+    wrong_n = P.Problem(P.CODELIST, 7, np.tile([-10.0, 10.0], 7), lv.coef, wid=3, group=7)
+    assert not accepts(wrong_n)[0]
