@@ -30,6 +30,10 @@ top-level statements (the whole 50-variable B&B run) are skipped.  The result-bo
 merging vectors come from the same execution of ``rosenbrock50.py``'s host
 functions ``combine`` / ``connectivity``.
 
+``--levy10000`` adds the reference's largest script (10 000 variables) to it;
+``--large`` writes ``reference_vectors_1000.npz`` from the four families'
+1000-variable scripts.
+
 ``--codelist`` writes ``codelist_vectors.npz`` instead: the value, sample and
 derivative code lists of the seven scripts without a built-in family (Levy,
 Salomon, Styblinski, Belegundu, Breiman, Fu, Zabinsky), which pin the code-list
@@ -363,10 +367,107 @@ def codelist_main(ref_root: str, only: list[str] | None = None):
     print("wrote", dst)
 
 
+def large_main(ref_root: str, n: int = 1000):
+    """The four families' 1000-variable scripts (rastrigin1000.py, ...): the same
+    device functions at the reference's larger size, written to
+    reference_vectors_1000.npz (12 children per family at the first, a middle
+    and the last cycle)."""
+    oracle.build()
+    sys.modules["numba"] = make_numba_stub()
+    rng = np.random.default_rng(0x6C617267)
+    out = {}
+    for name, (rel, ia_name, pre, dom, fam, coef, sign_times) in FAMILIES.items():
+        rel_n = rel.replace("50.py", f"{n}.py")
+        ia_mod = load_updated_ia(ref_root, sign_times)
+        ns = load_script(ref_root, rel_n, ia_name, ia_mod)
+        value, sample, deriv = ns[pre + "Value_IA"], ns[pre + "Sample_IA"], ns[pre + "Derivative_IA"]
+        complete = ns["completeRegion"]
+        lo, hi = dom
+        root = np.tile([lo, hi], n).astype(np.float64)
+        mid_cyc = 1 + GROUP * (n // (2 * GROUP))
+        last_cyc = n - GROUP + 1
+        c1 = np.asarray(complete(root, int(rng.integers(0, WID ** GROUP)), 1), dtype=np.float64)
+        xstar = 1.0 if name == "rosenbrock" else 0.0
+        small = np.empty(2 * n)
+        for i in range(n):
+            w = float(rng.uniform(0.5, 2.0)) * 1e-3
+            off = float(rng.uniform(-0.4, 0.4)) * w
+            small[2 * i], small[2 * i + 1] = xstar - w + off, xstar + w + off
+        parents = [(root, 1), (c1, mid_cyc), (small, last_cyc)]
+        pidx, cycs, codes, lbs, samps, dflags = [], [], [], [], [], []
+        t0 = time.time()
+        for k, (pbox, cyc) in enumerate(parents):
+            for q in [int(v) for v in rng.integers(0, WID ** GROUP, 3)] + [WID ** GROUP - 1]:
+                lb, _ = value(pbox, q, 1e300, 0, cyc)
+                lbs.append(float(lb))
+                samps.append(float(sample(pbox, q, SAMPLES, cyc)))
+                dflags.append(int(deriv(pbox, q, 0, cyc)) if name != "ackley" else -1)
+                pidx.append(k); cycs.append(cyc); codes.append(q)
+        out[name + "_family"] = np.array([fam])
+        out[name + "_coef"] = coef(n)
+        out[name + "_domain"] = np.tile(np.array(dom, dtype=np.float64), n)
+        out[name + "_parents"] = np.stack([pb for pb, _ in parents])
+        out[name + "_parent_idx"] = np.array(pidx, dtype=np.int64)
+        out[name + "_cyc"] = np.array(cycs, dtype=np.int64)
+        out[name + "_code"] = np.array(codes, dtype=np.int64)
+        out[name + "_lb"] = np.array(lbs)
+        out[name + "_samp"] = np.array(samps)
+        out[name + "_dflag"] = np.array(dflags, dtype=np.int64)
+        print(name, n, "cases", len(codes), f"{time.time() - t0:.0f} s", flush=True)
+    dst = os.path.join(HERE, f"reference_vectors_{n}.npz")
+    np.savez_compressed(dst, **out)
+    print("wrote", dst)
+
+
+def levy10000_main(ref_root: str):
+    """The reference's largest script, levy10000.py (10 000 variables, wid 4,
+    cycles of 10): value, sample and derivative of a few children at the first
+    cycle, a middle cycle and the last one, added to codelist_vectors.npz as
+    levy10000_*.  Exact rational rounding over 10^5 operations per child makes
+    this slow (minutes)."""
+    oracle.build()
+    sys.modules["numba"] = make_numba_stub()
+    rng = np.random.default_rng(0x6C763130)
+    n = 10000
+    dst = os.path.join(HERE, "codelist_vectors.npz")
+    out = dict(np.load(dst))
+    ia_mod = load_updated_ia(ref_root, True)
+    ns = load_script(ref_root, "GPUGO_1.1/6-Levy/levy10000.py", "IALevy", ia_mod)
+    value, sample, deriv = ns["LevyValue_IA"], ns["LevySample_IA"], ns["LevyDerivative_IA"]
+    complete = ns["completeRegion"]
+    root = np.tile([-10.0, 10.0], n).astype(np.float64)
+    mid = np.asarray(complete(root, int(rng.integers(0, WID ** GROUP)), 1), dtype=np.float64)
+    parents = [(root, 1), (mid, 4001), (root, n - 9)]
+    pidx, cycs, codes, lbs, samps, dflags = [], [], [], [], [], []
+    t0 = time.time()
+    for k, (pbox, cyc) in enumerate(parents):
+        for q in [int(v) for v in rng.integers(0, WID ** GROUP, 3)] + [WID ** GROUP - 1]:
+            lb, _ = value(pbox, q, 1e300, 0, cyc)
+            lbs.append(float(lb))
+            samps.append(float(sample(pbox, q, SAMPLES, cyc)))
+            dflags.append(int(deriv(pbox, q, 0, cyc)))
+            pidx.append(k); cycs.append(cyc); codes.append(q)
+            print("levy10000 child", len(codes), f"{time.time() - t0:.0f} s", flush=True)
+    out["levy10000_domain"] = np.tile(np.array([-10.0, 10.0]), n)
+    out["levy10000_parents"] = np.stack([pb for pb, _ in parents])
+    out["levy10000_parent_idx"] = np.array(pidx, dtype=np.int64)
+    out["levy10000_cyc"] = np.array(cycs, dtype=np.int64)
+    out["levy10000_code"] = np.array(codes, dtype=np.int64)
+    out["levy10000_lb"] = np.array(lbs)
+    out["levy10000_samp"] = np.array(samps)
+    out["levy10000_dflag"] = np.array(dflags, dtype=np.int64)
+    np.savez_compressed(dst, **out)
+    print("wrote", dst)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
     if "--codelist" in sys.argv:
         codelist_main(root, args[1:] or None)
+    elif "--levy10000" in sys.argv:
+        levy10000_main(root)
+    elif "--large" in sys.argv:
+        large_main(root)
     else:
         main(root)

@@ -472,3 +472,22 @@ def test_auto_gradient_of_fixed_coordinates_is_tabled():
     c = CL.compile_objective(sqr(X[0] + (-1.0)) + sqr(X[1]) * 3.0, 2, "auto")
     secs = CL.parse(c.coef)["sections"]
     assert len(secs) == 2 and all(s["tabled"] is not None for s in secs)
+
+
+def test_oracle_matches_reference_levy10000(oracle_lib):
+    """The reference's largest script (levy10000.py, 10 000 variables): value,
+    sample and derivative of children at the first, a middle and the last cycle,
+    bit for bit."""
+    z = np.load(CL_GOLD)
+    n = 10000
+    f, g, _ = O.levy(n)
+    p = P.Problem(P.CODELIST, n, z["levy10000_domain"], CL.compile_objective(f, n, g).coef, wid=4, group=10,
+                  samples=10)
+    pidx, cyc, code = z["levy10000_parent_idx"], z["levy10000_cyc"], z["levy10000_code"]
+    for k, pbox in enumerate(z["levy10000_parents"]):
+        sel = pidx == k
+        cy = int(cyc[sel][0])
+        lb, samp, _, dflag = oracle_lib.eval_children(p, pbox, cy, code[sel].astype(np.uint64), 1e300)
+        assert np.array_equal(_bits(lb), _bits(z["levy10000_lb"][sel]))
+        assert np.array_equal(_bits(samp), _bits(z["levy10000_samp"][sel]))
+        assert np.array_equal(dflag, z["levy10000_dflag"][sel])

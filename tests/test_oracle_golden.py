@@ -69,3 +69,36 @@ def test_box_decoder(oracle_lib, gold):
         box = oracle_lib.child_box(p, pb, int(gold["decoder_cyc"][t]), int(gold["decoder_code"][t]))
         np.testing.assert_array_equal(box, gold["decoder_complete"][t])
         np.testing.assert_array_equal(box, gold["decoder_select"][t])
+
+
+GOLD_1000 = os.path.join(os.path.dirname(__file__), "golden", "reference_vectors_1000.npz")
+
+
+def _eval_n(oracle_lib, g, name, n):
+    p = NS(family=int(g[name + "_family"][0]), n=n, wid=4, group=10, samples=10, stop_mode=0, width_tol=1e-4,
+           gap_tol=0.0, ub_init=1e6, domain=g[name + "_domain"], coef=g[name + "_coef"])
+    par, pidx, cyc, code = g[name + "_parents"], g[name + "_parent_idx"], g[name + "_cyc"], g[name + "_code"]
+    lbs, samps, dflags = [], [], []
+    for k in range(code.size):
+        lb, samp, _, dflag = oracle_lib.eval_children(p, par[pidx[k]], int(cyc[k]), np.array([code[k]]), 1e300)
+        lbs.append(lb[0]); samps.append(samp[0]); dflags.append(dflag[0])
+    return np.array(lbs), np.array(samps), np.array(dflags)
+
+
+@pytest.mark.parametrize("name", ["rastrigin", "rosenbrock", "ackley", "griewank"])
+def test_reference_1000_variable_scripts(oracle_lib, name):
+    """The same families at the reference's 1000-variable scripts (rastrigin1000.py,
+    ...): bit for bit where the reference's constants are exact, otherwise the
+    enclosure rule of the 50-variable vectors."""
+    g = np.load(GOLD_1000)
+    lb, samp, dflag = _eval_n(oracle_lib, g, name, 1000)
+    ref_lb, ref_s, ref_d = g[name + "_lb"], g[name + "_samp"], g[name + "_dflag"]
+    if name in ("rastrigin", "rosenbrock"):
+        np.testing.assert_array_equal(lb, ref_lb)
+        np.testing.assert_array_equal(samp, ref_s)
+    else:
+        assert np.all(lb <= ref_lb) and np.all(samp >= ref_s)
+        np.testing.assert_allclose(lb, ref_lb, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(samp, ref_s, rtol=1e-12, atol=1e-12)
+    m = ref_d >= 0
+    np.testing.assert_array_equal(dflag[m], ref_d[m])
