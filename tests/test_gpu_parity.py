@@ -55,6 +55,37 @@ def test_children_reference_setups(oracle_lib, name):
         assert _same(f_g, f_o), name
 
 
+GOLD_1000 = os.path.join(os.path.dirname(__file__), "golden", "reference_vectors_1000.npz")
+
+
+@pytest.mark.parametrize("name", ["rastrigin", "rosenbrock", "ackley", "griewank"])
+def test_children_reference_1000_variable_scripts(oracle_lib, name):
+    """The reference's 1000-variable scripts (rastrigin1000.py, ...): the term
+    tables no longer fit shared memory, so the children are bounded from the
+    global copy.  GPU against the oracle on random codes under each golden
+    parent, and against the reference's own values on the golden codes."""
+    g = np.load(GOLD_1000)
+    p = P.Problem(int(g[name + "_family"][0]), 1000, g[name + "_domain"], g[name + "_coef"], wid=4, group=10,
+                  samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6)
+    rng = np.random.default_rng(5)
+    cycs, pidx, gcode = g[name + "_cyc"], g[name + "_parent_idx"], g[name + "_code"]
+    for k, pbox in enumerate(g[name + "_parents"]):
+        cyc = int(cycs[pidx == k][0])
+        mine = gcode[pidx == k].astype(np.uint64)
+        codes = np.concatenate([rng.integers(0, 4 ** 10, 600).astype(np.uint64), mine])
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, codes, 1e300)
+        ub = float(np.quantile(lb_o, 0.5))
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cyc, codes, ub)
+        lb_g, s_g, f_g = G.eval_children(p, pbox, cyc, codes, ub)
+        assert _same(lb_g, lb_o) and _same(s_g, s_o) and _same(f_g, f_o), name
+        lb_r, s_r = g[name + "_lb"][pidx == k], g[name + "_samp"][pidx == k]
+        lb_m, s_m = lb_g[-mine.size:], s_g[-mine.size:]
+        if name in ("rastrigin", "rosenbrock"):
+            assert _same(lb_m, lb_r) and _same(s_m, s_r), name
+        else:
+            assert np.all(lb_m <= lb_r) and np.all(s_m >= s_r), name
+
+
 CFGS = [
     ("cfg1", lambda: P.config1()),
     ("cfg2", lambda: P.config2()),
