@@ -32,6 +32,8 @@ functions ``combine`` / ``connectivity``.
 
 ``--levy10000`` adds the reference's largest script (10 000 variables) to it;
 ``--large`` writes ``reference_vectors_1000.npz`` from the four families'
+1000-variable scripts, and ``--codelist-large`` writes
+``codelist_vectors_1000.npz`` from the seven code-list benchmarks'
 1000-variable scripts.
 
 ``--codelist`` writes ``codelist_vectors.npz`` instead: the value, sample and
@@ -419,6 +421,53 @@ def large_main(ref_root: str, n: int = 1000):
     print("wrote", dst)
 
 
+def codelist_large_main(ref_root: str, n: int = 1000):
+    """The seven code-list benchmarks' 1000-variable scripts (levy1000.py,
+    salomon1000.py, ...): value, sample and derivative of 12 children per script
+    at the first, a middle and the last cycle, written to
+    codelist_vectors_1000.npz."""
+    oracle.build()
+    sys.modules["numba"] = make_numba_stub()
+    rng = np.random.default_rng(0x636C3130)
+    out = {}
+    for name, (rel, ia_name, pre, dom, centre) in CODELIST_SCRIPTS.items():
+        ia_mod = load_updated_ia(ref_root, True)
+        ns = load_script(ref_root, rel.replace("50.py", f"{n}.py"), ia_name, ia_mod)
+        value, sample, deriv = ns[pre + "Value_IA"], ns[pre + "Sample_IA"], ns[pre + "Derivative_IA"]
+        complete = ns["completeRegion"]
+        lo, hi = dom
+        root = np.tile([lo, hi], n).astype(np.float64)
+        c1 = np.asarray(complete(root, int(rng.integers(0, WID ** GROUP)), 1), dtype=np.float64)
+        small = np.empty(2 * n)
+        for i in range(n):
+            w = float(rng.uniform(0.5, 2.0)) * SMALL_WIDTH.get(name, 1e-2) * (hi - lo)
+            off = float(rng.uniform(-0.4, 0.4)) * w
+            small[2 * i] = max(lo, centre - w + off)
+            small[2 * i + 1] = min(hi, centre + w + off)
+        parents = [(root, 1), (c1, 1 + GROUP * (n // (2 * GROUP))), (small, n - GROUP + 1)]
+        pidx, cycs, codes, lbs, samps, dflags = [], [], [], [], [], []
+        t0 = time.time()
+        for k, (pbox, cyc) in enumerate(parents):
+            for q in [int(v) for v in rng.integers(0, WID ** GROUP, 3)] + [WID ** GROUP - 1]:
+                lb, _ = value(pbox, q, 1e300, 0, cyc)
+                lbs.append(float(lb))
+                samps.append(float(sample(pbox, q, SAMPLES, cyc)))
+                dflags.append(int(deriv(pbox, q, 0, cyc)))
+                pidx.append(k); cycs.append(cyc); codes.append(q)
+        out[name + "_domain"] = np.tile(np.array(dom, dtype=np.float64), n)
+        out[name + "_parents"] = np.stack([pb for pb, _ in parents])
+        out[name + "_parent_idx"] = np.array(pidx, dtype=np.int64)
+        out[name + "_cyc"] = np.array(cycs, dtype=np.int64)
+        out[name + "_code"] = np.array(codes, dtype=np.int64)
+        out[name + "_lb"] = np.array(lbs)
+        out[name + "_samp"] = np.array(samps)
+        out[name + "_dflag"] = np.array(dflags, dtype=np.int64)
+        print(name, n, "cases", len(codes), f"{time.time() - t0:.0f} s", flush=True)
+    dst = os.path.join(HERE, f"codelist_vectors_{n}.npz")
+    np.savez_compressed(dst, **out)
+    print("wrote", dst)
+
+
 def levy10000_main(ref_root: str):
     """The reference's largest script, levy10000.py (10 000 variables, wid 4,
     cycles of 10): value, sample and derivative of a few children at the first
@@ -467,6 +516,8 @@ if __name__ == "__main__":
         codelist_main(root, args[1:] or None)
     elif "--levy10000" in sys.argv:
         levy10000_main(root)
+    elif "--codelist-large" in sys.argv:
+        codelist_large_main(root)
     elif "--large" in sys.argv:
         large_main(root)
     else:

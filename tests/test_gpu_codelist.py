@@ -184,3 +184,32 @@ def test_levy10000_reference_size(oracle_lib):
     r = G.solve(p, box_cap=4)
     assert r.status == G.ITER_LIMIT and r.boxes_bounded == 2 * 4 ** 10 and r.lb <= r.ub
     print(f"\nlevy10000: 2 iterations in {r.device_ms:.1f} ms, enclosure [{r.lb:.6g}, {r.ub:.6g}]")
+
+
+@pytest.mark.parametrize("name", sorted(O.REFERENCE))
+def test_children_match_reference_1000_variable_scripts(oracle_lib, name):
+    """The seven benchmarks' 1000-variable scripts: the reference's values on
+    its golden codes, and the oracle on more children with a UB that rules
+    some out, at the first, a middle and the last cycle."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "codelist_vectors_1000.npz"))
+    n = 1000
+    f, g, _ = O.REFERENCE[name](n)
+    p = P.Problem(P.CODELIST, n, z[name + "_domain"], CL.compile_objective(f, n, g).coef, wid=4, group=10,
+                  samples=10)
+    rng = np.random.default_rng(6)
+    pidx, cyc = z[name + "_parent_idx"], z[name + "_cyc"]
+    for k, pbox in enumerate(z[name + "_parents"]):
+        sel = pidx == k
+        cy = int(cyc[sel][0])
+        lb_g, s_g, f_g = G.eval_children(p, pbox, cy, z[name + "_code"][sel].astype(np.uint64), 1e300)
+        assert _same(lb_g, z[name + "_lb"][sel])
+        if (name, "samp") not in NOT_REPRODUCED:
+            assert _same(s_g, z[name + "_samp"][sel])
+        if (name, "dflag") not in NOT_REPRODUCED:
+            assert np.array_equal(f_g, z[name + "_dflag"][sel])
+        codes = np.concatenate([rng.integers(0, 4 ** 10, 300), [0, 4 ** 10 - 1]]).astype(np.uint64)
+        lb_o, _, _, _ = oracle_lib.eval_children(p, pbox, cy, codes, 1e300)
+        ub = float(np.quantile(lb_o, 0.5))
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cy, codes, ub)
+        lb_g, s_g, f_g = G.eval_children(p, pbox, cy, codes, ub)
+        assert _same(lb_g, lb_o) and _same(s_g, s_o) and np.array_equal(f_g, f_o)
