@@ -2515,6 +2515,7 @@ int gpugo_fp64_peak(int32_t repeats, double* tflops_out, double* ms_out) {
 }
 
 int gpugo_instance_bytes(const gpugo_spec* spec, int64_t* bytes_out) {
+  if (!bytes_out) return GPUGO_ERR_INVALID;
   int rc = validate(spec);
   if (rc) return rc;
   Layout L;
@@ -2942,7 +2943,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
 
 int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_done_out) {
   NvtxRange nvtx_range("gpugo_poll");
-  if (!E) return GPUGO_ERR_INVALID;
+  if (!E || max_done < 0 || (max_done > 0 && !done)) return GPUGO_ERR_INVALID;
   std::vector<int> fin;
   for (int s = 0; s < E->max_slots && (int)fin.size() < max_done; ++s)
     if (E->slots[s].used && E->h_state[s].status == ST_DONE) fin.push_back(s);
@@ -3195,7 +3196,8 @@ int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_
   NvtxRange nvtx_range("gpugo_eval_children");
   int rc = validate(spec);
   if (rc) return rc;
-  if (!parent_box || (!codes && m > 0) || m < 0 || cyc < 1 || cyc > spec->n) return GPUGO_ERR_INVALID;
+  if (!parent_box || (m > 0 && (!codes || !lb_out || !samp_out || !flag_out)) || m < 0 || cyc < 1 || cyc > spec->n)
+    return GPUGO_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
   int64_t M = children_host(spec, cyc);

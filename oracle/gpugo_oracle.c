@@ -818,12 +818,12 @@ static int cl_parse(const oc_spec* sp, consts* c)
     int prev_hi = 0;
     for (uint32_t s = 0; s < h[H_NSEC]; ++s) {
         const uint32_t* q = w + CL_HEADER + (size_t)CL_SEC * s;
-        int lo = (int)q[0], hi = (int)q[1], st = (int)q[2], ln = (int)q[3], r = (int)q[4];
+        int lo = (int)q[0], hi = (int)q[1], st = (int)q[2], ln = (int)q[3];
         int32_t chk = (int32_t)q[5];
-        uint32_t rs = q[6];
+        uint32_t r = q[4], rs = q[6];
         if (lo < prev_hi || lo >= hi || hi > n) return -2;   /* sections ascend and do not overlap */
         prev_hi = hi;
-        if (r >= nreg || (rs != CL_NONE && rs >= (uint32_t)nreg)) return -2;
+        if (r >= (uint32_t)nreg || (rs != CL_NONE && rs >= (uint32_t)nreg)) return -2;
         if ((long)lo + chk < 0 || (long)hi - 1 + chk >= n) return -2;
         /* a tabled section: its flag per (j, digits of X[j + o]) is what its code gives */
         if (q[7] > 1) return -2;

@@ -98,3 +98,40 @@ def test_spec_validation_on_the_host(lib):
     assert accepts(lv)[0]
     wrong_n = P.Problem(P.CODELIST, 7, np.tile([-10.0, 10.0], 7), lv.coef, wid=3, group=7)
     assert not accepts(wrong_n)[0]
+
+
+def test_null_arguments_are_rejected_before_the_device(lib):
+    """Missing output buffers, a null engine or a null problem give
+    GPUGO_ERR_INVALID from the host checks (no device is touched, so this runs
+    without a GPU)."""
+    import numpy as np
+    import gpugo_gb300 as G
+    INVALID = -1
+    p = G.config2()
+    s, keep = G._spec(p)
+    codes = np.zeros(4, dtype=np.uint64)
+    out = np.zeros(4)
+    flags = np.zeros(4, dtype=np.int32)
+    dp = ctypes.POINTER(ctypes.c_double)
+    box = p.domain.ctypes.data_as(dp)
+    cp = codes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    fp = flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    for fn in (lib.gpugo_eval_children, lib.gpugo_eval_children_static):
+        assert fn(ctypes.byref(s), box, 1, cp, 4, 1e300, None, out.ctypes.data_as(dp), fp) == INVALID
+        assert fn(ctypes.byref(s), box, 1, cp, 4, 1e300, out.ctypes.data_as(dp), None, fp) == INVALID
+        assert fn(ctypes.byref(s), box, 1, cp, 4, 1e300, out.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                  None) == INVALID
+        assert fn(ctypes.byref(s), None, 1, cp, 4, 1e300, out.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                  fp) == INVALID
+        assert fn(ctypes.byref(s), box, 0, cp, 4, 1e300, out.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                  fp) == INVALID                       # cycles are 1-based
+        assert fn(None, box, 1, cp, 4, 1e300, out.ctypes.data_as(dp), out.ctypes.data_as(dp), fp) == INVALID
+    assert lib.gpugo_instance_bytes(ctypes.byref(s), None) == INVALID
+    assert lib.gpugo_instance_bytes(None, ctypes.byref(ctypes.c_int64())) == INVALID
+    n_done = ctypes.c_int32()
+    assert lib.gpugo_poll(None, None, 0, ctypes.byref(n_done)) == INVALID
+    assert lib.gpugo_run(None, 1, None) == INVALID
+    assert lib.gpugo_solve(ctypes.byref(s), None, None, None, 0, None, None) == INVALID
+    nr = ctypes.c_int64()
+    assert lib.gpugo_combine(None, 3, 2, 1e-3, None, 0, ctypes.byref(nr)) == INVALID
+    assert lib.gpugo_combine(out.ctypes.data_as(dp), 1, 2, -1.0, None, 0, ctypes.byref(nr)) == INVALID

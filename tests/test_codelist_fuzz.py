@@ -1,0 +1,93 @@
+"""The library's code-list checks against the oracle's, on randomly damaged arrays.
+
+The device interpreter checks no index: ``gpugo_instance_bytes`` (and every
+entry point that takes a problem) must reject each array the interpreter could
+not run within bounds.  The oracle carries its own, separately written checks
+and runs every array it accepts.  Here thousands of compiled objectives with
+one or two integer words changed (registers, coordinates, offsets, ranges,
+opcodes, table and section fields) go to both: they must accept and reject the
+same arrays, and the oracle must evaluate every accepted one (value, sample and
+derivative lists) without failing.  No GPU is needed: the library validates on
+the host.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpugo_gb300 import codelist as CL
+from gpugo_gb300 import objectives as O
+from gpugo_gb300 import problems as P
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from gpugo_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def _objectives():
+    out = []
+    for name in sorted(O.REFERENCE):
+        for n in (6, 13):
+            f, g, dom = O.REFERENCE[name](n)
+            out.append((n, dom, CL.compile_objective(f, n, g).coef))
+            out.append((n, dom, CL.compile_objective(f, n, "auto").coef))
+            out.append((n, dom, CL.compile_objective(f, n, g, tables=False).coef))
+    return out
+
+
+def _damage(rng, coef, n):
+    """One or two integer words of the array replaced by a value that is near
+    a valid one (small numbers, +-1, +-n), a negative 32-bit number, one byte
+    of a packed instruction word, a flipped bit or anything at all."""
+    p = CL.parse(coef)
+    U = CL.HEADER + CL.SEC_WORDS * len(p["sections"])
+    I = U + CL.TAB_WORDS * len(p["tables"])
+    C = I + CL.INS_WORDS * len(p["instructions"])
+    c = coef.copy()
+    w = c.view(np.uint64)
+    for _ in range(1 + int(rng.random() < 0.25)):
+        k = int(rng.integers(0, C))
+        old = int(w[k])
+        kind = int(rng.integers(6))
+        if kind == 0:
+            v = int(rng.integers(0, 20))
+        elif kind == 1:
+            v = (old + int(rng.choice([-1, 1, -n, n, n + 1]))) & 0xFFFFFFFF
+        elif kind == 2:
+            v = int(rng.integers(0, 1 << 32))
+        elif kind == 3:
+            b = int(rng.integers(4))
+            v = (old & ~(0xFF << (8 * b))) | (int(rng.integers(0, 24)) << (8 * b))
+        elif kind == 4:
+            v = (-int(rng.integers(1, 4))) & 0xFFFFFFFF
+        else:
+            v = old ^ (1 << int(rng.integers(0, 32)))
+        w[k] = v
+    return c
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_library_and_oracle_accept_the_same_arrays(lib, oracle_lib, seed):
+    from gpugo_gb300 import _spec
+    objs = _objectives()
+    rng = np.random.default_rng(0x66757A7A + seed)
+    codes = np.array([0, 1, 3, 7], dtype=np.uint64)
+    accepted = 0
+    for t in range(5000):
+        n, dom, coef = objs[int(rng.integers(len(objs)))]
+        q = P.Problem(P.CODELIST, n, np.tile(dom, n), _damage(rng, coef, n), wid=2, group=3)
+        s, keep = _spec(q)
+        nbytes = ctypes.c_int64(0)
+        lib_ok = lib.gpugo_instance_bytes(ctypes.byref(s), ctypes.byref(nbytes)) == 0
+        try:
+            lb, samp, _, _ = oracle_lib.eval_children(q, q.domain, 1, codes, 1e300)
+            oracle_ok = True
+        except ValueError:
+            oracle_ok = False
+        assert lib_ok == oracle_ok, (t, n, lib_ok)
+        accepted += lib_ok
+    # both kinds of outcome are exercised
+    assert 500 < accepted < 4500
