@@ -18,11 +18,15 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgpugo_oracle.so")
+# another build of the same source (e.g. `make -C oracle asan`), used as is
+_LIB_OVERRIDE = os.environ.get("GPUGO_ORACLE_LIB")
 _lib = None
 
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, no GPU needed)."""
+    if _LIB_OVERRIDE:
+        return _LIB_OVERRIDE
     src = os.path.join(_HERE, "gpugo_oracle.c")
     if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -60,7 +64,7 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(_LIB_OVERRIDE or _LIB_PATH)
         dp = ctypes.POINTER(ctypes.c_double)
         L.oc_ia_op.argtypes = [ctypes.c_int, ctypes.c_long, dp, dp, dp]
         L.oc_round_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, dp, dp, dp]
