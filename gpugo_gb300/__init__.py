@@ -30,8 +30,10 @@ _dp = ctypes.POINTER(ctypes.c_double)
 
 
 def _spec(p: Problem):
-    dom = np.ascontiguousarray(p.domain, dtype=np.float64)
-    coef = np.ascontiguousarray(p.coef, dtype=np.float64)
+    dom = np.ascontiguousarray(p.domain, dtype=np.float64).ravel()
+    coef = np.ascontiguousarray(p.coef, dtype=np.float64).ravel()
+    if dom.size != 2 * int(p.n):      # the library reads 2n bounds through a plain pointer
+        raise ValueError(f"domain holds {dom.size} bounds, the problem needs 2n = {2 * int(p.n)}")
     s = _lib.Spec(int(p.family), int(p.n), int(p.wid), int(p.group), int(p.samples), int(p.stop_mode),
                   float(p.width_tol), float(p.gap_tol), float(p.ub_init),
                   dom.ctypes.data_as(_dp), coef.ctypes.data_as(_dp), coef.size, int(p.max_iter or 0),
@@ -123,6 +125,8 @@ def eval_children(p: Problem, parent_box: np.ndarray, cyc: int, codes: np.ndarra
     L = _lib.load()
     s, keep = _spec(p)
     pb = np.ascontiguousarray(parent_box, dtype=np.float64).ravel()
+    if pb.size != 2 * int(p.n):
+        raise ValueError(f"parent box holds {pb.size} bounds, the problem needs 2n = {2 * int(p.n)}")
     codes = np.ascontiguousarray(codes, dtype=np.uint64).ravel()
     m = codes.size
     lb = np.empty(m)

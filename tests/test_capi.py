@@ -135,3 +135,17 @@ def test_null_arguments_are_rejected_before_the_device(lib):
     nr = ctypes.c_int64()
     assert lib.gpugo_combine(None, 3, 2, 1e-3, None, 0, ctypes.byref(nr)) == INVALID
     assert lib.gpugo_combine(out.ctypes.data_as(dp), 1, 2, -1.0, None, 0, ctypes.byref(nr)) == INVALID
+
+
+def test_python_side_checks_array_sizes(lib):
+    """The C ABI reads 2n bounds through plain pointers: the Python mirror
+    refuses a domain or a parent box of the wrong size before the call."""
+    import numpy as np
+    import gpugo_gb300 as G
+    p = G.config2()
+    p.domain = p.domain[:-2]                  # changed after construction
+    with pytest.raises(ValueError):
+        G._spec(p)
+    q = G.config2()
+    with pytest.raises(ValueError):
+        G.eval_children(q, q.domain[:6], 1, np.zeros(2, dtype=np.uint64), 1e300)
