@@ -24,7 +24,8 @@ from .problems import (CHAINED, CODELIST, COSQUAD, EXPSQRT, PRODCOS, STOP_GAP, S
 
 __all__ = ["solve", "eval_children", "Engine", "SolveResult", "Problem", "GpugoError", "instance", "config1",
            "config2", "config3", "config4", "config5", "COSQUAD", "CHAINED", "EXPSQRT", "PRODCOS", "CODELIST",
-           "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info", "combine"]
+           "STOP_GAP", "STOP_WIDTH", "CERTIFIED", "FINISHED", "ITER_LIMIT", "device_info", "combine",
+           "checkpoint_ok"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -138,6 +139,13 @@ def eval_children(p: Problem, parent_box: np.ndarray, cyc: int, codes: np.ndarra
                                flag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
     _lib.check(rc, "gpugo_eval_children")
     return lb, samp, flag
+
+
+def checkpoint_ok(data: bytes) -> bool:
+    """Whether ``Engine.restore`` would accept a checkpoint (``gpugo_checkpoint_check``:
+    the problem, the state and every index the lists hold), checked on the host."""
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    return _lib.load().gpugo_checkpoint_check(buf, len(data)) == 0
 
 
 def combine(boxes: np.ndarray, tol: float = 1e-3) -> np.ndarray:

@@ -72,7 +72,7 @@ EXPORTS = [
     "gpugo_solve", "gpugo_eval_children", "gpugo_engine_create", "gpugo_engine_destroy", "gpugo_submit",
     "gpugo_run", "gpugo_poll", "gpugo_engine_free_bytes", "gpugo_instance_bytes", "gpugo_strerror",
     "gpugo_device_info", "gpugo_engine_stats", "gpugo_fp64_peak", "gpugo_eval_children_static",
-    "gpugo_combine", "gpugo_checkpoint", "gpugo_restore",
+    "gpugo_combine", "gpugo_checkpoint", "gpugo_restore", "gpugo_checkpoint_check",
 ]
 
 _lib = None
@@ -120,6 +120,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     L.gpugo_fp64_peak.argtypes = [ctypes.c_int32, _dp, _dp]
     L.gpugo_combine.argtypes = [_dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _dp, ctypes.c_int64, _i64p]
     L.gpugo_checkpoint.argtypes = [vp, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, _i64p]
+    L.gpugo_checkpoint_check.argtypes = [ctypes.c_void_p, ctypes.c_int64]
     L.gpugo_restore.argtypes = [vp, ctypes.c_void_p, ctypes.c_int64, _dp, _dp, ctypes.c_int64, _dp,
                                 ctypes.POINTER(Trace), _i64p]
     _lib = L

@@ -2723,6 +2723,79 @@ struct CkptHeader {
 };
 const char CKPT_MAGIC[8] = {'G', 'P', 'U', 'G', 'O', 'C', 'K', '1'};
 size_t pad8(size_t b) { return (b + 7) & ~size_t(7); }
+
+// The kernels trust a restored solve as they trust one they built: every index
+// its state and lists can form is checked here, so that a damaged or foreign
+// buffer is refused instead of read out of bounds.  `o` points at the parent
+// rows; the state is the one every iteration ends with (the checkpoint is taken
+// between runs).
+int check_restored(const gpugo_spec& sp, const CkptHeader& hd, const char* o) {
+  const State& st = hd.st;
+  const int n = sp.n;
+  if (st.status != ST_EXPAND && st.status != ST_REPOP && st.status != ST_DONE) return GPUGO_ERR_INVALID;
+  if (st.cyc < 1 || st.cyc > n || st.iter < 0 || st.iter + 1 != hd.rows) return GPUGO_ERR_INVALID;
+  if (st.m_children != children_host(&sp, st.cyc)) return GPUGO_ERR_INVALID;
+  if (st.out_count < hd.nout || st.count_before < 0 || st.count_before > hd.cnt || st.ubc_count < 0 ||
+      st.cand_total < 0 || st.cand_done < 0 || st.removed_new < 0 || st.bounded < 0 || st.samples < 0)
+    return GPUGO_ERR_INVALID;
+  if (st.has_who && (int)(st.ub_who & 0xff) >= sp.samples) return GPUGO_ERR_INVALID;
+  const char* q = o + 24 * (size_t)n * hd.rows;               // past the parent boxes and part widths
+  std::vector<int64_t> nchild((size_t)hd.rows);
+  for (int64_t r = 0; r < hd.rows; ++r) {
+    int32_t c;
+    memcpy(&c, q + 4 * r, 4);
+    if (c < 1 || c > n) return GPUGO_ERR_INVALID;
+    nchild[(size_t)r] = children_host(&sp, c);
+  }
+  q += pad8(4 * (size_t)hd.rows) + 8 * (size_t)hd.cnt;       // to the list keys
+  auto keys_ok = [&](const char* k, int64_t m) {
+    for (int64_t e = 0; e < m; ++e) {
+      uint64_t key;
+      memcpy(&key, k + 8 * e, 8);
+      const uint64_t row = key >> 32;
+      if (row >= (uint64_t)hd.rows || (int64_t)(key & 0xffffffffULL) >= nchild[(size_t)row]) return false;
+    }
+    return true;
+  };
+  if (!keys_ok(q, hd.cnt)) return GPUGO_ERR_INVALID;
+  q += 8 * (size_t)hd.cnt;                                     // emitted boxes
+  if (!keys_ok(q, hd.nout)) return GPUGO_ERR_INVALID;
+  return GPUGO_OK;
+}
+
+// Header, problem and state of a checkpoint buffer, all checked; *rows_at is
+// where the parent rows start.  The spec points into the buffer.
+int parse_checkpoint(const void* buf, int64_t bytes, CkptHeader* hdp, gpugo_spec* sp, const char** rows_at) {
+  if (!buf || bytes < (int64_t)sizeof(CkptHeader)) return GPUGO_ERR_INVALID;
+  CkptHeader& hd = *hdp;
+  memcpy(&hd, buf, sizeof(hd));
+  // every count is bounded by the buffer before the sizes are multiplied out
+  if (memcmp(hd.magic, CKPT_MAGIC, 8) != 0 || hd.n < 1 || hd.n > 16384 || hd.rows < 1 || hd.cnt < 0 ||
+      hd.nout < 0 || hd.ntrace < 0 || hd.ncoef < 0 || hd.rows > bytes / 4 || hd.cnt > bytes / 16 ||
+      hd.nout > bytes / 16 || hd.ntrace > bytes / 32 || hd.ncoef > bytes / 8)
+    return GPUGO_ERR_INVALID;
+  const int n = hd.n;
+  const size_t total = pad8(sizeof(hd)) + 8 * (2 * (size_t)n + (size_t)hd.ncoef) + 8 * 3 * (size_t)n * hd.rows +
+                       pad8(4 * (size_t)hd.rows) + 16 * (size_t)hd.cnt + 16 * (size_t)hd.nout +
+                       32 * (size_t)hd.ntrace;
+  if ((size_t)bytes < total) return GPUGO_ERR_INVALID;
+  const char* o = (const char*)buf + pad8(sizeof(hd));
+  const double* dom = (const double*)o; o += 16 * (size_t)n;
+  const double* coef = (const double*)o; o += 8 * (size_t)hd.ncoef;
+  memset(sp, 0, sizeof(*sp));
+  sp->family = hd.family; sp->n = n; sp->wid = hd.wid; sp->group = hd.group; sp->samples = hd.samples;
+  sp->stop_mode = hd.stop_mode; sp->width_tol = hd.width_tol; sp->gap_tol = hd.gap_tol; sp->ub_init = hd.ub_init;
+  sp->domain = dom; sp->coef = coef; sp->ncoef = hd.ncoef; sp->max_iter = hd.max_iter;
+  sp->pool_cap = hd.pool_cap; sp->parent_cap = hd.parent_cap;
+  int rc = validate(sp);
+  if (rc) return rc;
+  Layout L;
+  layout(sp, 1, 0, &L);   // list and parent capacities do not depend on the output sizes
+  if (hd.rows > L.parent_cap || hd.cnt > L.pool_cap) return GPUGO_ERR_INVALID;
+  if ((rc = check_restored(*sp, hd, o))) return rc;
+  *rows_at = o;
+  return GPUGO_OK;
+}
 }  // namespace
 extern "C" {
 
@@ -2788,34 +2861,25 @@ int gpugo_checkpoint(gpugo_engine* E, int64_t ticket, void* buf, int64_t cap, in
   return GPUGO_OK;
 }
 
+int gpugo_checkpoint_check(const void* buf, int64_t bytes) {
+  CkptHeader hd;
+  gpugo_spec sp;
+  const char* o;
+  return parse_checkpoint(buf, bytes, &hd, &sp, &o);
+}
+
 int gpugo_restore(gpugo_engine* E, const void* buf, int64_t bytes, double* boxes_out, double* box_lb_out,
                   int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out) {
   NvtxRange nvtx_range("gpugo_restore");
-  if (!E || !buf || bytes < (int64_t)sizeof(CkptHeader)) return GPUGO_ERR_INVALID;
+  if (!E) return GPUGO_ERR_INVALID;
   CkptHeader hd;
-  memcpy(&hd, buf, sizeof(hd));
-  if (memcmp(hd.magic, CKPT_MAGIC, 8) != 0 || hd.n < 1 || hd.rows < 1 || hd.cnt < 0 || hd.nout < 0 ||
-      hd.ntrace < 0 || hd.ncoef < 0)
-    return GPUGO_ERR_INVALID;
-  const int n = hd.n;
-  const size_t total = pad8(sizeof(hd)) + 8 * (2 * (size_t)n + (size_t)hd.ncoef) + 8 * 3 * (size_t)n * hd.rows +
-                       pad8(4 * (size_t)hd.rows) + 16 * (size_t)hd.cnt + 16 * (size_t)hd.nout +
-                       32 * (size_t)hd.ntrace;
-  if ((size_t)bytes < total) return GPUGO_ERR_INVALID;
-  const char* o = (const char*)buf + pad8(sizeof(hd));
-  const double* dom = (const double*)o; o += 16 * (size_t)n;
-  const double* coef = (const double*)o; o += 8 * (size_t)hd.ncoef;
   gpugo_spec sp;
-  memset(&sp, 0, sizeof(sp));
-  sp.family = hd.family; sp.n = n; sp.wid = hd.wid; sp.group = hd.group; sp.samples = hd.samples;
-  sp.stop_mode = hd.stop_mode; sp.width_tol = hd.width_tol; sp.gap_tol = hd.gap_tol; sp.ub_init = hd.ub_init;
-  sp.domain = dom; sp.coef = coef; sp.ncoef = hd.ncoef; sp.max_iter = hd.max_iter; sp.pool_cap = hd.pool_cap;
-  sp.parent_cap = hd.parent_cap;
-  int rc = validate(&sp);
+  const char* o;
+  int rc = parse_checkpoint(buf, bytes, &hd, &sp, &o);
   if (rc) return rc;
+  const int n = hd.n;
   Layout L;
   layout(&sp, cap, trace ? trace->cap : 0, &L);
-  if (hd.rows > L.parent_cap || hd.cnt > L.pool_cap) return GPUGO_ERR_INVALID;
   std::vector<Piece> pcs;
   auto take = [&](int64_t rel, size_t b, size_t advance) {
     if (b) pcs.push_back(Piece{(size_t)rel, o, b});

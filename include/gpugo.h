@@ -237,6 +237,13 @@ int gpugo_checkpoint(gpugo_engine* eng, int64_t ticket, void* buf, int64_t cap, 
 int gpugo_restore(gpugo_engine* eng, const void* buf, int64_t bytes, double* boxes_out, double* box_lb_out,
                   int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out);
 
+/* The checks gpugo_restore makes before it admits anything, on the host and
+   without a device: the problem, the state (status, cycle, iteration and row
+   count, counters) and every parent row and child code the lists hold.
+   GPUGO_OK or GPUGO_ERR_INVALID.  For checkpoints kept in files or sent
+   between processes; no counterpart in the reference. */
+int gpugo_checkpoint_check(const void* buf, int64_t bytes);
+
 /* Free bytes of the engine's arena (admission control). */
 int gpugo_engine_free_bytes(gpugo_engine* eng, int64_t* free_out);
 

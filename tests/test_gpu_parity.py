@@ -346,7 +346,9 @@ def test_checkpoint_rejects_unadmitted_and_bad_data():
         assert err.value.code == -7
         e.run(1)
         data = bytearray(e.checkpoint(t))
+        assert G.checkpoint_ok(bytes(data))       # a real checkpoint passes the host checks
         data[0] ^= 0xFF                           # corrupt the magic
+        assert not G.checkpoint_ok(bytes(data))
         with pytest.raises(G.GpugoError) as err:
             e.restore(p, bytes(data))
         assert err.value.code == -1
