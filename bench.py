@@ -188,7 +188,7 @@ def run_gpugo(args, dist):
     for _ in range(args.warmup):
         G.solve(p, box_cap=4)
     torch.cuda.synchronize()
-    e2e_s, e2e_boxes, h2d, d2h = 0.0, 0, 0, 0
+    e2e_s, e2e_boxes = 0.0, 0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -196,7 +196,6 @@ def run_gpugo(args, dist):
         r = G.solve(p, box_cap=4)
         e2e_s += time.perf_counter() - t0
         e2e_boxes += r.boxes_bounded
-        h2d += r.h2d_bytes if hasattr(r, "h2d_bytes") else 0
     # bytes per step from the raw result struct
     s_spec, keep = G._spec(p)
     res = _lib.Result()
