@@ -85,7 +85,10 @@ class GpugoError(RuntimeError):
 
 
 def path() -> str:
-    return _build.LIB
+    """The library loaded: the in-tree build, or another build of the same
+    source named by GPUGO_LIB (e.g. the host-sanitizer build of
+    ``build.build_host_asan``)."""
+    return os.environ.get("GPUGO_LIB") or _build.LIB
 
 
 def load(build_if_missing: bool = False) -> ctypes.CDLL:
@@ -93,7 +96,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     global _lib
     if _lib is not None:
         return _lib
-    p = _build.LIB
+    p = path()
     if build_if_missing and not os.path.exists(p):
         _build.build()
     if not os.path.exists(p):

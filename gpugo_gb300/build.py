@@ -55,5 +55,22 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+def build_host_asan() -> str:
+    """The same library with its host code under AddressSanitizer, for the tests
+    of the host-side checks (code lists, checkpoints, arguments) that run without
+    a GPU.  The device code is left as PTX (no ptxas pass), which keeps the build
+    short; load it with GPUGO_LIB=<path> and LD_PRELOAD=<gcc's libasan.so>."""
+    out = os.path.join(OUT_DIR, "asan", "libgpugo.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    cmd = [nvcc(), "-gencode=arch=compute_103a,code=compute_103a", "-O1", "-g", "-std=c++17", "--fmad=false",
+           "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math,-fsanitize=address,-fno-omit-frame-pointer",
+           "-o", out] + [os.path.join(CSRC, f) for f in SOURCES]
+    subprocess.run(cmd, check=True)
+    return out
+
+
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--host-asan" in sys.argv:
+        print(build_host_asan())
+    else:
+        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -51,8 +51,12 @@ def test_instance_bytes_validates(lib):
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     from gpugo_gb300 import _lib, build
+    monkeypatch.delenv("GPUGO_LIB", raising=False)
     monkeypatch.setattr(build, "LIB", str(tmp_path / "absent.so"))
     monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError):
+        _lib.load()
+    monkeypatch.setenv("GPUGO_LIB", str(tmp_path / "other.so"))   # a named build that is not there
     with pytest.raises(ImportError):
         _lib.load()
 
