@@ -1095,7 +1095,8 @@ static void eval_child(const oc_spec* sp, const consts* c, const child_t* ch, iv
 static int validate(const oc_spec* sp)
 {
     if (sp->n < 1 || sp->n > 16384) return -2;
-    if (sp->wid < 2 || sp->group < 1 || sp->samples < 1) return -2;
+    if (sp->wid < 2 || sp->group < 1 || sp->samples < 1 || sp->samples > 255) return -2;  /* 8-bit sample index */
+    if (sp->stop_mode != STOP_WIDTH && sp->stop_mode != STOP_GAP) return -2;
     if (!sp->domain) return -2;
     int g = sp->group < sp->n ? sp->group : sp->n;
     double m = pow((double)sp->wid, (double)g);

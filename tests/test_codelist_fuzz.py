@@ -1,4 +1,5 @@
-"""The library's code-list checks against the oracle's, on randomly damaged arrays.
+"""The library's input checks against the oracle's: code lists with damaged
+words, and problem descriptions with limits crossed.
 
 The device interpreter checks no index: ``gpugo_instance_bytes`` (and every
 entry point that takes a problem) must reject each array the interpreter could
@@ -91,3 +92,60 @@ def test_library_and_oracle_accept_the_same_arrays(lib, oracle_lib, seed):
         accepted += lib_ok
     # both kinds of outcome are exercised
     assert 500 < accepted < 4500
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_library_and_oracle_accept_the_same_specs(lib, oracle_lib, seed):
+    """Problem descriptions of the four built-in families with limits crossed
+    (dimension, split, samples, stop rule, coefficient count and signs, empty or
+    NaN domain intervals): the library and the oracle accept the same ones.  One
+    limit is the library's own: the chained family's gradient table holds wid^3
+    entries per coordinate, so it takes at most 64 parts (the oracle has no
+    tables)."""
+    from gpugo_gb300 import _spec
+    rng = np.random.default_rng(0x73706563 + seed)
+    need = {P.COSQUAD: lambda n: 3 * n, P.CHAINED: lambda n: 2 * n - 2, P.EXPSQRT: lambda n: 2 + n,
+            P.PRODCOS: lambda n: 1}
+    accepted = 0
+    for t in range(1500):
+        # a valid description, then zero to two fields moved to a boundary value
+        fam = int(rng.integers(1, 5))
+        n = int(rng.integers(2, 64))
+        wid, group, samples, stop = int(rng.integers(2, 6)), int(rng.integers(1, 11)), 10, 1
+        for _ in range(int(rng.integers(0, 3))):
+            f = int(rng.integers(6))
+            if f == 0:
+                fam = int(rng.choice([0, 5, 6, 1, 2]))
+            elif f == 1:
+                n = int(rng.choice([1, 2, 3, 50, 16384, 16385]))
+            elif f == 2:
+                wid = int(rng.choice([0, 1, 2, 64, 65, 65536]))
+            elif f == 3:
+                group = int(rng.choice([-1, 0, 1, 32, 33]))
+            elif f == 4:
+                samples = int(rng.choice([-1, 0, 1, 255, 256]))
+            else:
+                stop = int(rng.choice([-1, 0, 2]))
+        ncoef = max(0, need.get(fam, lambda n: 4)(n) + int(rng.choice([0, 0, 0, -1, 1])))
+        dom = np.tile([-1.0, 2.0], n)
+        if rng.random() < 0.1:
+            j = int(rng.integers(n))
+            dom[2 * j], dom[2 * j + 1] = 2.0, -1.0
+        if rng.random() < 0.05:
+            dom[int(rng.integers(2 * n))] = np.nan
+        coef = rng.uniform(0.5, 2.0, ncoef) * (-1.0 if rng.random() < 0.05 else 1.0)
+        p = P.Problem(fam, n, dom, coef, wid=wid, group=group, samples=samples, stop_mode=stop)
+        s, keep = _spec(p)
+        nbytes = ctypes.c_int64(0)
+        lib_ok = lib.gpugo_instance_bytes(ctypes.byref(s), ctypes.byref(nbytes)) == 0
+        try:
+            oracle_lib.eval_children(p, p.domain, 1, np.zeros(1, dtype=np.uint64), 1e300)
+            oracle_ok = True
+        except ValueError:
+            oracle_ok = False
+        if fam == P.CHAINED and wid > 64 and oracle_ok:
+            assert not lib_ok
+            continue
+        assert lib_ok == oracle_ok, (t, fam, n, wid, group, samples, stop, ncoef)
+        accepted += lib_ok
+    assert 300 < accepted < 1300
