@@ -2637,6 +2637,10 @@ int admit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* bo
   if (!E) return GPUGO_ERR_INVALID;
   int rc = validate(spec);
   if (rc) return rc;
+  // output sizes become device allocations: bounded before they are multiplied out
+  if (cap > (1LL << 40) || (trace && trace->cap > (1LL << 40))) return GPUGO_ERR_INVALID;
+  if (trace && trace->cap > 0 && (!trace->ub || !trace->n_surv || !trace->pool || !trace->sel))
+    return GPUGO_ERR_INVALID;
   int slot = -1;
   for (int s = 0; s < E->max_slots; ++s) if (!E->slots[s].used) { slot = s; break; }
   if (slot < 0) return GPUGO_ERR_BUSY;
@@ -3210,6 +3214,9 @@ int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, do
   if (!res) return GPUGO_ERR_INVALID;
   int rc = validate(spec);
   if (rc) return rc;
+  if (cap > (1LL << 40) || (trace && trace->cap > (1LL << 40))) return GPUGO_ERR_INVALID;
+  if (trace && trace->cap > 0 && (!trace->ub || !trace->n_surv || !trace->pool || !trace->sel))
+    return GPUGO_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_mu);
   Layout L;
   layout(spec, cap, trace ? trace->cap : 0, &L);

@@ -136,6 +136,10 @@ def test_null_arguments_are_rejected_before_the_device(lib):
     assert lib.gpugo_poll(None, None, 0, ctypes.byref(n_done)) == INVALID
     assert lib.gpugo_run(None, 1, None) == INVALID
     assert lib.gpugo_solve(ctypes.byref(s), None, None, None, 0, None, None) == INVALID
+    res = G._lib.Result()
+    assert lib.gpugo_solve(ctypes.byref(s), ctypes.byref(res), None, None, (1 << 40) + 1, None, None) == INVALID
+    tr = G._lib.Trace(16, None, None, None, None)          # rows promised, no arrays
+    assert lib.gpugo_solve(ctypes.byref(s), ctypes.byref(res), None, None, 4, None, ctypes.byref(tr)) == INVALID
     nr = ctypes.c_int64()
     assert lib.gpugo_combine(None, 3, 2, 1e-3, None, 0, ctypes.byref(nr)) == INVALID
     assert lib.gpugo_combine(out.ctypes.data_as(dp), 1, 2, -1.0, None, 0, ctypes.byref(nr)) == INVALID
