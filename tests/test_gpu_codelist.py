@@ -213,3 +213,29 @@ def test_children_match_reference_1000_variable_scripts(oracle_lib, name):
         lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, cy, codes, ub)
         lb_g, s_g, f_g = G.eval_children(p, pbox, cy, codes, ub)
         assert _same(lb_g, lb_o) and _same(s_g, s_o) and np.array_equal(f_g, f_o)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_objectives_match_oracle(oracle_lib, seed):
+    """Random objectives of the front end (the generator of
+    test_codelist_random: sums over one or two offsets, a fixed coordinate or an
+    inner reduction inside a body, products, derived gradients): children and a
+    bounded solve bit for bit against the oracle's interpreter."""
+    import test_codelist_random as R
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(2, 6))
+    f = R._objective(rng, n)
+    p = P.Problem(P.CODELIST, n, np.tile([-2.0, 2.5], n), CL.compile_objective(f, n, "auto").coef, wid=3,
+                  group=n, samples=4, max_iter=150)
+    codes = np.arange(3 ** n, dtype=np.uint64)
+    for t in range(3):
+        w = 4.5 * 10.0 ** rng.uniform(-4, -0.3, n)
+        c = rng.uniform(-2.0, 2.5 - w)
+        pbox = np.empty(2 * n)
+        pbox[0::2], pbox[1::2] = c, c + w
+        lb_o, _, _, _ = oracle_lib.eval_children(p, pbox, 1, codes, 1e300)
+        ub = float(np.quantile(lb_o, 0.5))
+        lb_o, s_o, f_o, _ = oracle_lib.eval_children(p, pbox, 1, codes, ub)
+        lb_g, s_g, f_g = G.eval_children(p, pbox, 1, codes, ub)
+        assert _same(lb_g, lb_o) and _same(s_g, s_o) and np.array_equal(f_g, f_o), (seed, t)
+    _compare(p, oracle_lib)
