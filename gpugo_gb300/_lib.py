@@ -20,7 +20,7 @@ ERRORS = {
 }
 CERTIFIED, FINISHED, ITER_LIMIT = 1, 2, 3
 CAND_AUTO, CAND_WARP, CAND_LANE = 0, 1, 2
-ERR_BUSY = -7
+ERR_INVALID, ERR_BUSY = -1, -7
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)

@@ -5,7 +5,10 @@ is admitted into the resident engine as soon as a slot and enough box-pool memor
 are free (``Engine.submit`` refuses otherwise); every resident solve keeps its
 list and UB on the device and advances inside the same persistent kernel; the
 kernel returns every ``slice_iters`` iterations so that finished solves are
-collected and waiting requests join the running batch.
+collected and waiting requests join the running batch.  A request the library
+refuses (an invalid description) or one too large for the empty engine is
+answered with its error (``RequestRecord.error``) and the stream goes on; a
+device or CUDA failure ends the run.
 
 The reference has no serving mode: each script solves one problem
 (GPUGO_1.1/1-Ackley/ackley50.py:950-1396).
@@ -29,6 +32,7 @@ class RequestRecord:
     admitted: float = -1.0
     finished: float = -1.0
     result: SolveResult | None = None
+    error: str | None = None       # why the request was refused (then result is None)
 
     @property
     def latency(self) -> float:
@@ -44,12 +48,14 @@ class ServeReport:
     engine_iterations: int
     boxes: int = 0
     certified: int = 0
+    rejected: int = 0
     p50_ms: float = 0.0
     p99_ms: float = 0.0
     extra: dict = field(default_factory=dict)
 
     def summary(self) -> dict:
-        return {"requests": len(self.records), "certified": self.certified, "wall_s": self.wall_s,
+        return {"requests": len(self.records), "certified": self.certified, "rejected": self.rejected,
+                "wall_s": self.wall_s,
                 "device_s": self.device_s, "boxes": self.boxes, "boxes_per_s": self.boxes / self.wall_s,
                 "p50_ms": self.p50_ms, "p99_ms": self.p99_ms, "kernel_launches": self.launches,
                 "engine_iterations": self.engine_iterations, **self.extra}
@@ -74,13 +80,27 @@ def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_byte
         while nxt < len(records) and stream[nxt][0] <= now:
             pending.append(nxt)
             nxt += 1
-        # admit in arrival order while slots and pool memory last
+        # admit in arrival order while slots and pool memory last; a request the
+        # library refuses (a bad description) or that cannot fit even an empty
+        # engine is answered with its error and the stream goes on
         while pending:
             i = pending[0]
-            t = eng.submit(stream[i][1], box_cap=box_cap)
+            try:
+                t = eng.submit(stream[i][1], box_cap=box_cap)
+            except _lib.GpugoError as e:
+                if e.code != _lib.ERR_INVALID:      # a device or CUDA failure ends the run
+                    raise
+                t, records[i].error = None, str(e)
+            except ValueError as e:                 # arrays of the wrong size
+                t, records[i].error = None, str(e)
+            if t is None and records[i].error is None and not tickets:
+                records[i].error = "does not fit an empty engine"
+            if records[i].error is not None:
+                pending.popleft()
+                records[i].finished = clock() - t0
+                done += 1
+                continue
             if t is None:
-                if not tickets:
-                    raise _lib.GpugoError(-7, f"request {i} does not fit an empty engine")
                 break
             pending.popleft()
             tickets[t] = i
@@ -103,12 +123,15 @@ def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_byte
     st1 = eng.stats()
     if own:
         eng.close()
-    lat = np.array([r.latency for r in records]) * 1e3
+    served = [r for r in records if r.result is not None]
+    lat = np.array([r.latency for r in served]) * 1e3
     rep = ServeReport(records, wall, (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
                       int(st1["kernel_launches"] - st0["kernel_launches"]),
                       int(st1["iterations"] - st0["iterations"]))
-    rep.boxes = sum(r.result.boxes_bounded for r in records)
-    rep.certified = sum(r.result.certified for r in records)
-    rep.p50_ms = float(np.percentile(lat, 50))
-    rep.p99_ms = float(np.percentile(lat, 99))
+    rep.boxes = sum(r.result.boxes_bounded for r in served)
+    rep.certified = sum(r.result.certified for r in served)
+    rep.rejected = len(records) - len(served)
+    if served:
+        rep.p50_ms = float(np.percentile(lat, 50))
+        rep.p99_ms = float(np.percentile(lat, 99))
     return rep

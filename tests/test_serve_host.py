@@ -86,3 +86,47 @@ def test_solve_all_admits_by_shape_and_returns_input_order():
     fake2 = FakeEngine(slots=7, iters=3)
     G.Engine.solve_all(fake2, probs, iters_per_run=1, group_by_shape=False)
     assert fake2.admit_order == [p.tag for p in probs]
+
+
+class PickyEngine(FakeEngine):
+    """Refuses problems tagged "bad" like the library refuses an invalid
+    description, and never has room for problems tagged "huge"."""
+
+    def submit(self, p, box_cap=4):
+        import gpugo_gb300 as G
+        if p.tag.startswith("bad"):
+            raise G.GpugoError(-1, "gpugo_submit")
+        if p.tag.startswith("huge"):
+            return None
+        return super().submit(p, box_cap)
+
+
+def test_refused_requests_are_answered_and_the_stream_goes_on():
+    """Host-side fault injection: an invalid request and one that cannot fit an
+    empty engine are answered with their error; every other request is served
+    in arrival order and the latency figures cover the served ones only."""
+    tags = ["q0", "bad1", "q2", "q3", "huge4", "q5", "bad6", "q7"]
+    stream = [(0.0005 * i, P.instance(P.COSQUAD, 2, i, tag=t)) for i, t in enumerate(tags)]
+    eng = PickyEngine(slots=2, iters=2)
+    rep = serve(stream, engine=eng, clock=FakeClock())
+    served = [r for r in rep.records if r.result is not None]
+    assert [r.result.tag for r in served] == ["q0", "q2", "q3", "q5", "q7"]
+    assert eng.admit_order == ["q0", "q2", "q3", "q5", "q7"]
+    refused = {r.index: r.error for r in rep.records if r.result is None}
+    assert set(refused) == {1, 4, 6}
+    assert "invalid" in refused[1] and "empty engine" in refused[4]
+    assert rep.rejected == 3 and rep.certified == 5 and rep.summary()["rejected"] == 3
+    assert rep.p99_ms >= rep.p50_ms > 0
+
+
+def test_device_failure_in_admission_is_not_swallowed():
+    import pytest
+    import gpugo_gb300 as G
+
+    class Broken(FakeEngine):
+        def submit(self, p, box_cap=4):
+            raise G.GpugoError(-2, "gpugo_submit")
+
+    stream = [(0.0, P.instance(P.COSQUAD, 2, 1, tag="q0"))]
+    with pytest.raises(G.GpugoError):
+        serve(stream, engine=Broken(slots=2, iters=1), clock=FakeClock())
