@@ -157,3 +157,24 @@ def test_python_side_checks_array_sizes(lib):
     q = G.config2()
     with pytest.raises(ValueError):
         G.eval_children(q, q.domain[:6], 1, np.zeros(2, dtype=np.uint64), 1e300)
+
+
+def test_integration_binding_matches_the_library(lib, monkeypatch):
+    """The ctypes binding shown to reference maintainers
+    declares the same structures as the library, and its rastrigin50.py spec
+    passes the library's checks (the solve itself needs a GPU)."""
+    import gpugo_gb300 as G
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = text.split("## 2. Python binding", 1)[1].split("```python", 1)[1].split("```", 1)[0]
+    setup = block.split("rc = lib.gpugo_solve", 1)[0]
+    monkeypatch.chdir(ROOT)
+    ns = {}
+    exec(compile(setup, "INTEGRATION.md", "exec"), ns)
+    for mine, theirs in ((ns["Spec"], G._lib.Spec), (ns["Result"], G._lib.Result)):
+        assert ctypes.sizeof(mine) == ctypes.sizeof(theirs)
+        assert [f[0] for f in mine._fields_] == [f[0] for f in theirs._fields_]
+        for (a, ta), (b, tb) in zip(mine._fields_, theirs._fields_):
+            assert getattr(mine, a).offset == getattr(theirs, b).offset, a
+    out = ctypes.c_int64()
+    assert lib.gpugo_instance_bytes(ctypes.cast(ctypes.byref(ns["spec"]), ctypes.POINTER(G._lib.Spec)),
+                                    ctypes.byref(out)) == 0 and out.value > 0
