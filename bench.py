@@ -115,6 +115,12 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # FP64 work model of the executed path (used for the roofline numerator)
 # ---------------------------------------------------------------------------
+# dram__bytes_read.sum + dram__bytes_write.sum of one solve_kernel launch of this
+# workload, from an `ncu --set full` capture of `bench.py --steps 2 --warmup 1`
+# (its summary is kept under profiles/)
+SOLVE_DRAM_BYTES = 226.8e3 + 6.1e3
+
+
 def fp64_ops_chained(p, iterations: int, bounded: int, sampled: int) -> float:
     """FP64 instructions the chained-family path executes (DADD/DMUL/DFMA/DDIV
     each counted as one; the reference's per-child code list is not re-run).
@@ -224,7 +230,10 @@ def run_gpugo(args, dist):
                 "d2h_bytes_per_step": int(res.d2h_bytes), "ms_per_step": 1e3 * e2e_t / args.steps},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                     "frac": achieved / peak.value if peak.value else None,
+                     # DRAM bytes of this launch (read + write) from the committed ncu capture of the
+                     # same command: the working set stays in L2
+                     "traffic": SOLVE_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu)",
                      "peak_source": "measured in this run: DFMA chains on all SMs (gpugo_fp64_peak), FMA=2 flops",
                      "numerator": "FP64 instructions of the executed path (bench.fp64_ops_chained), as flops"},
         "clocks": clk,
