@@ -3120,63 +3120,86 @@ int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_d
 }  // extern "C"
 
 // The only working memory of gpugo_eval_children_static.  In host code this name
-// is a stand-in, not a device address: the address is looked up once per device.
+// is a stand-in, not a device address: each call looks the address up.
 static __device__ __align__(256) unsigned char g_static_scratch[GPUGO_STATIC_SCRATCH_BYTES];
 
 namespace {
 std::mutex g_static_mu;
-constexpr int MAX_DEVICES = 64;
-void* g_static_ptr[MAX_DEVICES] = {};
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Checks both eval_children entry points make on the host, before any device
+// call: the problem, the pointers, the cycle, the code count, and every child
+// code against the children of the cycle (compared unsigned: a code is an index
+// in [0, wid^g); a packed code of a larger value would yield digits >= wid).
+int check_eval_args(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes, int64_t m,
+                    const double* lb_out, const double* samp_out, const int32_t* flag_out) {
+  int rc = validate(spec);
+  if (rc) return rc;
+  if (!parent_box || m < 0 || m > (1LL << 40) || (m > 0 && (!codes || !lb_out || !samp_out || !flag_out)) ||
+      cyc < 1 || cyc > spec->n)
+    return GPUGO_ERR_INVALID;
+  const uint64_t M = (uint64_t)children_host(spec, cyc);
+  for (int64_t t = 0; t < m; ++t)
+    if (codes[t] >= M) return GPUGO_ERR_INVALID;
+  return GPUGO_OK;
+}
+
+// Byte offsets of gpugo_eval_children_static's scratch:
+// descriptor | instance region | codes | lb | samp | flag
+struct StaticLayout {
+  Layout L;
+  size_t o_desc, o_inst, o_codes, o_lb, o_samp, o_flag, total;
+};
+
+void static_layout(const gpugo_spec* spec, int64_t m, StaticLayout* S) {
+  gpugo_spec s2 = *spec;
+  s2.pool_cap = 1;
+  s2.parent_cap = 1;
+  layout(&s2, 1, 0, &S->L);
+  S->o_desc = 0;
+  S->o_inst = align256(sizeof(Desc));
+  S->o_codes = S->o_inst + align256((size_t)S->L.bytes);
+  S->o_lb = S->o_codes + align256(8 * (size_t)m);
+  S->o_samp = S->o_lb + align256(8 * (size_t)m);
+  S->o_flag = S->o_samp + align256(8 * (size_t)m);
+  S->total = S->o_flag + align256(4 * (size_t)m);
+}
 }  // namespace
 
 extern "C" {
 
 int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes,
                                int64_t m, double ub, double* lb_out, double* samp_out, int32_t* flag_out) {
+  // every check is made on the host before the device is touched; an oversize
+  // request is refused before its codes are scanned
   int rc = validate(spec);
   if (rc) return rc;
-  if (!parent_box || (m > 0 && (!codes || !lb_out || !samp_out || !flag_out)) || m < 0 || cyc < 1 || cyc > spec->n)
-    return GPUGO_ERR_INVALID;
+  if (m < 0 || m > (1LL << 40)) return GPUGO_ERR_INVALID;
+  StaticLayout S;
+  static_layout(spec, m, &S);
+  if (S.total > GPUGO_STATIC_SCRATCH_BYTES) return GPUGO_ERR_SCRATCH_LIMIT;
+  if ((rc = check_eval_args(spec, parent_box, cyc, codes, m, lb_out, samp_out, flag_out))) return rc;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
-  const int64_t M = children_host(spec, cyc);
-  for (int64_t t = 0; t < m; ++t) if ((int64_t)codes[t] >= M) return GPUGO_ERR_INVALID;
+
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  // the array's device address in the context current now (looked up on every
+  // call: a cudaDeviceReset or another context since the last call moves it)
+  void* sp = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&sp, g_static_scratch);
+  if (e != cudaSuccess || !sp) return cuda_err(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
+  char* base = (char*)sp;
+  Desc* d_desc = (Desc*)(base + S.o_desc);
+  unsigned long long* d_codes = (unsigned long long*)(base + S.o_codes);
+  double* d_lb = (double*)(base + S.o_lb);
+  double* d_samp = (double*)(base + S.o_samp);
+  int* d_flag = (int*)(base + S.o_flag);
   gpugo_spec s2 = *spec;
   s2.pool_cap = 1;
   s2.parent_cap = 1;
-  Layout L;
-  layout(&s2, 1, 0, &L);
-  // scratch layout: descriptor | instance region | codes | lb | samp | flag
-  const size_t o_desc = 0;
-  const size_t o_inst = align256(sizeof(Desc));
-  const size_t o_codes = o_inst + align256((size_t)L.bytes);
-  const size_t o_lb = o_codes + align256(8 * (size_t)m);
-  const size_t o_samp = o_lb + align256(8 * (size_t)m);
-  const size_t o_flag = o_samp + align256(8 * (size_t)m);
-  const size_t total = o_flag + align256(4 * (size_t)m);
-  if (total > GPUGO_STATIC_SCRATCH_BYTES) return GPUGO_ERR_SCRATCH_LIMIT;
-
-  std::lock_guard<std::mutex> lock(g_static_mu);
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= MAX_DEVICES) return GPUGO_ERR_INVALID;
-  if (!g_static_ptr[dev]) {
-    // set-up, once per device, with that device current
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess || !p) return cuda_err(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
-    g_static_ptr[dev] = p;
-  }
-  char* base = (char*)g_static_ptr[dev];
-  Desc* d_desc = (Desc*)(base + o_desc);
-  unsigned long long* d_codes = (unsigned long long*)(base + o_codes);
-  double* d_lb = (double*)(base + o_lb);
-  double* d_samp = (double*)(base + o_samp);
-  int* d_flag = (int*)(base + o_flag);
   Desc D;
-  fill_desc(&s2, L, base + o_inst, &D);
+  fill_desc(&s2, S.L, base + S.o_inst, &D);
   CK(cudaMemcpy((void*)D.dom, spec->domain, 8 * 2 * spec->n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy((void*)D.coef, spec->coef, 8 * spec->ncoef, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.parents, parent_box, 8 * 2 * spec->n, cudaMemcpyHostToDevice));
@@ -3184,7 +3207,7 @@ int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box,
   if (m > 0) CK(cudaMemcpy(d_codes, codes, 8 * m, cudaMemcpyHostToDevice));
   eval_init_kernel<<<1, 32>>>(d_desc);
   CK(cudaGetLastError());
-  const int blocks = (int)std::min<int64_t>((L.a_items + 255) / 256, 4096);
+  const int blocks = (int)std::min<int64_t>((S.L.a_items + 255) / 256, 4096);
   eval_tables_kernel<<<std::max(blocks, 1), 256>>>(d_desc, cyc);
   CK(cudaGetLastError());
   if (m > 0) {
@@ -3265,14 +3288,10 @@ int gpugo_solve(const gpugo_spec* spec, gpugo_result* res, double* boxes_out, do
 int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_t cyc, const uint64_t* codes,
                         int64_t m, double ub, double* lb_out, double* samp_out, int32_t* flag_out) {
   NvtxRange nvtx_range("gpugo_eval_children");
-  int rc = validate(spec);
+  int rc = check_eval_args(spec, parent_box, cyc, codes, m, lb_out, samp_out, flag_out);
   if (rc) return rc;
-  if (!parent_box || (m > 0 && (!codes || !lb_out || !samp_out || !flag_out)) || m < 0 || cyc < 1 || cyc > spec->n)
-    return GPUGO_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
-  int64_t M = children_host(spec, cyc);
-  for (int64_t t = 0; t < m; ++t) if ((int64_t)codes[t] >= M) return GPUGO_ERR_INVALID;
   gpugo_spec s2 = *spec;
   s2.pool_cap = 1;
   s2.parent_cap = 1;

@@ -156,14 +156,18 @@ int gpugo_eval_children(const gpugo_spec* spec, const double* parent_box, int32_
  * process exits.  Inputs and outputs are host buffers, as for gpugo_eval_children.
  *
  * Limit: a request whose term tables plus 28 bytes per child code exceed the
- * scratch returns GPUGO_ERR_SCRATCH_LIMIT (the 8-variable chained instance with
- * wid = 4 fits about 290 000 child codes per call).  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current; make
- * it before any stream capture.  The array is shared by all calls and keeps the
- * last call's contents; nothing in it has to start at zero because every value a
- * call reads is written earlier in the same call.  Calls are serialised by a host
- * lock inside the library; two calls running on the GPU at the same time (for
- * example from two loaded copies of the library) would race on the array.
+ * scratch returns GPUGO_ERR_SCRATCH_LIMIT, checked on the host before anything
+ * else is done (the 8-variable chained instance with wid = 4 fits 296 672 child
+ * codes per call).  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the context current at the call, so the address
+ * stays right after a cudaDeviceReset or under another context.  The first call
+ * on a device also loads the library's device code there; make it before any
+ * stream capture.  The array is shared by every call through one loaded copy
+ * of the library on that device and keeps the last call's contents; nothing in
+ * it has to start at zero because every value a call reads is written earlier
+ * in the same call.  Calls that overlapped on the GPU would race on the array:
+ * the library prevents that with a lock that each call holds until its results
+ * are back in the caller's host buffers.
  */
 #define GPUGO_STATIC_SCRATCH_BYTES (8u << 20)
 int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box, int32_t cyc,

@@ -178,3 +178,61 @@ def test_integration_binding_matches_the_library(lib, monkeypatch):
     out = ctypes.c_int64()
     assert lib.gpugo_instance_bytes(ctypes.cast(ctypes.byref(ns["spec"]), ctypes.POINTER(G._lib.Spec)),
                                     ctypes.byref(out)) == 0 and out.value > 0
+
+
+def _eval_rc(lib, fn, p, codes, cyc=1):
+    import numpy as np
+    import gpugo_gb300 as G
+    s, keep = G._spec(p)
+    codes = np.ascontiguousarray(codes, dtype=np.uint64)
+    m = codes.size
+    out = np.zeros(max(m, 1))
+    flags = np.zeros(max(m, 1), dtype=np.int32)
+    dp = ctypes.POINTER(ctypes.c_double)
+    return getattr(lib, fn)(ctypes.byref(s), p.domain.ctypes.data_as(dp), cyc,
+                            codes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), m, 1e300,
+                            out.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                            flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+
+
+# Largest child-code count gpugo_eval_children_static takes for the 8-variable
+# chained instance (wid 4): its descriptor, instance region and 28 bytes per code
+# in 256-byte aligned pieces fill the 8 MiB scratch.
+STATIC_MAX_CODES_CHAINED8 = 296_672
+
+
+def test_child_codes_are_checked_unsigned_before_the_device(lib):
+    """A child code is an index in [0, wid^g).  Codes of 2^63 and above (negative
+    as signed integers) and codes at wid^g are refused by both eval entry
+    points with GPUGO_ERR_INVALID, on the host, before the device is queried
+    (the reference refuses indices outside its child grid, ackley50.py:532-540).
+    wid = 3 is not a power of two: there the digit packing of an out-of-range
+    code would give digits >= wid."""
+    import gpugo_gb300 as G
+    from gpugo_gb300 import problems as P
+    INVALID = -1
+    q = P.instance(P.COSQUAD, 5, 3, split=(3, 5))
+    M = 3 ** 5
+    for fn in ("gpugo_eval_children", "gpugo_eval_children_static"):
+        for bad in (1 << 63, (1 << 64) - 1, M, 1 << 32):
+            assert _eval_rc(lib, fn, q, [0, bad, 1]) == INVALID, (fn, bad)
+        assert _eval_rc(lib, fn, q, [0, M - 1]) != INVALID
+        # a short last cycle has fewer children: codes are checked against them
+        assert _eval_rc(lib, fn, G.config2(), [4 ** 7], cyc=2) == INVALID
+        assert _eval_rc(lib, fn, G.config2(), [4 ** 7 - 1], cyc=2) != INVALID
+
+
+def test_static_scratch_limit_is_checked_on_the_host(lib):
+    """gpugo_eval_children_static refuses a request larger than its scratch
+    (GPUGO_ERR_SCRATCH_LIMIT) before it scans the codes or queries a device;
+    the boundary is exact: one code fewer is accepted."""
+    import numpy as np
+    import gpugo_gb300 as G
+    p = G.config2()
+    m = STATIC_MAX_CODES_CHAINED8
+    assert _eval_rc(lib, "gpugo_eval_children_static", p, np.zeros(m + 1)) == -10
+    assert _eval_rc(lib, "gpugo_eval_children_static", p, np.zeros(m)) != -10
+    # an oversize request with invalid codes is still a scratch-limit refusal
+    assert _eval_rc(lib, "gpugo_eval_children_static", p, np.full(m + 1, 1 << 63)) == -10
+    # the allocating entry point has no such limit
+    assert _eval_rc(lib, "gpugo_eval_children", p, np.zeros(m + 1)) != -10

@@ -75,3 +75,25 @@ def test_static_rejects_oversize(lib):
     rc, *_ = _call(lib, "gpugo_eval_children_static", p, p.domain, 1, codes, 1e300)
     assert rc == -10
     assert lib.gpugo_strerror(rc).startswith(b"request exceeds the fixed scratch")
+
+
+def test_static_at_the_scratch_boundary(lib):
+    """The largest request that fits the scratch (every byte of the 8 MiB array
+    in use) gives the allocating entry point's results bit for bit, twice in a
+    row; one code more is refused."""
+    from test_capi import STATIC_MAX_CODES_CHAINED8 as M
+    from gpugo_gb300 import problems as P
+    p = P.config2()
+    rng = np.random.default_rng(5)
+    codes = rng.integers(0, 4 ** 8, M).astype(np.uint64)
+    rc0, lb0, s0, f0 = _call(lib, "gpugo_eval_children", p, p.domain, 1, codes, 1e300)
+    ub = float(np.quantile(lb0, 0.3))
+    rc0, lb0, s0, f0 = _call(lib, "gpugo_eval_children", p, p.domain, 1, codes, ub)
+    assert rc0 == 0
+    for _ in range(2):
+        rc1, lb1, s1, f1 = _call(lib, "gpugo_eval_children_static", p, p.domain, 1, codes, ub)
+        assert rc1 == 0
+        assert _same(lb1, lb0) and _same(s1, s0)
+        np.testing.assert_array_equal(f1, f0)
+    rc2, *_ = _call(lib, "gpugo_eval_children_static", p, p.domain, 1, np.append(codes, codes[:1]), ub)
+    assert rc2 == -10
