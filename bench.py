@@ -1,20 +1,25 @@
 """Benchmark: certified interval B&B solves on GB300.
 
-Workload (a step): one complete solve of the n=8 chained-quartic instance
-(f = sum p_i (x_{i+1} - x_i^2)^2 + q_i (1 - x_i)^2, p~U[50,150], q~U[0.5,2],
-domain [-5,10]^8, 4^8 children per iteration, stop at UB-LB <= 1e-6, seeded).
-Metric: child boxes bounded per second.
+Workload (a step, the default line): one certified solve of the whole mixed
+batch of 1024 instances -- families F1-F4 (cosine-quadratic, chained quartic,
+exp-sqrt composite, product-cosine), n log-uniform in 2..64, stop at
+UB-LB <= 1e-6, seeded -- in one persistent engine.  Metric: child boxes bounded
+per second.
 
-  value   device time of the persistent solve kernel (CUDA events on the engine
-          stream) with the problem already resident on the GPU
-  e2e     the same solve through the C ABI call gpugo_solve with host buffers,
-          host<->device copies included, wall clock
+  value   device time of the engine's persistent kernel (CUDA events on the
+          engine stream) with the problems admitted
+  e2e     the same batch through the public API (Engine.solve_all: problem
+          descriptions from host memory, results and minimiser boxes back to
+          host memory), wall clock, copies included
+  config  the plain one-instance-per-launch path on the same problems
+          (gpugo_solve in a loop: time, speed-up, identical results) and a
+          serving record: the 4096-request Poisson stream, p50/p99 latency
   cpu_baseline / --impl reference
           the CPU oracle (a C restatement of the reference B&B, OpenMP over the
-          children) on the host cores
+          children) on the host cores, on instances of the same batch
 
-Multi-GPU: replicas only (one independent solve stream per rank), max time over
-ranks, value summed over ranks.
+Multi-GPU: replicas (one batch per rank; max time over ranks, boxes summed);
+the serving record deals the arrivals round-robin over the ranks.
 """
 from __future__ import annotations
 
@@ -22,6 +27,7 @@ import argparse
 import json
 import math
 import os
+import re
 import shutil
 import statistics
 import subprocess
@@ -32,8 +38,11 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "cfg2-chained8: n=8 chained quartic, [-5,10]^8, 4^8 children/iter, S=10, UB-LB<=1e-6"
+WORKLOAD = ("cfg4-batch1024: 1024 mixed instances (F1-F4, n log-uniform 2..64), UB-LB<=1e-6, "
+            "one persistent engine")
 METRIC = "boxes/s"
+# ncu summary of this workload's persistent kernel (FP64 instruction and DRAM counters)
+COUNTER_PROFILE = os.path.join(ROOT, "profiles", "solve_kernel_cfg4_batch1024.md")
 
 
 # ---------------------------------------------------------------------------
@@ -44,6 +53,15 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def check_gpus(requested: int) -> None:
+    """--gpus N must match the ranks the launcher started (torchrun sets
+    WORLD_SIZE); a single process never stands in for several GPUs."""
+    ws, _, _ = dist_env()
+    if requested != ws:
+        raise SystemExit(f"bench.py --gpus {requested} but WORLD_SIZE={ws}: launch N ranks with "
+                         f"python -m torch.distributed.run --nproc-per-node {requested} bench.py --gpus {requested}")
 
 
 def init_dist(backend: str):
@@ -113,263 +131,369 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# FP64 work model of the executed path (used for the roofline numerator)
+# workload and work counts
 # ---------------------------------------------------------------------------
-# dram__bytes_read.sum + dram__bytes_write.sum of one solve_kernel launch of this
-# workload, from an `ncu --set full` capture of `bench.py --steps 2 --warmup 1`
-# (its summary is kept under profiles/)
-SOLVE_DRAM_BYTES = 226.8e3 + 6.1e3
+def batch_problems(count: int = 1024):
+    """The mixed batch with the tuned fan-out table applied: every arm of the
+    benchmark (GPU batch, plain loop, CPU oracle) solves these same problems."""
+    from gpugo_gb300 import autotune as A
+    from gpugo_gb300 import problems as P
+    return A.apply_fanout(P.config4(count=count))
 
 
-def fp64_ops_chained(p, iterations: int, bounded: int, sampled: int) -> float:
-    """FP64 instructions the chained-family path executes (DADD/DMUL/DFMA/DDIV
-    each counted as one; the reference's per-child code list is not re-run).
-    Per child: n-1 directed adds (lower-bound chain).  Per sampled child: S(n-1)
-    directed adds + S compares.  Per iteration, term tables: (n-1) w^2 (S+1)
-    entries x 40 ops and n w^3 gradient entries x 45 ops."""
-    n, w, S = p.n, p.wid, p.samples
-    per_iter = (n - 1) * w * w * (S + 1) * 40 + n * w ** 3 * 45
-    return bounded * (n - 1) + sampled * S * (n - 1 + 1) + iterations * per_iter
+def serving_stream(count: int, rate: float):
+    from gpugo_gb300 import autotune as A
+    from gpugo_gb300 import problems as P
+    stream = P.config5(count=count, rate=rate)
+    return list(zip([t for t, _ in stream], A.apply_fanout([p for _, p in stream])))
+
+
+def cpu_sample(probs, k: int):
+    """Every (len/k)-th instance of the batch: the CPU legs' bounded sample."""
+    from gpugo_gb300 import autotune as A
+    return A.sample_problems(probs, k)
+
+
+T_TRANS = 20   # FP64 operations charged per transcendental endpoint evaluation (declared convention)
+
+
+def reference_flops(p, boxes: int, sampled: int) -> float:
+    """Interval FP64 operations the reference's code lists spend on `boxes`
+    children, `sampled` of which also reach the derivative list: per child the
+    value list and S sample lists, per sampled child the gradient list, with the
+    per-operation weights add/times 2, multiply 8, square 2, transcendental T."""
+    n, S, T = p.n, p.samples, T_TRANS
+    fam = int(p.family)
+    if fam == 1:
+        per, grad = n * (10 + 2 * T), n * (8 + 2 * T)
+    elif fam == 2:
+        per, grad = 18 * (n - 1), 26 * n
+    elif fam == 3:
+        per, grad = n * (10 + 2 * T) + 4 * T + 14, n * (30 + 4 * T)
+    else:
+        per, grad = n * (14 + 2 * T) + 6, n * (38 + 6 * T)
+    return float(boxes) * per * (1 + S) + float(sampled) * grad
+
+
+def profile_counters(path: str = COUNTER_PROFILE) -> dict | None:
+    """Per-box FP64 and DRAM figures of this workload's persistent kernel from
+    its ncu summary (lines `key: value` in the summary's counter block)."""
+    if not os.path.exists(path):
+        return None
+    out = {}
+    for line in open(path):
+        m = re.match(r"^\s*(fp64_thread_ops_per_box|dram_bytes_per_box|boxes_captured|fp64_pipe_active_pct)"
+                     r":\s*([0-9.eE+-]+)", line)
+        if m:
+            out[m.group(1)] = float(m.group(2))
+    return out or None
 
 
 # ---------------------------------------------------------------------------
-# arms
+# GPU arm: the batch line
 # ---------------------------------------------------------------------------
-def run_gpugo(args, dist):
+def tune_engine(probs, args):
+    """Block size and candidate scheduling picked on half the batch (work-neutral:
+    the results are identical under every configuration)."""
+    from gpugo_gb300 import autotune as A
+    if not args.autotune:
+        return A.EngineConfig(), 0.0, []
+    t0 = time.perf_counter()
+    tr = A.tune(probs, sample=min(512, len(probs)), fanout_options=(), n_classes=(),
+                timer=lambda ps, cfg: A.time_engine(ps, cfg, arena_bytes=args.arena_gb << 30))
+    return tr.engine, time.perf_counter() - t0, tr.trials
+
+
+def run_batch(args, dist):
+    import ctypes
+
     import torch
 
     import gpugo_gb300 as G
-    from gpugo_gb300 import _lib, problems as P
+    from gpugo_gb300 import _lib
+    from gpugo_gb300.serve import serve_sharded
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     L = _lib.load()
-    p = P.config2()
+    probs = batch_problems(args.count)
+    ecfg, tune_s, trials = tune_engine(probs, args)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # 256 MiB > 129 MB L2
 
-    eng = G.Engine(max_slots=1, arena_bytes=256 << 20)
+    eng = G.Engine(max_slots=len(probs), arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
+                   blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode)
+    for _ in range(args.warmup):
+        eng.solve_all(probs, box_cap=4)
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    dev_ms, wall_s, boxes, sampled = 0.0, 0.0, 0, 0
+    st_first = eng.stats()
+    res = None
+    for _ in range(args.steps):
+        flush.zero_()                      # L2 flushed between steps, outside both clocks
+        torch.cuda.synchronize()
+        st0 = eng.stats()
+        t0 = time.perf_counter()
+        res = eng.solve_all(probs, box_cap=4)
+        wall_s += time.perf_counter() - t0
+        st1 = eng.stats()
+        dev_ms += st1["total_run_ms"] - st0["total_run_ms"]
+        boxes += sum(r.boxes_bounded for r in res)
+        sampled += sum(r.samples_evaluated for r in res)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    st_last = eng.stats()
+    eng.close()
+    assert all(r.certified and r.ub - r.lb <= p.gap_tol for r, p in zip(res, probs))
+    launches = st_last["kernel_launches"] - st_first["kernel_launches"]
+    h2d = (st_last["h2d_bytes"] - st_first["h2d_bytes"]) // args.steps
+    d2h = (st_last["d2h_bytes"] - st_first["d2h_bytes"]) // args.steps
+    t_max, boxes_all = reduce_max_sum(dist, dev_ms, float(boxes), device="cuda")
+    w_max, _ = reduce_max_sum(dist, wall_s, 0.0, device="cuda")
+
+    # the plain path: the same problems, one gpugo_solve (one launch series) each
+    batch_s = wall_s / args.steps
+    plain_s = plain_dev_s = same = None
+    if args.plain:
+        for p in probs[:8]:
+            G.solve(p, box_cap=4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain = [G.solve(p, box_cap=4) for p in probs]
+        plain_s = time.perf_counter() - t0
+        plain_dev_s = sum(r.device_ms for r in plain) * 1e-3
+        same = all((a.lb, a.ub, a.iterations, a.boxes_bounded, a.status) ==
+                   (b.lb, b.ub, b.iterations, b.boxes_bounded, b.status) for a, b in zip(plain, res))
+
+    # serving: the config-5 stream, arrivals dealt over the ranks
+    serving = None
+    if args.serve_count > 0:
+        stream = serving_stream(args.serve_count, args.rate)
+        slots = min(len(stream), 2048)
+        with G.Engine(max_slots=slots, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
+                      blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as seng:
+            serving = serve_sharded(stream, dist, max_slots=slots, slice_iters=args.slice, engine=seng)
+        if serving is not None:
+            serving["workload"] = (f"cfg5-serve{args.serve_count}: Poisson {args.rate:g}/s, F1-F4, n log-uniform "
+                                   f"2..128, tol 1e-6 or 1e-4, arena {args.arena_gb} GiB, slice {args.slice}")
+
+    # roofline: FP64 throughput of the persistent kernel against a DFMA peak measured now
+    peak = ctypes.c_double()
+    pms = ctypes.c_double()
+    _lib.check(L.gpugo_fp64_peak(5, ctypes.byref(peak), ctypes.byref(pms)))
+    cnt = profile_counters()
+    sec = dev_ms * 1e-3
+    ref_fl = sum(reference_flops(p, r.boxes_bounded, r.samples_evaluated) for p, r in zip(probs, res)) * args.steps
+    roof = {"bound": "fp64", "peak": peak.value, "unit": "TFLOP/s",
+            "peak_source": "measured in this run: DFMA chains on all SMs (gpugo_fp64_peak), FMA = 2 flops; "
+                           "MEASURED_PEAKS.json has no FP64 figure",
+            "reference_equivalent_tflops": ref_fl / sec / 1e12,
+            "reference_equivalent_note": "the reference's per-child code-list work (value + S samples + gradient, "
+                                         f"add 2, mul 8, transcendental {T_TRANS}) over the same boxes: term tables "
+                                         "and sample skipping remove most of it with identical results"}
+    if cnt and cnt.get("fp64_thread_ops_per_box"):
+        ach = cnt["fp64_thread_ops_per_box"] * boxes / sec / 1e12
+        roof.update({"achieved": ach, "frac": ach / peak.value if peak.value else None,
+                     "numerator": "executed FP64 thread operations (DADD, DMUL = 1, DFMA = 2) per bounded box "
+                                  "from ncu's sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum over "
+                                  "this workload's kernel, times the boxes of this run",
+                     "traffic": cnt.get("dram_bytes_per_box", 0.0) * boxes / args.steps,
+                     "traffic_unit": "DRAM bytes per step (ncu dram__bytes_read.sum + write.sum per box x boxes)",
+                     "counter_source": os.path.relpath(COUNTER_PROFILE, ROOT)})
+    else:
+        roof.update({"achieved": None, "frac": None, "traffic": None})
+
+    out = {
+        "metric": METRIC, "value": boxes_all / (t_max * 1e-3), "unit": "boxes/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded instances, config-4 and config-5 generators)",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas{ws}",
+                   "l2": "flushed between steps (256 MiB write)",
+                   "engine": ecfg.label(), "engine_tuning_s": tune_s,
+                   "engine_trials": [{"config": t["config"], "seconds": round(t["seconds"], 4)} for t in trials],
+                   "fanout": "3 parts per coordinate: 3^5 children per iteration for n in 8..16, 3^6 above "
+                             "(the autotuner's table); n < 8 the default splits",
+                   "instances": len(probs), "certified": sum(r.certified for r in res),
+                   "boxes_per_step": boxes // args.steps, "samples_per_step": sampled // args.steps,
+                   "iterations_max": max(r.iterations for r in res),
+                   "time_to_certified_batch_ms": t_max / args.steps,
+                   "batch_wall_s": batch_s,
+                   "plain_wall_s": plain_s, "plain_device_s": plain_dev_s, "plain_launch_series": len(probs),
+                   "speedup_vs_plain": plain_s / batch_s if plain_s else None,
+                   "speedup_vs_plain_device": plain_dev_s / (sec / args.steps) if plain_dev_s else None,
+                   "identical_to_plain": same,
+                   "serving": serving},
+        "e2e": {"value": boxes_all / w_max, "unit": "boxes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * w_max / args.steps,
+                "api": "Engine.solve_all (gpugo_submit / gpugo_run / gpugo_poll), host buffers"},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk,
+    }
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU legs
+# ---------------------------------------------------------------------------
+def run_cpu_baseline(probs, k: int = 16):
+    """The oracle on every (1024/k)-th instance of the batch: once as the
+    reference computes (every child's samples evaluated), once with the GPU's
+    sample skipping (children whose LB is above the UB keep their samples
+    unevaluated; same results)."""
+    import oracle
+    oracle.build()
+    samp = cpu_sample(probs, k)
+    out = {}
+    for skip in (False, True):
+        t0 = time.perf_counter()
+        boxes = 0
+        for p in samp:
+            boxes += oracle.solve(p, box_cap=4, skip_samples=skip).boxes_bounded
+        out[skip] = (boxes / (time.perf_counter() - t0), time.perf_counter() - t0)
+    (v, dt), (v2, dt2) = out[False], out[True]
+    return {"value": v, "unit": "boxes/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{len(samp)} of the {len(probs)} batch instances (every {len(probs) // len(samp)}th), "
+                      f"complete solves in {dt:.1f} s, OpenMP over the children, every child's samples evaluated "
+                      f"as in the reference",
+            "skip_samples_value": v2,
+            "skip_samples_note": f"the same {len(samp)} solves with the GPU's sample skipping: {dt2:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's B&B on the host cores.  The reference's
+    own code is Numba CUDA and cannot run on this machine; the oracle (a C
+    restatement of its algorithm, OpenMP over the children, every child's
+    samples evaluated) stands in.  Each step solves 4 instances of the batch,
+    the steps walking through a 64-instance sample (every 16th instance)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    import oracle
+    oracle.build()
+    probs = batch_problems(args.count)
+    samp = cpu_sample(probs, 64)
+    per = 4
+    small = min(samp, key=lambda p: p.n)
+    for _ in range(args.warmup):
+        oracle.solve(small, box_cap=4, skip_samples=False)
+    t0 = time.perf_counter()
+    boxes = 0
+    for k in range(args.steps):
+        for j in range(per):
+            boxes += oracle.solve(samp[(k * per + j) % len(samp)], box_cap=4, skip_samples=False).boxes_bounded
+    dt = time.perf_counter() - t0
+    v = boxes / dt
+    sample = (f"{args.steps} steps of {per} complete solves each, walking through {len(samp)} of the "
+              f"{len(probs)} batch instances (every {len(probs) // len(samp)}th); the reference's Numba CUDA "
+              f"kernels cannot run here (numba is absent), so this is the oracle's C restatement of its B&B")
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "boxes/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded instances, config-4 generator)",
+            "config": {"workload": WORKLOAD, "parallelism": "host cores"},
+            "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": oracle.num_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------------------
+# other workloads (their own records)
+# ---------------------------------------------------------------------------
+def run_chained8(args):
+    """Config 2: one certified solve of the n=8 chained quartic (4^8 children per
+    iteration) per step, resident (engine CUDA events) and through gpugo_solve."""
     import ctypes
-    stats = _lib.Stats()
+
+    import numpy as np
+    import torch
+
+    import gpugo_gb300 as G
+    from gpugo_gb300 import _lib, problems as P
+    L = _lib.load()
+    p = P.config2()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    eng = G.Engine(max_slots=1, arena_bytes=256 << 20)
 
     def one_step():
         flush.zero_()
         torch.cuda.synchronize()
-        t = eng.submit(p, box_cap=4)
-        assert t is not None
+        assert eng.submit(p, box_cap=4) is not None
         eng.run(0)
-        _lib.check(L.gpugo_engine_stats(eng._h, ctypes.byref(stats)))
-        ms = stats.last_run_ms
+        ms = eng.stats()["last_run_ms"]
         (tk, r), = eng.poll()
         assert r.status == G.CERTIFIED and r.ub - r.lb <= p.gap_tol
         return ms, r
 
     for _ in range(args.warmup):
         one_step()
-    _lib.check(L.gpugo_engine_stats(eng._h, ctypes.byref(stats)))
-    launches0 = stats.kernel_launches
-    clocks = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    dev_ms, boxes, sampled, iters = 0.0, 0, 0, 0
-    last = None
+    dev_ms, boxes = 0.0, 0
     for _ in range(args.steps):
         ms, r = one_step()
         dev_ms += ms
         boxes += r.boxes_bounded
-        sampled += r.samples_evaluated
-        iters += r.iterations
-        last = r
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    _lib.check(L.gpugo_engine_stats(eng._h, ctypes.byref(stats)))
-    launches = stats.kernel_launches - launches0
     eng.close()
-    t_max, boxes_all = reduce_max_sum(dist, dev_ms, float(boxes), device="cuda")
-
-    # end to end through the C ABI (host buffers, copies inside)
     for _ in range(args.warmup):
         G.solve(p, box_cap=4)
-    torch.cuda.synchronize()
-    e2e_s, e2e_boxes = 0.0, 0
+    e2e_s = 0.0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = G.solve(p, box_cap=4)
+        G.solve(p, box_cap=4)
         e2e_s += time.perf_counter() - t0
-        e2e_boxes += r.boxes_bounded
-    # bytes per step from the raw result struct
-    s_spec, keep = G._spec(p)
-    res = _lib.Result()
-    import numpy as np
-    bx = np.zeros((4, 2 * p.n)); lbs = np.zeros(4); xh = np.zeros(p.n)
-    dp = ctypes.POINTER(ctypes.c_double)
-    _lib.check(L.gpugo_solve(ctypes.byref(s_spec), ctypes.byref(res), bx.ctypes.data_as(dp), lbs.ctypes.data_as(dp),
-                             4, xh.ctypes.data_as(dp), None))
-    e2e_t, e2e_all = reduce_max_sum(dist, e2e_s, float(e2e_boxes), device="cuda")
-
-    # roofline: FP64 throughput of the persistent kernel against a measured DFMA peak
     peak = ctypes.c_double()
     pms = ctypes.c_double()
     _lib.check(L.gpugo_fp64_peak(5, ctypes.byref(peak), ctypes.byref(pms)))
-    ops = fp64_ops_chained(p, iters, boxes, sampled)
-    achieved = ops / (dev_ms * 1e-3) / 1e12
-    out = {
-        "metric": METRIC, "value": boxes_all / (t_max * 1e-3), "unit": "boxes/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded instance, MASTER_SEED+2)",
-        "config": {"workload": WORKLOAD, "parallelism": f"replicas{ws}", "l2": "flushed between steps (256 MiB write)",
-                   "iterations_per_solve": last.iterations, "boxes_per_solve": last.boxes_bounded,
-                   "time_to_certified_ms": t_max / args.steps, "enclosure": [last.lb, last.ub]},
-        "e2e": {"value": e2e_all / e2e_t, "unit": "boxes/s", "h2d_bytes_per_step": int(res.h2d_bytes),
-                "d2h_bytes_per_step": int(res.d2h_bytes), "ms_per_step": 1e3 * e2e_t / args.steps},
-        "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value else None,
-                     # DRAM bytes of this launch (read + write) from the committed ncu capture of the
-                     # same command: the working set stays in L2
-                     "traffic": SOLVE_DRAM_BYTES, "traffic_unit": "bytes per launch (ncu)",
-                     "peak_source": "measured in this run: DFMA chains on all SMs (gpugo_fp64_peak), FMA=2 flops",
-                     "numerator": "FP64 instructions of the executed path (bench.fp64_ops_chained), as flops"},
-        "clocks": clk,
-    }
-    return out
-
-
-def run_cpu_baseline(seconds: float = 15.0):
-    """The oracle (C restatement of the reference B&B) on the host cores, faithful
-    mode (every child's samples evaluated, as the reference does)."""
-    import oracle
-    from gpugo_gb300 import problems as P
-    oracle.build()
-    p = P.config2()
-    t0 = time.perf_counter()
-    boxes = 0
-    solves = 0
-    while True:
-        r = oracle.solve(p, box_cap=4, skip_samples=False)
-        boxes += r.boxes_bounded
-        solves += 1
-        if time.perf_counter() - t0 > seconds:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": boxes / dt, "unit": "boxes/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"{solves} complete solves of the workload in {dt:.1f} s (OpenMP over children, "
-                      f"all sample points evaluated as in the reference)"}, solves, dt
-
-
-def run_reference(args):
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return None
-    import oracle
-    from gpugo_gb300 import problems as P
-    oracle.build()
-    p = P.config2()
-    for _ in range(args.warmup):
-        oracle.solve(p, box_cap=4, skip_samples=False)
-    t0 = time.perf_counter()
-    boxes = 0
-    for _ in range(args.steps):
-        r = oracle.solve(p, box_cap=4, skip_samples=False)
-        boxes += r.boxes_bounded
-    dt = time.perf_counter() - t0
-    v = boxes / dt
-    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "boxes/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded instance, MASTER_SEED+2)",
-            "config": {"workload": WORKLOAD, "parallelism": "host cores"},
-            "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": oracle.num_threads(), "kind": "port",
-                             "sample": f"{args.steps} complete solves (the reference's Numba CUDA kernels cannot "
-                                       f"run here: numba is absent; this is the oracle's C restatement)"},
-            "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return {"metric": METRIC, "value": boxes / (dev_ms * 1e-3), "unit": "boxes/s", "n_gpus": 1, "dtype": "f64",
+            "steps": args.steps, "ms_per_step": dev_ms / args.steps,
+            "config": {"workload": "cfg2-chained8: n=8 chained quartic, [-5,10]^8, 4^8 children/iter, S=10, "
+                                   "UB-LB<=1e-6", "iterations": r.iterations, "boxes_per_solve": r.boxes_bounded,
+                       "enclosure": [r.lb, r.ub]},
+            "e2e": {"value": boxes / e2e_s, "unit": "boxes/s", "ms_per_step": 1e3 * e2e_s / args.steps},
+            "fp64_peak_tflops": peak.value}
 
 
 def run_batched(args):
-    """Config 4: a mixed batch solved by one engine vs the same problems solved
-    one per launch (gpugo_solve in a loop); results must be identical."""
+    """Config 4 with the full autotuner (engine configuration and fan-out tuned
+    on the batch), against the plain kernel on the same re-split problems."""
     import gpugo_gb300 as G
     from gpugo_gb300 import autotune as A
     from gpugo_gb300 import problems as P
     probs = P.config4(count=args.count)
-    tuned = None
-    ecfg = A.EngineConfig()
-    if args.autotune:
-        # block size, candidates per warp and fan-out picked on a sample of the batch;
-        # the plain loop then solves the same (re-split) problems
-        t0 = time.perf_counter()
-        tuned = A.tune(probs, sample=min(512, args.count))
-        tune_s = time.perf_counter() - t0
-        probs = tuned.apply(probs)
-        ecfg = tuned.engine
+    t0 = time.perf_counter()
+    tuned = A.tune(probs, sample=min(512, args.count),
+                   timer=lambda ps, cfg: A.time_engine(ps, cfg, arena_bytes=args.arena_gb << 30))
+    tune_s = time.perf_counter() - t0
+    probs = tuned.apply(probs)
+    ecfg = tuned.engine
     for p in probs[:8]:
-        G.solve(p, box_cap=4)                      # warm-up
+        G.solve(p, box_cap=4)
     t0 = time.perf_counter()
     plain = [G.solve(p, box_cap=4) for p in probs]
     t_plain = time.perf_counter() - t0
-    dev_plain = sum(r.device_ms for r in plain) * 1e-3
     with G.Engine(max_slots=args.count, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
                   blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as eng:
-        eng.solve_all(probs[:8], box_cap=4)        # warm-up
-        st0 = eng.stats()
+        eng.solve_all(probs[:8], box_cap=4)
         t0 = time.perf_counter()
         res = eng.solve_all(probs, box_cap=4)
         t_b = time.perf_counter() - t0
-        st1 = eng.stats()
     same = all((a.lb, a.ub, a.iterations, a.status) == (b.lb, b.ub, b.iterations, b.status)
                for a, b in zip(plain, res))
     boxes = sum(r.boxes_bounded for r in res)
     return {"metric": "boxes/s", "value": boxes / t_b, "unit": "boxes/s", "n_gpus": 1, "dtype": "f64",
-            "higher_is_better": True, "data": "synthetic (config 4 generator, MASTER_SEED+4)",
-            "config": {"workload": f"cfg4-batch{args.count}: families F1-F4, n log-uniform 2..64, UB-LB<=1e-6",
-                       "certified": sum(r.certified for r in res), "boxes": boxes,
-                       "samples_evaluated": sum(r.samples_evaluated for r in res),
-                       "max_iterations": max(r.iterations for r in res)},
-            "batched_wall_s": t_b, "batched_device_s": (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3,
-            "batched_launches": st1["kernel_launches"] - st0["kernel_launches"],
-            "plain_wall_s": t_plain, "plain_device_s": dev_plain, "plain_launches": 2 * len(probs),
-            "speedup_vs_plain": t_plain / t_b, "identical_to_plain": same,
-            "engine": ecfg.label(),
-            **({"autotune": {"seconds": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in
-                                                             tuned.fanout.items()},
-                             "trials": tuned.trials}} if tuned else {})}
-
-
-def run_serving(args):
-    """Config 5: Poisson stream of requests, continuous batching, p50/p99."""
-    import gpugo_gb300 as G
-    from gpugo_gb300 import autotune as A
-    from gpugo_gb300 import problems as P
-    from gpugo_gb300.serve import serve
-    stream = P.config5(count=args.count, rate=args.rate)
-    ecfg, tuned, tune_s = A.EngineConfig(), None, 0.0
-    if args.autotune:
-        # tuned on a sample of the request mix before the stream starts
-        t0 = time.perf_counter()
-        tuned = A.tune([p for _, p in stream], sample=min(128, args.count))
-        tune_s = time.perf_counter() - t0
-        stream = list(zip([t for t, _ in stream], tuned.apply([p for _, p in stream])))
-        ecfg = tuned.engine
-    slots = min(args.count, 2048)
-    with G.Engine(max_slots=slots, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
-                  blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as eng:
-        rep = serve(stream, max_slots=slots, slice_iters=args.slice, engine=eng)
-    sm = rep.summary()
-    return {"metric": "time-to-certified p50/p99 (ms) and boxes/s", "value": sm["boxes_per_s"], "unit": "boxes/s",
-            "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"], "n_gpus": 1, "dtype": "f64",
-            "data": "synthetic (config 5 generator, MASTER_SEED+5)",
-            "config": {"workload": f"cfg5-serve{args.count}: Poisson {args.rate}/s, F1-F4, n log-uniform 2..128, "
-                                   f"tol 1e-6 or 1e-4, pool arena {args.arena_gb} GiB",
-                       "slice_iters": args.slice, "engine": ecfg.label(),
-                       **({"autotune_s": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in
-                                                             tuned.fanout.items()}} if tuned else {})},
-            **{k: v for k, v in sm.items() if k not in ("p50_ms", "p99_ms")}}
+            "config": {"workload": f"cfg4-batch{args.count} with the full autotuner", "boxes": boxes,
+                       "certified": sum(r.certified for r in res)},
+            "batched_wall_s": t_b, "plain_wall_s": t_plain, "speedup_vs_plain": t_plain / t_b,
+            "identical_to_plain": same, "engine": ecfg.label(),
+            "autotune": {"seconds": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in tuned.fanout.items()},
+                         "matches_table": tuned.fanout == A.TUNED_FANOUT, "trials": tuned.trials}}
 
 
 def run_list_pass(args):
@@ -378,8 +502,6 @@ def run_list_pass(args):
     iterations; the list grows by about 1 Mi entries per iteration.  The pass
     is timed with the engine's phase stamps (GPUGO_PHASE_STAMPS) and its
     algorithmic bytes are 16 B per entry read plus 16 B per entry written."""
-    import os
-    import tempfile
     import numpy as np
     path = os.path.join(tempfile.mkdtemp(), "stamps")
     os.environ["GPUGO_PHASE_STAMPS"] = path
@@ -433,7 +555,6 @@ def run_codelist(args):
     """The reference's seven benchmarks without a built-in family, as code
     lists (n = 8, split 3^8, UB-LB <= 1e-6), plus config 2 restated as a code
     list next to its built-in kernel; the CPU oracle solves each once."""
-    import time
     import gpugo_gb300 as G
     import oracle
     from gpugo_gb300 import objectives as O
@@ -477,36 +598,38 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpugo", choices=["gpugo", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="cfg2",
-                    choices=["cfg2", "cfg1", "cfg3", "cfg4", "cfg5", "listpass", "codelist"],
-                    help="cfg2 is the benchmark line; the others print their own records")
-    ap.add_argument("--count", type=int, default=None, help="instances (cfg4: 1024) or requests (cfg5: 4096)")
+    ap.add_argument("--workload", default="batch",
+                    choices=["batch", "cfg1", "cfg2", "cfg3", "cfg4-tune", "listpass", "codelist"],
+                    help="batch is the benchmark line; the others print their own records")
+    ap.add_argument("--count", type=int, default=1024, help="instances of the batch")
+    ap.add_argument("--serve-count", type=int, default=4096, help="requests of the serving record (0: none)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
+    ap.add_argument("--cpu-instances", type=int, default=16, help="batch instances the CPU baseline solves")
+    ap.add_argument("--no-plain", dest="plain", action="store_false",
+                    help="skip the plain one-instance-per-launch comparison")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
-                    help="cfg4/cfg5: skip the autotuner (block size, candidates per warp, fan-out)")
+                    help="skip tuning the engine configuration (block size, candidates per warp)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.count is None:
-        args.count = 4096 if args.workload == "cfg5" else 1024
+    check_gpus(args.gpus)
     ws, rank, local = dist_env()
-    if args.workload != "cfg2" and args.impl == "gpugo":
-        fn = {"cfg1": run_single, "cfg3": run_single, "cfg4": run_batched, "cfg5": run_serving,
-              "listpass": run_list_pass, "codelist": run_codelist}[args.workload]
-        print(json.dumps(fn(args)))
-        return
     if args.impl == "reference":
         out = run_reference(args)
         if out is not None:
             print(json.dumps(out))
         return
+    if args.workload != "batch":
+        fn = {"cfg1": run_single, "cfg2": run_chained8, "cfg3": run_single, "cfg4-tune": run_batched,
+              "listpass": run_list_pass, "codelist": run_codelist}[args.workload]
+        print(json.dumps(fn(args)))
+        return
     dist = init_dist("nccl")
-    out = run_gpugo(args, dist)
+    out = run_batch(args, dist)
     if rank == 0:
-        cb, _, _ = run_cpu_baseline(args.cpu_seconds)
-        out["cpu_baseline"] = cb
+        if args.cpu_instances > 0:
+            out["cpu_baseline"] = run_cpu_baseline(batch_problems(args.count), args.cpu_instances)
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

@@ -135,3 +135,57 @@ def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_byte
         rep.p50_ms = float(np.percentile(lat, 50))
         rep.p99_ms = float(np.percentile(lat, 99))
     return rep
+
+
+# ---------------------------------------------------------------------------
+# several GPUs: one process and one engine per GPU, arrivals dealt round-robin
+# ---------------------------------------------------------------------------
+def partition_stream(stream: list[tuple[float, Problem]], rank: int, world: int) -> list[tuple[float, Problem]]:
+    """The requests rank ``rank`` of ``world`` serves: every world-th arrival,
+    starting at the rank's index, with the arrival times kept.  Requests are
+    independent, so no data crosses between ranks while they are served."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError(f"rank {rank} of {world}")
+    return stream[rank::world]
+
+
+def latency_record(rep: ServeReport) -> dict:
+    """What one rank contributes to the merged report: its served latencies (ms),
+    counts and wall time (plain numbers, so that it can cross process boundaries)."""
+    served = [r for r in rep.records if r.result is not None]
+    return {"latencies_ms": [r.latency * 1e3 for r in served], "boxes": rep.boxes, "certified": rep.certified,
+            "rejected": rep.rejected, "requests": len(rep.records), "wall_s": rep.wall_s, "device_s": rep.device_s,
+            "launches": rep.launches}
+
+
+def merge_records(recs: list[dict]) -> dict:
+    """Merged serving figures over ranks: p50/p99 over every served request's
+    latency, boxes and certified solves summed, boxes/s over the slowest rank's
+    wall time (the job ends when the last rank does)."""
+    lat = np.array([x for r in recs for x in r["latencies_ms"]], dtype=np.float64)
+    wall = max(r["wall_s"] for r in recs)
+    boxes = sum(r["boxes"] for r in recs)
+    return {"ranks": len(recs), "requests": sum(r["requests"] for r in recs),
+            "certified": sum(r["certified"] for r in recs), "rejected": sum(r["rejected"] for r in recs),
+            "wall_s": wall, "device_s_max": max(r["device_s"] for r in recs), "boxes": boxes,
+            "boxes_per_s": boxes / wall if wall > 0 else 0.0,
+            "p50_ms": float(np.percentile(lat, 50)) if lat.size else 0.0,
+            "p99_ms": float(np.percentile(lat, 99)) if lat.size else 0.0,
+            "kernel_launches": sum(r["launches"] for r in recs)}
+
+
+def serve_sharded(stream: list[tuple[float, Problem]], dist=None, **kw) -> dict | None:
+    """Serve ``stream`` across the ranks of ``dist`` (torch.distributed, already
+    initialised; None for one process): each rank serves its round-robin share
+    on its own GPU, then rank 0 gathers the per-rank records and returns the
+    merged figures (other ranks return None).  The only collective is that
+    gather, after the stream has been served."""
+    world = dist.get_world_size() if dist is not None else 1
+    rank = dist.get_rank() if dist is not None else 0
+    rep = serve(partition_stream(stream, rank, world), **kw)
+    rec = latency_record(rep)
+    if dist is None:
+        return merge_records([rec])
+    out = [None] * world if rank == 0 else None
+    dist.gather_object(rec, out, dst=0)
+    return merge_records(out) if rank == 0 else None
