@@ -606,7 +606,7 @@ def main():
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
-    ap.add_argument("--cpu-instances", type=int, default=16, help="batch instances the CPU baseline solves")
+    ap.add_argument("--cpu-instances", type=int, default=64, help="batch instances the CPU baseline solves")
     ap.add_argument("--no-plain", dest="plain", action="store_false",
                     help="skip the plain one-instance-per-launch comparison")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

@@ -8,8 +8,10 @@
 //   exp  IA.py:532-570
 // The reference widens libdevice's sin/cos/pow results by 5 ulp and exp by 2
 // ulp through their bit patterns.  The endpoint functions here are this
-// project's own (Cody-Waite reduction in double-double, Taylor series; error
-// below 1.2 ulp), so the same widening keeps every bound rigorous.  Every
+// project's own (Cody-Waite reduction in double-double, Taylor series; largest
+// error measured against mpmath 0.66 ulp for sin/cos and 0.59 ulp for exp, the
+// tests bounding it by 1.2 and 1.0 ulp), so the same widening keeps every bound
+// rigorous.  Every
 // round-to-nearest operation is written as an explicit __d*_rn / __fma_rn call
 // so that no contraction changes a rounding: the same sequence, compiled for the
 // host in the CPU oracle, yields identical bits.

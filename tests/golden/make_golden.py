@@ -509,10 +509,199 @@ def levy10000_main(ref_root: str):
     print("wrote", dst)
 
 
+# ---------------------------------------------------------------------------
+# the reference's host loop, run as written on a reduced problem
+# ---------------------------------------------------------------------------
+# Text substitutions that shrink rastrigin50.py to 10 variables split in two
+# parts each (2^10 = 1024 children per iteration, one cycle of 10 coordinates)
+# and size its kernel grids to those 1024 children.  Each is applied exactly as
+# many times as listed, or the run stops: the script's own logic is otherwise
+# executed unchanged.
+LOOP_SCRIPT = "GPUGO_1.1/7-Rastrigin/rastrigin50.py"
+LOOP_N, LOOP_WID = 10, 2
+LOOP_SUBS = [
+    ("    n = 50 # The number of variables in the Rastrigin function", f"    n = {LOOP_N}", 3),
+    ("    length = 50 # The number of variables in the Rastrigin function", f"    length = {LOOP_N}", 2),
+    ("    wid = 4", f"    wid = {LOOP_WID}", 2),
+    ("initialRegion = np.tile([-5.5, 6], 50)", f"initialRegion = np.tile([-5.5, 6], {LOOP_N})", 1),
+    ("maximumCyc = 41", "maximumCyc = 1", 1),
+    ("    blockspergridSample = 2048", "    blockspergridSample = 4", 1),
+    ("    threadsperblockSample = 512", "    threadsperblockSample = 256", 1),
+    ("    blockspergridRule = 4096", "    blockspergridRule = 4", 1),
+]
+
+
+class _LoopDone(Exception):
+    pass
+
+
+def make_kernel_runtime():
+    """Stand-in for the parts of numba.cuda the host loop and its kernels use.
+    A kernel launch runs every thread of the grid: one after another in thread
+    order (the order the reference's atomic counters would take if its threads
+    ran in order), or, for a kernel that synchronises its block, as one Python
+    thread per CUDA thread with a barrier for cuda.syncthreads."""
+    import threading
+    tls = threading.local()
+
+    class _Idx:
+        def __init__(self, attr):
+            self.attr = attr
+
+        @property
+        def x(self):
+            return getattr(tls, self.attr)
+
+    class DeviceArray(np.ndarray):
+        def copy_to_host(self):
+            return np.array(self)
+
+    def to_device(a):
+        return np.array(a).view(DeviceArray)
+
+    def device_array(shape, dtype=np.float64):
+        return np.zeros(shape, dtype=dtype).view(DeviceArray)
+
+    class Kernel:
+        def __init__(self, fn):
+            self.fn = fn
+            self.syncs = "syncthreads" in fn.__code__.co_names
+
+        def __call__(self, *args):          # called from device code: a device function
+            return self.fn(*args)
+
+        def __getitem__(self, cfg):
+            blocks, threads = cfg
+
+            def launch(*args):
+                for b in range(blocks):
+                    shared = {}
+                    if not self.syncs:
+                        for t in range(threads):
+                            tls.block, tls.thread, tls.dim, tls.shared, tls.barrier = b, t, threads, shared, None
+                            self.fn(*args)
+                        continue
+                    barrier = threading.Barrier(threads)
+                    errs = []
+
+                    def body(t):
+                        tls.block, tls.thread, tls.dim, tls.shared, tls.barrier = b, t, threads, shared, barrier
+                        try:
+                            self.fn(*args)
+                        except Exception as e:      # surfaced after the block
+                            errs.append(e)
+                            barrier.abort()
+                    ts = [threading.Thread(target=body, args=(t,)) for t in range(threads)]
+                    for th in ts:
+                        th.start()
+                    for th in ts:
+                        th.join()
+                    if errs:
+                        raise errs[0]
+            return launch
+
+    def jit(*args, **kwargs):
+        if args and callable(args[0]):
+            return Kernel(args[0])
+        return lambda f: f                  # device functions run as plain Python
+
+    _shared_lock = threading.Lock()
+
+    def shared_array(shape, dtype):
+        with _shared_lock:                  # one array per block, shared by its threads
+            return tls.shared.setdefault(("a", shape), np.zeros(shape, dtype=dtype))
+
+    def atomic_min(arr, i, v):
+        old = arr[i]
+        if v < old:
+            arr[i] = v
+        return old
+
+    def atomic_add(arr, i, v):
+        old = arr[i]
+        arr[i] = old + v
+        return old
+
+    numba = make_numba_stub()
+    cuda = numba.cuda
+    cuda.jit = jit
+    cuda.grid = lambda d: tls.block * tls.dim + tls.thread
+    cuda.threadIdx = _Idx("thread")
+    cuda.blockIdx = _Idx("block")
+    cuda.blockDim = _Idx("dim")
+    cuda.syncthreads = lambda: tls.barrier.wait()
+    cuda.shared = types.SimpleNamespace(array=shared_array)
+    cuda.atomic = types.SimpleNamespace(min=atomic_min, add=atomic_add)
+    cuda.to_device = to_device
+    cuda.device_array = device_array
+    cuda.synchronize = lambda: None
+    return numba
+
+
+def loop_main(ref_root: str, iters: int = 1000):
+    """Run the host loop of rastrigin50.py (reduced by LOOP_SUBS) to its end (or
+    `iters` expansions) and record, per iteration: the UB after the sampling
+    kernel, the survivors ruleOutGPU appended, the list length after the update,
+    and the entry selected as the next parent (its iteration, child position,
+    cycle and box); at the end, the printed enclosure and output regions.
+    Written to reference_loop_rastrigin10.npz.  Every child's interval
+    operations run as Python with exact rational rounding: about a minute per
+    iteration."""
+    oracle.build()
+    path = os.path.join(ref_root, LOOP_SCRIPT)
+    src = open(path).read()
+    for old, new, count in LOOP_SUBS:
+        if src.count(old) != count:
+            raise SystemExit(f"{LOOP_SCRIPT}: expected {count} x {old!r}, found {src.count(old)}")
+        src = src.replace(old, new)
+    sys.modules["numba"] = make_kernel_runtime()
+    sys.modules["IARastrigin"] = load_updated_ia(ref_root, False)
+    rec = {"ub": [], "n_surv": [], "pool": [], "sel_iter": [], "sel_pos": [], "sel_cyc": [], "parent": []}
+    t0 = time.time()
+    ns: dict = {"__name__": "ref_loop"}
+
+    def hook(*a, **k):
+        msg = " ".join(str(x) for x in a)
+        if msg.startswith("Number of remaining regions"):
+            rec["ub"].append(float(ns["lowestUpperVal"]))
+            rec["n_surv"].append(int(ns["length"]))
+            rec["pool"].append(int(ns["lengthList"]))
+            print(f"iteration {len(rec['ub']) - 1}: UB {rec['ub'][-1]!r}, survivors {rec['n_surv'][-1]}, "
+                  f"list {rec['pool'][-1]}, {time.time() - t0:.0f} s", flush=True)
+        elif msg.startswith("The selected region for the next iteration step is"):
+            rec["sel_iter"].append(int(ns["iteration"]))
+            rec["sel_pos"].append(int(ns["index"]))
+            rec["sel_cyc"].append(int(ns["cycleIdxVal"]))
+            rec["parent"].append(np.array(ns["selected_region"], dtype=np.float64))
+            if len(rec["sel_iter"]) >= iters:
+                raise _LoopDone()
+    ns["print"] = hook
+    finished = True
+    try:
+        exec(compile(src, path, "exec"), ns)
+    except _LoopDone:
+        finished = False
+    out = {k: np.array(v) for k, v in rec.items()}
+    out["n"] = np.array([LOOP_N]); out["wid"] = np.array([LOOP_WID])
+    out["finished"] = np.array([int(finished)])
+    if finished:
+        # what the script prints at the end: the enclosure, the output regions, the iterations
+        out["lb"] = np.array([float(np.min(ns["outputValLower"]))])
+        out["ub_final"] = np.array([float(np.min(ns["outputValUpper"]))])
+        out["output"] = np.array(ns["output"], dtype=np.float64)
+        out["output_lb"] = np.array(ns["outputValLower"], dtype=np.float64)
+        out["iterations"] = np.array([int(ns["iter"])])
+    dst = os.path.join(HERE, "reference_loop_rastrigin10.npz")
+    np.savez_compressed(dst, **out)
+    print("wrote", dst, len(rec["ub"]), "iterations", "(finished)" if finished else "(stopped)")
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
-    if "--codelist" in sys.argv:
+    if "--loop" in sys.argv:
+        loop_main(root, int(args[1]) if len(args) > 1 else 1000)
+    elif "--codelist" in sys.argv:
         codelist_main(root, args[1:] or None)
     elif "--levy10000" in sys.argv:
         levy10000_main(root)

@@ -141,6 +141,19 @@ def test_solve_trace_parity(oracle_lib, name, make):
     assert rg.lb - 1e-12 <= fx <= rg.ub + 1e-12
 
 
+def test_solve_matches_the_reference_host_loop(oracle_lib):
+    """The whole solve against the reference's own top-level loop
+    (tests/golden/reference_loop_rastrigin10.npz: rastrigin50.py reduced to 10
+    variables, 1024 children per iteration, run to its end): every iteration's
+    UB, survivors, list length and selected parent, and the printed enclosure
+    and output region, on the GPU and in the oracle."""
+    from test_oracle_golden import LOOP, check_loop_trace, loop_problem
+    g = np.load(LOOP)
+    p = loop_problem(g)
+    rg, ro = _compare_solves(p, oracle_lib, box_cap=64)
+    check_loop_trace(rg, g)
+
+
 def test_solve_large_list_parity(oracle_lib):
     """Lists of tens of thousands of entries take the grid-wide compaction and
     argmin path instead of the block-level one; the trace must not change."""

@@ -102,3 +102,52 @@ def test_reference_1000_variable_scripts(oracle_lib, name):
         np.testing.assert_allclose(samp, ref_s, rtol=1e-12, atol=1e-12)
     m = ref_d >= 0
     np.testing.assert_array_equal(dflag[m], ref_d[m])
+
+
+LOOP = os.path.join(os.path.dirname(__file__), "golden", "reference_loop_rastrigin10.npz")
+
+
+def loop_problem(g):
+    """The problem the reference's host loop solved for reference_loop_rastrigin10.npz:
+    rastrigin50.py reduced to 10 variables split in 2 parts each (one cycle of
+    10, 1024 children per iteration), its own domain, width rule 1e-4, initial
+    UB 1e6 and 10 samples (tests/golden/make_golden.py, LOOP_SUBS)."""
+    from gpugo_gb300 import problems as P
+    n, wid = int(g["n"][0]), int(g["wid"][0])
+    return P.Problem(P.COSQUAD, n, np.tile([-5.5, 6.0], n),
+                     np.concatenate([np.ones(n), np.full(n, 10.0), np.ones(n)]), wid=wid, group=10, samples=10,
+                     stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6)
+
+
+def check_loop_trace(r, g):
+    """A solve's per-iteration trace and result against the reference's own host
+    loop (ackley50.py:1269-1370 in its Rastrigin form): the UB after each
+    sampling kernel, the survivors ruleOutGPU appended, the list length, the
+    entry selected as the next parent (its iteration and child position, whose
+    tie-break the reference's atomics give in thread order), and at the end the
+    printed enclosure, output regions and iteration count."""
+    assert g["finished"][0] == 1
+    assert r.iterations == g["iterations"][0]
+    np.testing.assert_array_equal(r.trace["ub"], g["ub"])
+    np.testing.assert_array_equal(r.trace["n_surv"], g["n_surv"])
+    np.testing.assert_array_equal(r.trace["pool"], g["pool"])
+    assert np.all(g["sel_cyc"] == 1)                 # one cycle: every parent starts at coordinate 1
+    want = (g["sel_iter"].astype(np.int64) << 32) | g["sel_pos"].astype(np.int64)
+    np.testing.assert_array_equal(r.trace["sel"][:want.size], want)
+    assert np.all(r.trace["sel"][want.size:] == -1)
+    assert r.lb == g["lb"][0] and r.ub == g["ub_final"][0]
+    boxes = np.asarray(r.boxes).reshape(-1, 2 * int(g["n"][0]))
+    np.testing.assert_array_equal(boxes, g["output"])
+    np.testing.assert_array_equal(r.box_lbs, g["output_lb"])
+
+
+def test_oracle_reproduces_the_reference_host_loop(oracle_lib):
+    """The reference's own top-level loop (rastrigin50.py:844-1302, run by
+    make_golden.py --loop with its kernels executed thread by thread) pins the
+    oracle's selection, cycle, width-rule and UB bookkeeping, not only its
+    per-child bounds."""
+    g = np.load(LOOP)
+    r = oracle_lib.solve(loop_problem(g), box_cap=64, trace_cap=1000, skip_samples=False)
+    check_loop_trace(r, g)
+    r2 = oracle_lib.solve(loop_problem(g), box_cap=64, trace_cap=1000, skip_samples=True)
+    check_loop_trace(r2, g)
