@@ -982,7 +982,7 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
 // has enough work to pay for the copy): the blocks copy them in parallel, and
 // every later access avoids an L2 round trip.
 __device__ int stage_tables(const KArgs& a, bool worth = true) {
-  extern __shared__ double s_tab[];
+  extern __shared__ __align__(16) double s_tab[];
   if (a.ctl->nA != 1 || !worth) return -1;
   const int si = a.idsA[0];
   const Desc& D = a.desc[si];
@@ -995,16 +995,35 @@ __device__ int stage_tables(const KArgs& a, bool worth = true) {
   return si;
 }
 
-__device__ __forceinline__ void append_survivor(const KArgs& a, int s, unsigned long long code, double lb) {
-  if (feq(lb, 0.0)) lb = 0.0;  // list keys order -0 before +0; the LB comparison does not
-  const Desc& D = a.desc[s];
-  State& st = a.st[s];
-  long long pos = (long long)atomicAdd((unsigned long long*)&st.count, 1ULL);
-  if (pos < D.pool_cap) {
-    D.pool_lb[st.cur][pos] = lb;
-    D.pool_key[st.cur][pos] = ((unsigned long long)st.iter << 32) | code;
-  } else {
-    atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
+// Survivors of one warp (lanes with keep set; lane i's child `code` of instance
+// `s` with lower bound `lb`) appended to their instances' lists with one
+// atomicAdd per instance present in the warp: lanes are grouped by instance with
+// ballots and each takes its place from its rank in the group.  Every lane of
+// the warp calls it.  Positions inside the list carry no meaning (selection ties
+// are broken by the key), so any order of the appends gives the same solve.
+__device__ __noinline__ void warp_append_survivors(const KArgs& a, bool keep, int s, unsigned long long code,
+                                                      double lb) {
+  const int lane = threadIdx.x & 31;
+  unsigned int act = __ballot_sync(0xffffffffu, keep);
+  while (act) {
+    const int leader = __ffs(act) - 1;
+    const int ls = __shfl_sync(0xffffffffu, s, leader);
+    const unsigned int m = __ballot_sync(0xffffffffu, keep && s == ls);
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd((unsigned long long*)&a.st[ls].count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (keep && s == ls) {
+      const Desc& D = a.desc[ls];
+      State& st = a.st[ls];
+      const long long pos = (long long)base + __popc(m & ((1u << lane) - 1u));
+      if (pos < D.pool_cap) {
+        D.pool_lb[st.cur][pos] = feq(lb, 0.0) ? 0.0 : lb;  // list keys order -0 before +0; LB comparisons do not
+        D.pool_key[st.cur][pos] = ((unsigned long long)st.iter << 32) | code;
+      } else {
+        atomicCAS(&st.outcome, 0, GPUGO_ERR_POOL_OVERFLOW);
+      }
+    }
+    act &= ~m;
   }
 }
 
@@ -1013,7 +1032,7 @@ __device__ __forceinline__ void append_survivor(const KArgs& a, int s, unsigned 
 template <bool CL>
 __device__ void phase_bound(const KArgs& a) {
   bstamp(a, 2);
-  extern __shared__ double s_tab[];
+  extern __shared__ __align__(16) double s_tab[];
   const int si = stage_tables(a);
   const long long tot = a.ctl->totB;
   const int nA = a.ctl->nA;
@@ -1097,7 +1116,7 @@ __device__ void phase_bound(const KArgs& a) {
         bool kk = warp_candidate<CL>(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
         if (lane == b) keep = kk;
       }
-      if (keep) append_survivor(a, s, code, lb);
+      warp_append_survivors(a, keep, s, code, lb);
     }
   }
   __syncthreads();
@@ -1135,7 +1154,7 @@ __device__ void prefill_ready(const KArgs& a) {
 // pass 2 then starts every candidate's sample passes from.
 template <bool CL>
 __device__ void phase_seed(const KArgs& a) {
-  extern __shared__ double s_tab[];
+  extern __shared__ __align__(16) double s_tab[];
   const int si = stage_tables(a);
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
@@ -1214,7 +1233,7 @@ __device__ __forceinline__ void instance_ready(const KArgs& a, int s) {
 
 template <bool CL>
 __device__ void phase_candidates(const KArgs& a) {
-  extern __shared__ double s_tab[];
+  extern __shared__ __align__(16) double s_tab[];
   __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
   __shared__ unsigned long long s_claimed;
   // a few candidates per block do not pay for copying the tables
@@ -1295,7 +1314,12 @@ __device__ void phase_candidates(const KArgs& a) {
           int rr = thread_candidate<CL>(a, s, T, code, lb, aux, pfx_on ? T + a.desc[s].t_off[T_PFX] : nullptr);
           keep = rr & 1;
           sampled = rr & 2;
-          if (keep) append_survivor(a, s, code, lb);
+        }
+        {
+          const unsigned long long q = valid ? h + surv[idx] : 0ULL;
+          const unsigned long long code = valid ? (a.cands[CAND_WORDS * q] & 0xffffffffULL) : 0ULL;
+          const double lb = valid ? __longlong_as_double((long long)a.cands[CAND_WORDS * q + 1]) : 0.0;
+          warp_append_survivors(a, keep, s, code, lb);
         }
         unsigned int act = __ballot_sync(0xffffffffu, valid);
         while (act) {
@@ -1336,6 +1360,7 @@ __device__ void phase_candidates(const KArgs& a) {
         live = !flt(atomic_ub_read(&a.st[s].ub), lb);
       }
       unsigned int lm = __ballot_sync(0xffffffffu, live);
+      bool kept = false;   // this lane's own entry survived
       while (lm) {
         const int b = __ffs(lm) - 1;
         lm &= lm - 1;
@@ -1347,8 +1372,9 @@ __device__ void phase_candidates(const KArgs& a) {
         ca[1] = shfl_d(aux[1], b);
         const double* T = (cs == si) ? s_tab : a.desc[cs].tab;
         const bool keep = warp_candidate<CL>(a, cs, T, cc, cl, ca, pfx_on ? T + a.desc[cs].t_off[T_PFX] : nullptr);
-        if (keep && lane == 0) append_survivor(a, cs, cc, cl);
+        if (lane == b) kept = keep;
       }
+      warp_append_survivors(a, kept, s, code, lb);
       __syncwarp();
       // every entry of the claim is done: count them per instance
       unsigned int act = __ballot_sync(0xffffffffu, valid);
@@ -1377,76 +1403,216 @@ __device__ void phase_candidates(const KArgs& a) {
 // ---------------------------------------------------------------------------
 // grid-wide path for large pools: compaction + per-tile argmin, then selection
 // ---------------------------------------------------------------------------
+// The list pass streams each tile's LB and key slices (2048 entries, 32 KB)
+// from global memory into shared memory with bulk asynchronous copies
+// (cp.async.bulk, completion counted in bytes on an mbarrier), three tiles in
+// flight per block in the dynamic shared memory the tables use in the other
+// phases.  While a tile is filtered and its survivors written, the copies of
+// the next two are under way, so the block never waits for a whole round trip
+// to memory per tile.
+constexpr int POOL_STAGES = 3;
+constexpr int POOL_STAGE_BYTES = TD * 16;   // LB slice, then key slice
+constexpr int POOL_PER = TD / 256;          // entries per thread and tile (256 or 512 threads)
+static_assert(POOL_STAGES * POOL_STAGE_BYTES <= SMEM_TAB_BYTES, "pool stages exceed the dynamic shared memory");
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(unsigned long long* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for phase `parity` of an mbarrier: false when the budget ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned long long budget_ns) {
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try_wait(bar, parity))
+    if (gtimer() - t0 > budget_ns) return false;
+  return true;
+}
+// Global -> shared bulk copy whose completion is counted on `bar` (16-byte
+// aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+struct PoolTile {
+  long long lo, hi, count_before;
+  double ub;
+  int s, cur, compact, tile;
+};
+
 __device__ void phase_pool(const KArgs& a) {
+  extern __shared__ __align__(16) double s_tab[];
+  __shared__ __align__(8) unsigned long long s_bar[POOL_STAGES];
+  __shared__ PoolTile s_meta[POOL_STAGES];
+  __shared__ unsigned int s_cnt[POOL_PER * (MAX_THREADS / 32)];   // survivors per (round, warp)
+  __shared__ unsigned long long s_base;
+  __shared__ int s_fail;
   const long long tot = a.ctl->totD;
   const int nB = a.ctl->nBig;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int per = TD / blockDim.x;
+  const long long mine = (long long)blockIdx.x < tot ? (tot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  if (mine == 0) return;   // the same for every thread of the block
+  char* smem = (char*)s_tab;
   int hint = -1;
-  for (long long t = blockIdx.x; t < tot; t += gridDim.x) {
-    int k = find_seg(a.prefD, nB, t, hint);
-    hint = k;
-    int s = a.idsE[k];
-    const Desc& D = a.desc[s];
-    State& st = a.st[s];
-    const long long tile = t - a.prefD[k];
-    const long long cnt = st.count < D.pool_cap ? st.count : D.pool_cap;
-    const bool compact = st.ub != st.ub_start;
-    const double ub = ord_val(st.ub);
-    const int cur = st.cur;
-    const long long lo = tile * TD, hi = min(cnt, lo + TD);
-    Best b = best_none();
+  // thread 0: tile j of this block into stage j % POOL_STAGES.  The stage's
+  // earlier contents were read by every thread before the __syncthreads that
+  // precedes this call; the proxy fence orders those reads before the copy.
+  auto issue = [&](long long j) {
+    const int k = (int)(j % POOL_STAGES);
+    const long long t = blockIdx.x + j * gridDim.x;
+    const int sk = find_seg(a.prefD, nB, t, hint);
+    hint = sk;
+    PoolTile m;
+    m.s = a.idsE[sk];
+    const Desc& D = a.desc[m.s];
+    const State& st = a.st[m.s];
+    const long long count = vload(st.count);
+    const long long cnt = count < D.pool_cap ? count : D.pool_cap;
+    const unsigned long long ubk = vload(st.ub);
+    m.tile = (int)(t - a.prefD[sk]);
+    m.lo = (long long)m.tile * TD;
+    m.hi = min(cnt, m.lo + TD);
+    m.cur = vload(st.cur);
+    m.compact = ubk != vload(st.ub_start);
+    m.ub = ord_val(ubk);
+    m.count_before = vload(st.count_before);
+    s_meta[k] = m;
+    // an even number of entries: 16-byte multiples from a 16 KB-aligned tile start
+    const unsigned pair = (unsigned)((m.hi - m.lo) & ~1LL);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(&s_bar[k], pair * 16u);
+    if (pair) {
+      bulk_load(smem + k * POOL_STAGE_BYTES, D.pool_lb[m.cur] + m.lo, pair * 8u, &s_bar[k]);
+      bulk_load(smem + k * POOL_STAGE_BYTES + TD * 8, D.pool_key[m.cur] + m.lo, pair * 8u, &s_bar[k]);
+    }
+  };
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < POOL_STAGES; ++k) mbar_init(&s_bar[k], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+    for (long long j = 0; j < mine && j < POOL_STAGES; ++j) issue(j);
+  }
+  __syncthreads();
+  long long waited = 0;   // tiles whose copies this block has seen complete
+  for (long long j = 0; j < mine; ++j) {
+    const int k = (int)(j % POOL_STAGES);
+    const unsigned parity = (unsigned)((j / POOL_STAGES) & 1);
+    if (!mbar_wait(&s_bar[k], parity, a.timeout_ns)) {
+      atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT);
+      s_fail = 1;
+    }
+    __syncthreads();
+    if (s_fail) break;
+    waited = j + 1;
+    const PoolTile m = s_meta[k];
+    const Desc& D = a.desc[m.s];
+    State& st = a.st[m.s];
+    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
+    const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
+    const long long n = m.hi - m.lo, pair = n & ~1LL;
+    // entry i of the tile: from the stage, or (the odd last entry of a list, not
+    // in the bulk copy) from global memory
+    auto entry_lb = [&](long long i) { return i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i); };
+    auto entry_key = [&](long long i) { return i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i); };
+    unsigned keepm = 0;
     long long removed_new = 0;
-    // the tile's entries are loaded all at once (TD / blockDim per thread, at most
-    // 8), then filtered; the kept ones get one block-wide offset from a single
-    // atomic per tile (the order inside the new buffer is free: selection ties
-    // are broken by key, not by position)
-    constexpr int PER = 8;
-    double lbv[PER];
-    unsigned long long key[PER];
-    bool keep[PER];
-    int nk = 0;
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      const long long e = lo + threadIdx.x + (long long)j * blockDim.x;
-      const bool in = e < hi && j * (int)blockDim.x < TD;
-      lbv[j] = in ? D.pool_lb[cur][e] : 0.0;
-      key[j] = in ? D.pool_key[cur][e] : 0ULL;
-      keep[j] = in && (!compact || !flt(ub, lbv[j]));
-      if (compact && in && !keep[j] && e >= st.count_before) removed_new++;
-      nk += keep[j] ? 1 : 0;
-    }
-    unsigned long long base = 0;
-    if (compact) {
-      __shared__ unsigned long long s_base;
-      long long tk;
-      const long long off = block_exclusive_scan((long long)nk, &tk);
-      if (threadIdx.x == 0) s_base = tk ? atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk) : 0ULL;
-      __syncthreads();
-      base = s_base + (unsigned long long)off;
-    }
-#pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      if (!keep[j]) continue;
-      unsigned long long pos = (unsigned long long)(lo + threadIdx.x + (long long)j * blockDim.x);
-      if (compact) {
-        pos = base++;
-        D.pool_lb[cur ^ 1][pos] = lbv[j];
-        D.pool_key[cur ^ 1][pos] = key[j];
+    for (int r = 0; r < POOL_PER; ++r) {
+      const long long i = threadIdx.x + (long long)r * blockDim.x;
+      const bool in = r < per && i < n;
+      const bool keep = in && (!m.compact || !flt(m.ub, entry_lb(i)));
+      if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
+      keepm |= keep ? (1u << r) : 0u;
+      if (m.compact && r < per) {
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) s_cnt[r * nw + wid] = __popc(b);
       }
-      Best c; c.lbk = ord_key(lbv[j]); c.key = key[j]; c.idx = pos;
-      if (best_less(c, b)) b = c;
     }
-    if (compact) {
+    if (m.compact) {
+      __syncthreads();
+      // exclusive prefix of the survivor counts in tile order (round, warp, lane):
+      // survivors keep their order, and each warp's stores are contiguous
+      if (wid == 0) {
+        const int nc = per * nw;   // TD / 32 = 64
+        unsigned c0 = lane < nc ? s_cnt[lane] : 0u, c1 = lane + 32 < nc ? s_cnt[lane + 32] : 0u;
+        unsigned x0 = c0, x1 = c1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          unsigned y0 = __shfl_up_sync(0xffffffffu, x0, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
+          if (lane >= o) { x0 += y0; x1 += y1; }
+        }
+        const unsigned t0 = __shfl_sync(0xffffffffu, x0, 31);
+        x1 += t0;
+        const unsigned tk = __shfl_sync(0xffffffffu, x1, 31);
+        if (lane < nc) s_cnt[lane] = x0 - c0;
+        if (lane + 32 < nc) s_cnt[lane + 32] = x1 - c1;
+        if (lane == 0) s_base = tk ? atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk) : 0ULL;
+      }
+      __syncthreads();
+    }
+    Best b = best_none();
+#pragma unroll
+    for (int r = 0; r < POOL_PER; ++r) {
+      const bool keep = (keepm >> r) & 1u;
+      const long long i = threadIdx.x + (long long)r * blockDim.x;
+      unsigned long long pos = (unsigned long long)(m.lo + i);
+      double lv = 0.0;
+      unsigned long long kv = 0ULL;
+      if (keep) { lv = entry_lb(i); kv = entry_key(i); }
+      if (m.compact && r < per) {
+        const unsigned bm = __ballot_sync(0xffffffffu, keep);
+        pos = s_base + s_cnt[r * nw + wid] + __popc(bm & ((1u << lane) - 1u));
+        if (keep) {
+          D.pool_lb[m.cur ^ 1][pos] = lv;
+          D.pool_key[m.cur ^ 1][pos] = kv;
+        }
+      }
+      if (keep) {
+        Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
+        if (best_less(c, b)) b = c;
+      }
+    }
+    if (m.compact) {
       for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
       if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
     }
-    b = block_min(b);
+    b = block_min(b);   // synchronises: every thread is done with the stage
     if (threadIdx.x == 0) {
-      unsigned long long* tb = D.tile_best + 3 * tile;
+      unsigned long long* tb = D.tile_best + 3 * m.tile;
       tb[0] = b.lbk; tb[1] = b.key; tb[2] = b.idx;
+      if (j + POOL_STAGES < mine) issue(j + POOL_STAGES);
     }
     __syncthreads();
   }
+  // after an expired wait: wait (bounded again) for the copies still in flight
+  // before the shared memory is used for anything else
+  if (s_fail && threadIdx.x == 0) {
+    const long long issued = mine < waited + POOL_STAGES ? mine : waited + POOL_STAGES;
+    for (long long j = waited; j < issued; ++j)
+      mbar_wait(&s_bar[j % POOL_STAGES], (unsigned)((j / POOL_STAGES) & 1), a.timeout_ns);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < POOL_STAGES; ++k) mbar_inval(&s_bar[k]);
+  __syncthreads();
 }
 
 __device__ void phase_select_big(const KArgs& a) {
