@@ -551,6 +551,41 @@ def run_single(args):
                        "boxes_per_solve": r.boxes_bounded, "enclosure": [r.lb, r.ub], "certified": r.certified}}
 
 
+def run_cfg3_full(args):
+    """Config 3 as stated: the n = 32 exp-sqrt composite split in 2 parts per
+    coordinate, 2^32 children per iteration, streamed through the candidate
+    queue in passes (2^20 children each) with the list capped at --pool-gb.
+    Every first-level child contains the minimiser at the centre of the domain,
+    so none can be ruled out: the 2^32 survivors of the first iteration need a
+    64 GiB list per buffer.  Runs --steps iterations (1 or 2) and reports the
+    boxes bounded per second and how the solve ended (GPUGO_ERR_POOL_OVERFLOW,
+    -4, when the cap is reached)."""
+    import gpugo_gb300 as G
+    from gpugo_gb300 import problems as P
+    p = P.config3()
+    p.max_iter = max(1, args.steps)
+    pool_bytes = args.pool_gb << 30
+    p.pool_cap = pool_bytes // 32              # two buffers of (LB, key) entries
+    need = G.instance_bytes(p)
+    with G.Engine(max_slots=1, arena_bytes=need + (64 << 20), wait_timeout_s=120.0) as eng:
+        st0 = eng.stats()
+        t0 = time.perf_counter()
+        eng.submit(p, box_cap=4)
+        eng.run(0)
+        (_, r), = eng.poll()
+        wall = time.perf_counter() - t0
+        st1 = eng.stats()
+    dev_s = (st1["total_run_ms"] - st0["total_run_ms"]) * 1e-3
+    return {"metric": "boxes/s", "value": r.boxes_bounded / dev_s, "unit": "boxes/s", "n_gpus": 1, "dtype": "f64",
+            "config": {"workload": "cfg3-expsqrt32 as stated: (2, 32) split, 2^32 children per iteration, children "
+                                   f"streamed in passes of 2^20, list capped at {args.pool_gb} GiB",
+                       "pool_cap_entries": p.pool_cap, "arena_bytes": need, "max_iter": p.max_iter},
+            "status": r.status, "status_text": G._lib.ERRORS.get(r.status, "ok") if r.status < 0 else "solve state",
+            "iterations": r.iterations, "boxes_bounded": r.boxes_bounded, "samples_evaluated": r.samples_evaluated,
+            "pool_size": r.pool_size, "device_s": dev_s, "wall_s": wall, "ub": r.ub, "lb": r.lb,
+            "kernel_launches": st1["kernel_launches"] - st0["kernel_launches"]}
+
+
 def run_codelist(args):
     """The reference's seven benchmarks without a built-in family, as code
     lists (n = 8, split 3^8, UB-LB <= 1e-6), plus config 2 restated as a code
@@ -599,13 +634,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpugo", choices=["gpugo", "reference"])
     ap.add_argument("--workload", default="batch",
-                    choices=["batch", "cfg1", "cfg2", "cfg3", "cfg4-tune", "listpass", "codelist"],
+                    choices=["batch", "cfg1", "cfg2", "cfg3", "cfg3-full", "cfg4-tune", "listpass", "codelist"],
                     help="batch is the benchmark line; the others print their own records")
     ap.add_argument("--count", type=int, default=1024, help="instances of the batch")
     ap.add_argument("--serve-count", type=int, default=4096, help="requests of the serving record (0: none)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
+    ap.add_argument("--pool-gb", type=int, default=64, help="cfg3-full: list cap (two buffers)")
     ap.add_argument("--cpu-instances", type=int, default=64, help="batch instances the CPU baseline solves")
     ap.add_argument("--no-plain", dest="plain", action="store_false",
                     help="skip the plain one-instance-per-launch comparison")
@@ -621,7 +657,8 @@ def main():
             print(json.dumps(out))
         return
     if args.workload != "batch":
-        fn = {"cfg1": run_single, "cfg2": run_chained8, "cfg3": run_single, "cfg4-tune": run_batched,
+        fn = {"cfg1": run_single, "cfg2": run_chained8, "cfg3": run_single, "cfg3-full": run_cfg3_full,
+              "cfg4-tune": run_batched,
               "listpass": run_list_pass, "codelist": run_codelist}[args.workload]
         print(json.dumps(fn(args)))
         return

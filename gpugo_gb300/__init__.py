@@ -187,10 +187,10 @@ class Engine:
     """
 
     def __init__(self, max_slots: int = 1024, arena_bytes: int = 8 << 30, wait_timeout_s: float = 60.0,
-                 blocks_per_sm: int = 0, cand_mode: int = _lib.CAND_AUTO, threads: int = 256):
+                 blocks_per_sm: int = 0, cand_mode: int = _lib.CAND_AUTO, threads: int = 256, chunk_children: int = 0):
         self._L = _lib.load()
         cfg = _lib.EngineCfg(int(max_slots), int(threads), int(arena_bytes), float(wait_timeout_s),
-                             int(blocks_per_sm), int(cand_mode))
+                             int(blocks_per_sm), int(cand_mode), int(chunk_children))
         h = ctypes.c_void_p()
         _lib.check(self._L.gpugo_engine_create(ctypes.byref(cfg), ctypes.byref(h)), "gpugo_engine_create")
         self._h = h

@@ -60,6 +60,7 @@ class EngineCfg(ctypes.Structure):
     _fields_ = [
         ("max_slots", ctypes.c_int32), ("threads", ctypes.c_int32), ("arena_bytes", ctypes.c_int64),
         ("wait_timeout_s", ctypes.c_double), ("blocks_per_sm", ctypes.c_int32), ("cand_mode", ctypes.c_int32),
+        ("chunk_children", ctypes.c_int64),
     ]
 
 

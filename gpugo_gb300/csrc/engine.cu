@@ -113,7 +113,8 @@ struct Ctl {
   unsigned long long cand_head;   // candidate queue: entries claimed in pass 2
   long long cand_claim;           // entries claimed per atomic in pass 2
   int seed_on;                    // run the seed pass this iteration
-  int pad2;
+  int b_last;                     // the children pass [b_lo, b_hi) is the iteration's last
+  long long b_lo, b_hi;           // flat children range of the current pass
 };
 
 struct KArgs {
@@ -128,6 +129,7 @@ struct KArgs {
   unsigned long long* queue;  // [max_slots] ready queue entries: epoch << 32 | slot
   unsigned long long* cands;  // [cand_cap][CAND_WORDS] candidate queue: slot << 32 | code, lb bits, aux
   long long cand_cap;
+  long long chunk;            // children bounded per pass (at most cand_cap)
   int cand_mode;              // GPUGO_CAND_AUTO / _WARP / _LANE
   int max_slots;
   int fam_hi;                 // highest family number resident (work lists are grouped up to it)
@@ -241,6 +243,17 @@ __device__ long long children_of(const Desc& D, int cyc) {
   return m;
 }
 
+// An iteration's children are bounded in passes of at most a.chunk children (the
+// candidate queue's capacity unless the engine sets fewer), so that every
+// candidate of a pass has a place in the queue however many children the
+// iteration has (up to 2^32 for one instance).  Instances are updated after
+// the last pass.
+__device__ __forceinline__ void set_first_pass(const KArgs& a, long long totB) {
+  a.ctl->b_lo = 0;
+  a.ctl->b_hi = totB < a.chunk ? totB : a.chunk;
+  a.ctl->b_last = totB <= a.chunk;
+}
+
 // Lists for the next iteration: expanding instances (tables, children) and the
 // ready queue pre-filled with instances that only pop (width-rule emissions).
 // Large batches list the expanding instances family by family: warps walk the
@@ -291,6 +304,7 @@ __device__ void build_lists_warp(const KArgs& a) {
     a.ctl->chunk_next = 0;
     a.ctl->cand_tail = 0;
     a.ctl->cand_head = 0;
+    set_first_pass(a, totB);
   }
 }
 
@@ -355,6 +369,7 @@ __device__ void build_lists(const KArgs& a) {
     a.ctl->chunk_next = 0;
     a.ctl->cand_tail = 0;
     a.ctl->cand_head = 0;
+    set_first_pass(a, baseSB);
   }
 }
 
@@ -1034,13 +1049,13 @@ __device__ void phase_bound(const KArgs& a) {
   bstamp(a, 2);
   extern __shared__ __align__(16) double s_tab[];
   const int si = stage_tables(a);
-  const long long tot = a.ctl->totB;
+  const long long lo = vload(a.ctl->b_lo), tot = vload(a.ctl->b_hi);   // this pass's children
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
   const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
   const long long w = ((long long)(threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
   int hint = -1;
-  for (long long base = w * 32; base < tot; base += W * 32) {
+  for (long long base = lo + w * 32; base < tot; base += W * 32) {
     long long it = base + lane;
     bool valid = it < tot;
     int k = valid ? find_seg(a.prefB, nA, it, hint) : -1;
@@ -1126,12 +1141,16 @@ __device__ void phase_bound(const KArgs& a) {
 // instances without queued candidates are ready for their list update at once
 __device__ void prefill_ready(const KArgs& a) {
   const int nA = a.ctl->nA;
-  for (int k = threadIdx.x; k < nA; k += blockDim.x) {
-    int s = a.idsA[k];
-    if (a.st[s].cand_total == 0) queue_push(a, s);
+  // after the last children pass: instances whose candidates are all done (or
+  // that had none) go to their list update at once
+  if (vload(a.ctl->b_last)) {
+    for (int k = threadIdx.x; k < nA; k += blockDim.x) {
+      int s = a.idsA[k];
+      if (vload(a.st[s].cand_total) == vload(a.st[s].cand_done)) queue_push(a, s);
+    }
   }
   if (threadIdx.x == 0) {
-    long long tot = (long long)a.ctl->cand_tail;
+    long long tot = (long long)vload(a.ctl->cand_tail);
     if (tot > a.cand_cap) tot = a.cand_cap;
     long long W = ((long long)gridDim.x * blockDim.x) >> 5;
     long long c = tot / (2 * W);
@@ -1237,14 +1256,16 @@ __device__ void phase_candidates(const KArgs& a) {
   __shared__ unsigned int s_surv[MAX_THREADS / 32][64];
   __shared__ unsigned long long s_claimed;
   // a few candidates per block do not pay for copying the tables
-  const int si = stage_tables(a, a.ctl->cand_tail >= 16ULL * gridDim.x);
+  const int si = stage_tables(a, vload(a.ctl->cand_tail) >= 16ULL * gridDim.x);
   if (threadIdx.x == 0) s_claimed = 0;
   __syncthreads();
   bstamp(a, 6);
   const int lane = threadIdx.x & 31;
-  const unsigned long long tot = a.ctl->cand_tail;
-  const unsigned long long K = (unsigned long long)a.ctl->cand_claim;
-  const bool pfx_on = a.ctl->seed_on != 0;   // the seed pass stored the shared sample prefixes
+  const unsigned long long tot = vload(a.ctl->cand_tail);
+  const unsigned long long K = (unsigned long long)vload(a.ctl->cand_claim);
+  const bool pfx_on = vload(a.ctl->seed_on) != 0;   // the seed pass stored the shared sample prefixes
+  // instances are updated only after the iteration's last children pass
+  const bool last = vload(a.ctl->b_last) != 0;
   // With a short queue (a warp per candidate) the first claim of warp g (numbered
   // across the blocks first) is the range g*K: the candidates land on warps of
   // different SMs, which do not share an FP64 unit.  Later claims, and every
@@ -1290,7 +1311,7 @@ __device__ void phase_candidates(const KArgs& a) {
           {
             int fin = 0;
             if (lane == leader) fin = count_done(a, ls, __popc(m));
-            if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
+            if (__shfl_sync(0xffffffffu, fin, leader) && last) instance_ready(a, ls);
           }
           act &= ~m;
         }
@@ -1332,7 +1353,7 @@ __device__ void phase_candidates(const KArgs& a) {
             if (sm) atomicAdd((unsigned long long*)&a.st[ls].samples, (unsigned long long)__popc(sm));
             fin = count_done(a, ls, __popc(m));
           }
-          if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
+          if (__shfl_sync(0xffffffffu, fin, leader) && last) instance_ready(a, ls);
           act &= ~m;
         }
       }
@@ -1385,7 +1406,7 @@ __device__ void phase_candidates(const KArgs& a) {
         {
             int fin = 0;
             if (lane == leader) fin = count_done(a, ls, __popc(m));
-            if (__shfl_sync(0xffffffffu, fin, leader)) instance_ready(a, ls);
+            if (__shfl_sync(0xffffffffu, fin, leader) && last) instance_ready(a, ls);
           }
         act &= ~m;
       }
@@ -1605,9 +1626,12 @@ __device__ void phase_pool(const KArgs& a) {
   // after an expired wait: wait (bounded again) for the copies still in flight
   // before the shared memory is used for anything else
   if (s_fail && threadIdx.x == 0) {
+    // at least two seconds, however short the engine's budget: a bulk copy
+    // normally lands within microseconds
+    const unsigned long long budget = a.timeout_ns > 2000000000ULL ? a.timeout_ns : 2000000000ULL;
     const long long issued = mine < waited + POOL_STAGES ? mine : waited + POOL_STAGES;
     for (long long j = waited; j < issued; ++j)
-      mbar_wait(&s_bar[j % POOL_STAGES], (unsigned)((j / POOL_STAGES) & 1), a.timeout_ns);
+      mbar_wait(&s_bar[j % POOL_STAGES], (unsigned)((j / POOL_STAGES) & 1), budget);
   }
   __syncthreads();
   if (threadIdx.x == 0)
@@ -1655,6 +1679,21 @@ struct TailPrefill {
   const KArgs* a;
   __device__ void operator()() const { prefill_ready(*a); }
 };
+// the next children pass of the iteration
+struct TailNextPass {
+  const KArgs* a;
+  __device__ void operator()() const {
+    if (threadIdx.x == 0) {
+      Ctl* c = a->ctl;
+      const long long lo = c->b_hi, tot = c->totB;
+      c->b_lo = lo;
+      c->b_hi = (tot - lo < a->chunk) ? tot : lo + a->chunk;
+      c->b_last = c->b_hi >= tot;
+      c->cand_tail = 0;
+      c->cand_head = 0;
+    }
+  }
+};
 struct TailAfterChildren {
   const KArgs* a;
   __device__ void operator()() const {
@@ -1681,6 +1720,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   TailLists tl{&a};
   TailAfterChildren tc{&a};
   TailPrefill tp{&a};
+  TailNextPass tn{&a};
   // queue entries of earlier launches carry stale epochs
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_slots; i += gridDim.x * blockDim.x) a.queue[i] = 0ULL;
   if (!grid_barrier(a, tl)) return;
@@ -1691,13 +1731,17 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
     phase_tables<CL>(a);
     if (!grid_barrier(a, NoTail{})) return;
     stamp(a, it, 1);
-    phase_bound<CL>(a);
-    if (!grid_barrier(a, tp)) return;
-    if (a.ctl->seed_on) {
-      phase_seed<CL>(a);
-      if (!grid_barrier(a, NoTail{})) return;
+    for (;;) {   // the iteration's children, one pass of at most a.chunk after the other
+      phase_bound<CL>(a);
+      if (!grid_barrier(a, tp)) return;
+      if (vload(a.ctl->seed_on)) {
+        phase_seed<CL>(a);
+        if (!grid_barrier(a, NoTail{})) return;
+      }
+      phase_candidates<CL>(a);
+      if (vload(a.ctl->b_last)) break;
+      if (!grid_barrier(a, tn)) return;
     }
-    phase_candidates<CL>(a);
     if (!grid_barrier(a, tc)) return;
     stamp(a, it, 2);
     if (a.ctl->nBig > 0) {
@@ -2036,6 +2080,7 @@ struct gpugo_engine {
   unsigned long long* d_queue = nullptr;
   unsigned long long* d_cands = nullptr;
   long long cand_cap = 0;
+  long long chunk = 0;           // children per pass (<= cand_cap)
   long long* d_pref = nullptr;   // prefA | prefB | prefD
   char* d_arena = nullptr;
   Arena arena;
@@ -2693,6 +2738,7 @@ int gpugo_instance_bytes(const gpugo_spec* spec, int64_t* bytes_out) {
 int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
   if (!cfg || !out || cfg->max_slots < 1 || cfg->max_slots > 8192 || cfg->arena_bytes <= 0) return GPUGO_ERR_INVALID;
   if (cfg->cand_mode < GPUGO_CAND_AUTO || cfg->cand_mode > GPUGO_CAND_LANE) return GPUGO_ERR_INVALID;
+  if (cfg->chunk_children < 0) return GPUGO_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GPUGO_ERR_NO_DEVICE;
   gpugo_engine* E = new (std::nothrow) gpugo_engine();
@@ -2733,6 +2779,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     if ((rc = cuda_err(cudaMalloc(&E->d_queue, sizeof(unsigned long long) * E->max_slots)))) break;
     E->cand_cap = std::min<long long>(1LL << 24, std::max<long long>(1LL << 20, 8192LL * E->max_slots));
     if ((rc = cuda_err(cudaMalloc(&E->d_cands, 8 * CAND_WORDS * (size_t)E->cand_cap)))) break;
+    E->chunk = cfg->chunk_children > 0 ? std::min<long long>(cfg->chunk_children, E->cand_cap) : E->cand_cap;
     if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
@@ -3119,6 +3166,7 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.queue = E->d_queue;
   a.cands = E->d_cands;
   a.cand_cap = E->cand_cap;
+  a.chunk = E->chunk;
   a.cand_mode = E->cand_mode;
   a.max_slots = E->max_slots;
   a.max_iters = max_iters;

@@ -186,6 +186,10 @@ typedef struct gpugo_engine_cfg {
     double  wait_timeout_s;     /* bound of every device-side wait (0: 60 s) */
     int32_t blocks_per_sm;      /* 0: occupancy maximum (one per SM for engines of at most 4 slots) */
     int32_t cand_mode;          /* candidate scheduling, GPUGO_CAND_* (results are the same in every mode) */
+    int64_t chunk_children;     /* children bounded per pass (0: the candidate queue's capacity, 2^20 to 2^24).
+                                   An iteration with more children (up to 2^32 for one instance, against the
+                                   reference's 4^10, ackley50.py:1053-1054) streams them through the queue in
+                                   passes of this size; results do not depend on it */
 } gpugo_engine_cfg;
 
 /* Candidate children (LB not above the UB) are sampled and KKT-tested either by

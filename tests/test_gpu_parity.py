@@ -231,6 +231,48 @@ def test_engine_batch_matches_oracle(oracle_lib, mode):
         assert _same(rg.box_lbs, ro.box_lbs), p.tag
 
 
+def test_iteration_streamed_in_passes(oracle_lib):
+    """The shape of config 3 scaled down: the exp-sqrt composite at n = 16 split
+    in 2 parts per coordinate (2^16 children per iteration, every first-level
+    child touching the minimiser at the centre of the domain), solved in one
+    children pass per iteration and in passes of 4096 and of 1000 children
+    (the candidate queue refilled 16 and 66 times per iteration): every trace
+    equals the oracle's."""
+    p = P.instance(P.EXPSQRT, 16, 7, 1e-4, split=(2, 16))
+    p.max_iter = 4
+    ro = oracle_lib.solve(p, box_cap=16, trace_cap=64)
+    assert ro.trace["n_surv"][0] == 1 << 16          # nothing of the first split can be ruled out
+    for chunk in (0, 4096, 1000):
+        with G.Engine(max_slots=1, arena_bytes=1 << 30, chunk_children=chunk) as eng:
+            eng.submit(p, box_cap=16, trace_cap=64)
+            eng.run(0)
+            (_, rg), = eng.poll()
+        assert (rg.iterations, rg.lb, rg.ub, rg.pool_size, rg.status) == \
+            (ro.iterations, ro.lb, ro.ub, ro.pool_size, G.ITER_LIMIT), chunk
+        for k in ("ub", "n_surv", "pool", "sel"):
+            assert _same(rg.trace[k], ro.trace[k]), (chunk, k)
+        assert _same(rg.box_lbs, ro.box_lbs), chunk
+
+
+def test_batch_streamed_in_passes(oracle_lib):
+    """A mixed batch whose children passes end inside instances: instances are
+    updated only after the iteration's last pass, and every result equals the
+    oracle's."""
+    probs = [make() for _, make in CFGS[:4]] + P.config4(count=10, seed=78, nmax=10)
+    for p in probs:
+        p.max_iter = 3000
+    ros = [oracle_lib.solve(p, box_cap=8, trace_cap=100000) for p in probs]
+    with G.Engine(max_slots=len(probs), arena_bytes=2 << 30, chunk_children=777) as eng:
+        tickets = [eng.submit(p, box_cap=8, trace_cap=100000) for p in probs]
+        eng.run(0)
+        done = dict(eng.poll())
+    for t, p, ro in zip(tickets, probs, ros):
+        rg = done[t]
+        assert (rg.iterations, rg.lb, rg.ub, rg.pool_size) == (ro.iterations, ro.lb, ro.ub, ro.pool_size), p.tag
+        for k in ("ub", "n_surv", "pool", "sel"):
+            assert _same(rg.trace[k], ro.trace[k]), (p.tag, k)
+
+
 EDGE = [
     ("cosquad1", lambda: P.instance(P.COSQUAD, 1, 31, 1e-6)),
     ("chained2_s1", lambda: P.instance(P.CHAINED, 2, 32, 1e-6, samples=1)),
