@@ -468,7 +468,8 @@ def run_batched(args):
     from gpugo_gb300 import problems as P
     probs = P.config4(count=args.count)
     t0 = time.perf_counter()
-    tuned = A.tune(probs, sample=min(512, args.count),
+    tuned = A.tune(probs, sample=min(512, args.count), n_classes=tuple(A.SMALL_FANOUT) + A.N_CLASSES,
+                   fanout_options=dict(A.SMALL_FANOUT), per_class=32,
                    timer=lambda ps, cfg: A.time_engine(ps, cfg, arena_bytes=args.arena_gb << 30))
     tune_s = time.perf_counter() - t0
     probs = tuned.apply(probs)
@@ -493,7 +494,8 @@ def run_batched(args):
             "batched_wall_s": t_b, "plain_wall_s": t_plain, "speedup_vs_plain": t_plain / t_b,
             "identical_to_plain": same, "engine": ecfg.label(),
             "autotune": {"seconds": tune_s, "fanout": {f"{lo}-{hi}": list(v) for (lo, hi), v in tuned.fanout.items()},
-                         "matches_table": tuned.fanout == A.TUNED_FANOUT, "trials": tuned.trials}}
+                         "matches_table": all(tuned.fanout.get(c) == v for c, v in A.TUNED_FANOUT.items()),
+                         "trials": tuned.trials}}
 
 
 def run_list_pass(args):
@@ -511,7 +513,7 @@ def run_list_pass(args):
     p = P.Problem(P.COSQUAD, n, np.tile([-5.5, 6.0], n), np.concatenate([np.ones(n), np.full(n, 10.0), np.ones(n)]),
                   wid=4, group=10, samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6,
                   max_iter=args.steps, pool_cap=1 << 26)
-    with G.Engine(max_slots=1, arena_bytes=8 << 30) as eng:
+    with G.Engine(max_slots=1, arena_bytes=8 << 30, threads=args.threads) as eng:
         eng.submit(p, box_cap=4, trace_cap=4096)
         eng.run(0)
         (_, r), = eng.poll()
@@ -530,7 +532,7 @@ def run_list_pass(args):
     best = max(big, key=lambda d: d["GBps"]) if big else None
     return {"metric": "list pass GB/s (algorithmic)", "value": best["GBps"] if best else None, "unit": "GB/s",
             "n_gpus": 1, "dtype": "f64/u64", "config": {"workload": "rastrigin50 reference loop, 4^10 children/iter",
-                                                      "iterations": int(st.shape[0])},
+                                                      "iterations": int(st.shape[0]), "threads": args.threads},
             "per_iteration": per}
 
 
@@ -642,6 +644,7 @@ def main():
     ap.add_argument("--slice", type=int, default=16)
     ap.add_argument("--arena-gb", type=int, default=80)
     ap.add_argument("--pool-gb", type=int, default=64, help="cfg3-full: list cap (two buffers)")
+    ap.add_argument("--threads", type=int, default=256, help="listpass: threads per block (256 or 512)")
     ap.add_argument("--cpu-instances", type=int, default=64, help="batch instances the CPU baseline solves")
     ap.add_argument("--no-plain", dest="plain", action="store_false",
                     help="skip the plain one-instance-per-launch comparison")

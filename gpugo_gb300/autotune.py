@@ -32,6 +32,16 @@ from .problems import Problem
 FANOUT_OPTIONS: tuple[tuple[int, int], ...] = ((3, 4), (3, 5), (3, 6), (3, 8), (5, 4), (5, 5), (3, 10))
 # dimension classes for the fan-out choice (instances with n < 8 keep the default table)
 N_CLASSES: tuple[tuple[int, int], ...] = ((8, 16), (17, 32), (33, 64), (65, 4096))
+# the small dimensions, one class each, with their own options (the default
+# table's split first; odd wid, wid^min(group, n) children per iteration)
+SMALL_FANOUT: dict[tuple[int, int], tuple[tuple[int, int], ...]] = {
+    (2, 2): ((31, 2), (15, 2), (9, 2), (7, 2), (5, 2)),
+    (3, 3): ((9, 3), (7, 3), (5, 3), (3, 3)),
+    (4, 4): ((7, 4), (5, 4), (3, 4)),
+    (5, 5): ((5, 5), (3, 5), (5, 4), (3, 4)),
+    (6, 6): ((5, 6), (3, 6), (5, 5), (3, 5), (5, 4)),
+    (7, 7): ((3, 7), (3, 6), (5, 5), (3, 5)),
+}
 
 
 @dataclass(frozen=True)
@@ -116,10 +126,12 @@ def sample_problems(problems: Sequence[Problem], k: int) -> list[Problem]:
 
 
 def tune(problems: Sequence[Problem], sample: int = 512, configs: Sequence[EngineConfig] = ENGINE_CONFIGS,
-         fanout_options: Sequence[tuple[int, int]] = FANOUT_OPTIONS,
+         fanout_options: Sequence[tuple[int, int]] | dict = FANOUT_OPTIONS,
          n_classes: Sequence[tuple[int, int]] = N_CLASSES, per_class: int = 16,
          timer: Callable[[Sequence[Problem], EngineConfig], float] = time_engine) -> TuneResult:
-    """Pick the engine configuration, then the fan-out per dimension class."""
+    """Pick the engine configuration, then the fan-out per dimension class.
+    ``fanout_options`` is one list of splits for every class, or a dict of
+    class -> splits (a class missing from it takes FANOUT_OPTIONS)."""
     trials: list[dict] = []
     base = sample_problems(problems, sample)
     best_cfg, best_t = configs[0], math.inf
@@ -135,7 +147,8 @@ def tune(problems: Sequence[Problem], sample: int = 512, configs: Sequence[Engin
             continue
         members = sample_problems(members, per_class)
         best_split, best_ts = None, math.inf
-        for wid, group in fanout_options:
+        options = fanout_options.get((lo, hi), FANOUT_OPTIONS) if isinstance(fanout_options, dict) else fanout_options
+        for wid, group in options:
             if wid ** min(group, lo) > 2 ** 32:
                 continue
             trial = [dataclasses.replace(p, wid=wid, group=group) for p in members]

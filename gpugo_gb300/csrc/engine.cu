@@ -1433,7 +1433,6 @@ __device__ void phase_candidates(const KArgs& a) {
 // to memory per tile.
 constexpr int POOL_STAGES = 3;
 constexpr int POOL_STAGE_BYTES = TD * 16;   // LB slice, then key slice
-constexpr int POOL_PER = TD / 256;          // entries per thread and tile (256 or 512 threads)
 static_assert(POOL_STAGES * POOL_STAGE_BYTES <= SMEM_TAB_BYTES, "pool stages exceed the dynamic shared memory");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -1478,54 +1477,75 @@ struct PoolTile {
   int s, cur, compact, tile;
 };
 
+// Each warp filters its own contiguous quarter/eighth of a tile, reserves the
+// places of its survivors with one atomicAdd and writes them in order (its
+// stores are contiguous); the block meets once per tile, to combine the warps'
+// minima and to hand the stage to the next copy.
 __device__ void phase_pool(const KArgs& a) {
   extern __shared__ __align__(16) double s_tab[];
   __shared__ __align__(8) unsigned long long s_bar[POOL_STAGES];
   __shared__ PoolTile s_meta[POOL_STAGES];
-  __shared__ unsigned int s_cnt[POOL_PER * (MAX_THREADS / 32)];   // survivors per (round, warp)
-  __shared__ unsigned long long s_base;
+  __shared__ Best s_wbest[2][MAX_THREADS / 32];   // per warp, double-buffered by tile parity
   __shared__ int s_fail;
   const long long tot = a.ctl->totD;
   const int nB = a.ctl->nBig;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int per = TD / blockDim.x;
+  const int span = TD / nw;        // entries per warp and tile: 256 (8 warps) or 128 (16 warps)
+  const int rounds = span >> 5;    // 8 or 4
   const long long mine = (long long)blockIdx.x < tot ? (tot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   if (mine == 0) return;   // the same for every thread of the block
   char* smem = (char*)s_tab;
-  int hint = -1;
-  // thread 0: tile j of this block into stage j % POOL_STAGES.  The stage's
-  // earlier contents were read by every thread before the __syncthreads that
-  // precedes this call; the proxy fence orders those reads before the copy.
+  // the current instance's fields (stable during this phase), kept by thread 0
+  // in shared memory: consecutive tiles of a block mostly belong to one instance
+  struct InstCache {
+    PoolTile m;
+    long long start, end, cnt;
+    const double* lb;
+    const unsigned long long* key;
+    int k;
+  };
+  __shared__ InstCache s_inst;
+  // thread 0: tile j of this block into stage j % POOL_STAGES.  Every thread has
+  // finished with the stage's earlier contents (block barrier before the call);
+  // the proxy fence orders those reads before the copy's writes.
   auto issue = [&](long long j) {
     const int k = (int)(j % POOL_STAGES);
     const long long t = blockIdx.x + j * gridDim.x;
-    const int sk = find_seg(a.prefD, nB, t, hint);
-    hint = sk;
-    PoolTile m;
-    m.s = a.idsE[sk];
-    const Desc& D = a.desc[m.s];
-    const State& st = a.st[m.s];
-    const long long count = vload(st.count);
-    const long long cnt = count < D.pool_cap ? count : D.pool_cap;
-    const unsigned long long ubk = vload(st.ub);
-    m.tile = (int)(t - a.prefD[sk]);
+    InstCache& c = s_inst;
+    if (t >= c.end) {
+      c.k = find_seg(a.prefD, nB, t, c.k);
+      c.start = a.prefD[c.k];
+      c.end = a.prefD[c.k + 1];
+      c.m.s = a.idsE[c.k];
+      const Desc& D = a.desc[c.m.s];
+      const State& st = a.st[c.m.s];
+      const long long count = vload(st.count);
+      c.cnt = count < D.pool_cap ? count : D.pool_cap;
+      const unsigned long long ubk = vload(st.ub);
+      c.m.cur = vload(st.cur);
+      c.m.compact = ubk != vload(st.ub_start);
+      c.m.ub = ord_val(ubk);
+      c.m.count_before = vload(st.count_before);
+      c.lb = D.pool_lb[c.m.cur];
+      c.key = D.pool_key[c.m.cur];
+    }
+    PoolTile m = c.m;
+    m.tile = (int)(t - c.start);
     m.lo = (long long)m.tile * TD;
-    m.hi = min(cnt, m.lo + TD);
-    m.cur = vload(st.cur);
-    m.compact = ubk != vload(st.ub_start);
-    m.ub = ord_val(ubk);
-    m.count_before = vload(st.count_before);
+    m.hi = min(c.cnt, m.lo + TD);
     s_meta[k] = m;
     // an even number of entries: 16-byte multiples from a 16 KB-aligned tile start
     const unsigned pair = (unsigned)((m.hi - m.lo) & ~1LL);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_arrive_expect_tx(&s_bar[k], pair * 16u);
     if (pair) {
-      bulk_load(smem + k * POOL_STAGE_BYTES, D.pool_lb[m.cur] + m.lo, pair * 8u, &s_bar[k]);
-      bulk_load(smem + k * POOL_STAGE_BYTES + TD * 8, D.pool_key[m.cur] + m.lo, pair * 8u, &s_bar[k]);
+      bulk_load(smem + k * POOL_STAGE_BYTES, c.lb + m.lo, pair * 8u, &s_bar[k]);
+      bulk_load(smem + k * POOL_STAGE_BYTES + TD * 8, c.key + m.lo, pair * 8u, &s_bar[k]);
     }
   };
   if (threadIdx.x == 0) {
+    s_inst.k = -1;
+    s_inst.end = -1;
     for (int k = 0; k < POOL_STAGES; ++k) mbar_init(&s_bar[k], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_fail = 0;
@@ -1536,92 +1556,83 @@ __device__ void phase_pool(const KArgs& a) {
   for (long long j = 0; j < mine; ++j) {
     const int k = (int)(j % POOL_STAGES);
     const unsigned parity = (unsigned)((j / POOL_STAGES) & 1);
-    if (!mbar_wait(&s_bar[k], parity, a.timeout_ns)) {
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&s_bar[k], parity, a.timeout_ns));
+    Best b = best_none();
+    if (ok) {
+      const PoolTile m = s_meta[k];
+      const Desc& D = a.desc[m.s];
+      State& st = a.st[m.s];
+      const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
+      const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
+      const long long n = m.hi - m.lo, pair = n & ~1LL;
+      // entry i of the tile: from the stage, or (the odd last entry of a list, not
+      // in the bulk copy) from global memory
+      auto entry_lb = [&](long long i) { return i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i); };
+      auto entry_key = [&](long long i) { return i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i); };
+      const long long w0 = (long long)wid * span;
+      unsigned bal[TD / 256];   // survivors of each round of 32 (warp-uniform)
+      unsigned tk = 0;
+      long long removed_new = 0;
+#pragma unroll
+      for (int r = 0; r < TD / 256; ++r) {
+        bal[r] = 0;
+        if (r < rounds) {
+          const long long i = w0 + r * 32 + lane;
+          const bool in = i < n;
+          const bool keep = in && (!m.compact || !flt(m.ub, entry_lb(i)));
+          if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
+          bal[r] = __ballot_sync(0xffffffffu, keep);
+          tk += __popc(bal[r]);
+        }
+      }
+      unsigned long long base = 0;
+      if (m.compact) {
+        if (lane == 0 && tk) base = atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+      }
+      unsigned pre = 0;
+#pragma unroll
+      for (int r = 0; r < TD / 256; ++r) {
+        if (r < rounds) {
+          const long long i = w0 + r * 32 + lane;
+          if ((bal[r] >> lane) & 1u) {
+            const double lv = entry_lb(i);
+            const unsigned long long kv = entry_key(i);
+            unsigned long long pos = (unsigned long long)(m.lo + i);
+            if (m.compact) {
+              pos = base + pre + __popc(bal[r] & ((1u << lane) - 1u));
+              D.pool_lb[m.cur ^ 1][pos] = lv;
+              D.pool_key[m.cur ^ 1][pos] = kv;
+            }
+            Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
+            if (best_less(c, b)) b = c;
+          }
+          pre += __popc(bal[r]);
+        }
+      }
+      if (m.compact) {
+        for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
+        if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
+      }
+    } else if (lane == 0) {
       atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT);
       s_fail = 1;
     }
-    __syncthreads();
+    b = warp_min(b);
+    if (lane == 0) s_wbest[j & 1][wid] = b;
+    __syncthreads();   // every warp is done with the stage and has posted its minimum
     if (s_fail) break;
     waited = j + 1;
-    const PoolTile m = s_meta[k];
-    const Desc& D = a.desc[m.s];
-    State& st = a.st[m.s];
-    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
-    const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
-    const long long n = m.hi - m.lo, pair = n & ~1LL;
-    // entry i of the tile: from the stage, or (the odd last entry of a list, not
-    // in the bulk copy) from global memory
-    auto entry_lb = [&](long long i) { return i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i); };
-    auto entry_key = [&](long long i) { return i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i); };
-    unsigned keepm = 0;
-    long long removed_new = 0;
-#pragma unroll
-    for (int r = 0; r < POOL_PER; ++r) {
-      const long long i = threadIdx.x + (long long)r * blockDim.x;
-      const bool in = r < per && i < n;
-      const bool keep = in && (!m.compact || !flt(m.ub, entry_lb(i)));
-      if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
-      keepm |= keep ? (1u << r) : 0u;
-      if (m.compact && r < per) {
-        const unsigned b = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) s_cnt[r * nw + wid] = __popc(b);
+    if (wid == 0) {
+      Best c = lane < nw ? s_wbest[j & 1][lane] : best_none();
+      c = warp_min(c);
+      if (lane == 0) {
+        const PoolTile& m = s_meta[k];
+        unsigned long long* tb = a.desc[m.s].tile_best + 3 * m.tile;
+        tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
+        if (j + POOL_STAGES < mine) issue(j + POOL_STAGES);
       }
     }
-    if (m.compact) {
-      __syncthreads();
-      // exclusive prefix of the survivor counts in tile order (round, warp, lane):
-      // survivors keep their order, and each warp's stores are contiguous
-      if (wid == 0) {
-        const int nc = per * nw;   // TD / 32 = 64
-        unsigned c0 = lane < nc ? s_cnt[lane] : 0u, c1 = lane + 32 < nc ? s_cnt[lane + 32] : 0u;
-        unsigned x0 = c0, x1 = c1;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          unsigned y0 = __shfl_up_sync(0xffffffffu, x0, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
-          if (lane >= o) { x0 += y0; x1 += y1; }
-        }
-        const unsigned t0 = __shfl_sync(0xffffffffu, x0, 31);
-        x1 += t0;
-        const unsigned tk = __shfl_sync(0xffffffffu, x1, 31);
-        if (lane < nc) s_cnt[lane] = x0 - c0;
-        if (lane + 32 < nc) s_cnt[lane + 32] = x1 - c1;
-        if (lane == 0) s_base = tk ? atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk) : 0ULL;
-      }
-      __syncthreads();
-    }
-    Best b = best_none();
-#pragma unroll
-    for (int r = 0; r < POOL_PER; ++r) {
-      const bool keep = (keepm >> r) & 1u;
-      const long long i = threadIdx.x + (long long)r * blockDim.x;
-      unsigned long long pos = (unsigned long long)(m.lo + i);
-      double lv = 0.0;
-      unsigned long long kv = 0ULL;
-      if (keep) { lv = entry_lb(i); kv = entry_key(i); }
-      if (m.compact && r < per) {
-        const unsigned bm = __ballot_sync(0xffffffffu, keep);
-        pos = s_base + s_cnt[r * nw + wid] + __popc(bm & ((1u << lane) - 1u));
-        if (keep) {
-          D.pool_lb[m.cur ^ 1][pos] = lv;
-          D.pool_key[m.cur ^ 1][pos] = kv;
-        }
-      }
-      if (keep) {
-        Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
-        if (best_less(c, b)) b = c;
-      }
-    }
-    if (m.compact) {
-      for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
-      if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
-    }
-    b = block_min(b);   // synchronises: every thread is done with the stage
-    if (threadIdx.x == 0) {
-      unsigned long long* tb = D.tile_best + 3 * m.tile;
-      tb[0] = b.lbk; tb[1] = b.key; tb[2] = b.idx;
-      if (j + POOL_STAGES < mine) issue(j + POOL_STAGES);
-    }
-    __syncthreads();
   }
   // after an expired wait: wait (bounded again) for the copies still in flight
   // before the shared memory is used for anything else
