@@ -317,8 +317,8 @@ def run_batch(args, dist):
                    "l2": "flushed between steps (256 MiB write)",
                    "engine": ecfg.label(), "engine_tuning_s": tune_s,
                    "engine_trials": [{"config": t["config"], "seconds": round(t["seconds"], 4)} for t in trials],
-                   "fanout": "3 parts per coordinate: 3^5 children per iteration for n in 8..16, 3^6 above "
-                             "(the autotuner's table); n < 8 the default splits",
+                   "fanout": "the autotuner's table: 3^5 children per iteration for n = 5 and n in 8..16, 3^6 "
+                             "for n = 6 and above 16, 3^7 for n = 7, 7^4 / 9^3 / 31^2 for n = 4 / 3 / 2",
                    "instances": len(probs), "certified": sum(r.certified for r in res),
                    "boxes_per_step": boxes // args.steps, "samples_per_step": sampled // args.steps,
                    "iterations_max": max(r.iterations for r in res),

@@ -57,11 +57,15 @@ class EngineConfig:
 
 # The fan-out this tuner chose on a GB300 for the mixed batch of generated
 # instances (families F1-F4, n log-uniform in 2..64 and 2..128): three parts per
-# coordinate, 3^5 children per iteration for n <= 16 and 3^6 above.  Workloads
-# that must solve identical problems in several runs (a GPU run and a CPU
-# baseline) apply this table instead of tuning the fan-out again.
-TUNED_FANOUT: dict[tuple[int, int], tuple[int, int]] = {(8, 16): (3, 5), (17, 32): (3, 6), (33, 64): (3, 6),
-                                                        (65, 4096): (3, 6)}
+# coordinate, 3^5 children per iteration for n <= 16 and 3^6 above; for the
+# small dimensions the default table's split except at n = 5 and n = 6, where
+# three parts per coordinate (3^5, 3^6 children) certified the class's sample
+# 7x and 14x faster than five parts (5^5, 5^6).  Workloads that must solve
+# identical problems in several runs (a GPU run and a CPU baseline) apply this
+# table instead of tuning the fan-out again.
+TUNED_FANOUT: dict[tuple[int, int], tuple[int, int]] = {
+    (2, 2): (31, 2), (3, 3): (9, 3), (4, 4): (7, 4), (5, 5): (3, 5), (6, 6): (3, 6), (7, 7): (3, 7),
+    (8, 16): (3, 5), (17, 32): (3, 6), (33, 64): (3, 6), (65, 4096): (3, 6)}
 
 ENGINE_CONFIGS: tuple[EngineConfig, ...] = (
     EngineConfig(256, 0, _lib.CAND_AUTO),
