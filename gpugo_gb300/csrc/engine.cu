@@ -51,7 +51,7 @@ struct NvtxRange {
 
 namespace gg {
 
-constexpr int TD = 1024;           // pool entries per list-pass tile
+constexpr int TD = 2048;           // pool entries per phase-D tile
 constexpr int MAX_THREADS = 512;  // block size is 256 or 512
 
 // instance life cycle
@@ -103,7 +103,6 @@ struct Ctl {
   int nE;                     // instances active this iteration
   int nBig;                   // instances whose pool takes the grid-wide path
   long long totA, totB, totD; // flat work sizes
-  long long totA2;            // table items built during the bound pass
   long long iters;            // iterations run by the last launch
   int q_tail;                 // ready queue: slots reserved
   int q_head;                 // ready queue: slots claimed
@@ -123,8 +122,7 @@ struct KArgs {
   State* st;
   Ctl* ctl;
   int* idsA;                  // [max_slots] expanding instances
-  long long* prefA;           // [max_slots + 1] prefix of the table items the bound pass reads
-  long long* prefA2;          // [max_slots + 1] prefix of the other table items (built during the bound pass)
+  long long* prefA;           // [max_slots + 1] table items prefix
   long long* prefB;           // [max_slots + 1] children prefix
   int* idsE;                  // [max_slots] big-pool instances (grid-wide path)
   long long* prefD;           // [max_slots + 1] pool tiles prefix of big instances
@@ -271,38 +269,32 @@ __device__ void build_lists_warp(const KArgs& a) {
   const bool have = s < a.max_slots;
   const int stt = have ? a.st[s].status : ST_DONE;
   const bool ex = stt == ST_EXPAND, rp = stt == ST_REPOP;
-  const long long items = ex ? lb_items(a.desc[s]) : 0, items2 = ex ? a.desc[s].a_items - items : 0;
-  const long long kids = ex ? a.st[s].m_children : 0;
+  const long long items = ex ? a.desc[s].a_items : 0, kids = ex ? a.st[s].m_children : 0;
   const unsigned mA = __ballot_sync(0xffffffffu, ex), mR = __ballot_sync(0xffffffffu, rp);
   const unsigned mE = __ballot_sync(0xffffffffu, ex || rp);
   const unsigned below = (1u << lane) - 1u;
-  long long pA = items, pA2 = items2, pB = kids;   // inclusive scans
+  long long pA = items, pB = kids;   // inclusive scans
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     long long ya = __shfl_up_sync(0xffffffffu, pA, o), yb = __shfl_up_sync(0xffffffffu, pB, o);
-    long long y2 = __shfl_up_sync(0xffffffffu, pA2, o);
-    if (lane >= o) { pA += ya; pB += yb; pA2 += y2; }
+    if (lane >= o) { pA += ya; pB += yb; }
   }
   if (ex) {
     const int o = __popc(mA & below);
     a.idsA[o] = s;
     a.prefA[o] = pA - items;
-    a.prefA2[o] = pA2 - items2;
     a.prefB[o] = pB - kids;
   }
   if (rp) a.queue[__popc(mR & below)] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
   const long long totA = __shfl_sync(0xffffffffu, pA, 31), totB = __shfl_sync(0xffffffffu, pB, 31);
-  const long long totA2 = __shfl_sync(0xffffffffu, pA2, 31);
   __syncwarp();
   if (lane == 0) {
     const int nA = __popc(mA);
     a.prefA[nA] = totA;
-    a.prefA2[nA] = totA2;
     a.prefB[nA] = totB;
     a.ctl->nA = nA;
     a.ctl->nE = __popc(mE);
     a.ctl->totA = totA;
-    a.ctl->totA2 = totA2;
     a.ctl->totB = totB;
     a.ctl->q_tail = __popc(mR);
     a.ctl->q_head = 0;
@@ -335,46 +327,39 @@ __device__ void build_lists(const KArgs& a) {
   long long tE, tR;
   block_exclusive_scan(cE, &tE);
   long long oR = block_exclusive_scan(cR, &tR);
-  long long baseA = 0, baseSA = 0, baseSA2 = 0, baseSB = 0;
+  long long baseA = 0, baseSA = 0, baseSB = 0;
   for (int f = grouped ? 1 : 0; f <= (grouped ? a.fam_hi : 0); ++f) {
-    long long cA = 0, sA = 0, sA2 = 0, sB = 0;
+    long long cA = 0, sA = 0, sB = 0;
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
-        const long long li = lb_items(a.desc[s]);
-        cA++; sA += li; sA2 += a.desc[s].a_items - li; sB += a.st[s].m_children;
+        cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children;
       }
     }
-    long long tA, tSA, tSA2, tSB;
+    long long tA, tSA, tSB;
     long long oA = baseA + block_exclusive_scan(cA, &tA);
     long long oSA = baseSA + block_exclusive_scan(sA, &tSA);
-    long long oSA2 = baseSA2 + block_exclusive_scan(sA2, &tSA2);
     long long oSB = baseSB + block_exclusive_scan(sB, &tSB);
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
-        const long long li = lb_items(a.desc[s]);
         a.idsA[oA] = s;
         a.prefA[oA] = oSA;
-        a.prefA2[oA] = oSA2;
         a.prefB[oA] = oSB;
         oA++;
-        oSA += li;
-        oSA2 += a.desc[s].a_items - li;
+        oSA += a.desc[s].a_items;
         oSB += a.st[s].m_children;
       }
     }
-    baseA += tA; baseSA += tSA; baseSA2 += tSA2; baseSB += tSB;
+    baseA += tA; baseSA += tSA; baseSB += tSB;
   }
   for (int s = lo; s < hi; ++s)
     if (a.st[s].status == ST_REPOP) a.queue[oR++] = ((unsigned long long)(a.ctl->epoch + 1) << 32) | (unsigned)s;
   __syncthreads();
   if (threadIdx.x == 0) {
     a.prefA[baseA] = baseSA;
-    a.prefA2[baseA] = baseSA2;
     a.prefB[baseA] = baseSB;
     a.ctl->nA = (int)baseA;
     a.ctl->nE = (int)tE;
     a.ctl->totA = baseSA;
-    a.ctl->totA2 = baseSA2;
     a.ctl->totB = baseSB;
     a.ctl->q_tail = (int)tR;
     a.ctl->q_head = 0;
@@ -495,35 +480,10 @@ __device__ void phase_tables(const KArgs& a) {
     int s = a.idsA[k];
     const Desc& D = a.desc[s];
     const State& st = a.st[s];
-    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc,
-                   D.lb_lo + (it - a.prefA[k]));
+    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k]);
   }
   __syncthreads();
   bstamp(a, 1);
-}
-
-// The other table items (sample points, KKT flags), built by the bound pass's
-// warps before their children: nothing reads them before the pass ends.
-template <bool CL>
-__device__ __noinline__ void deferred_tables(const KArgs& a) {
-  const long long tot = a.ctl->totA2;
-  const int nA = a.ctl->nA;
-  const int lane = threadIdx.x & 31;
-  const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long w = ((long long)(threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
-  int hint = -1;
-  for (long long base = w * 32; base < tot; base += W * 32) {
-    long long it = base + lane;
-    if (it >= tot) continue;
-    int k = find_seg(a.prefA2, nA, it, hint);
-    hint = k;
-    int s = a.idsA[k];
-    const Desc& D = a.desc[s];
-    const State& st = a.st[s];
-    long long u = it - a.prefA2[k];
-    if (u >= D.lb_lo) u += D.lb_hi - D.lb_lo;
-    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, u);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1090,7 +1050,6 @@ __device__ void phase_bound(const KArgs& a) {
   extern __shared__ __align__(16) double s_tab[];
   const int si = stage_tables(a);
   const long long lo = vload(a.ctl->b_lo), tot = vload(a.ctl->b_hi);   // this pass's children
-  if (lo == 0) deferred_tables<CL>(a);
   const int nA = a.ctl->nA;
   const int lane = threadIdx.x & 31;
   const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -1157,10 +1116,22 @@ __device__ void phase_bound(const KArgs& a) {
         if (lane == leader) atomicAdd((unsigned long long*)&a.st[ls].cand_total, (unsigned long long)__popc(m));
         act &= ~m;
       }
-    } else if (lane == 0) {
-      // a pass has at most a.chunk <= cand_cap children, so the queue cannot
-      // fill up; this is a guard, not a path
-      atomicCAS(&a.ctl->error, 0, GPUGO_ERR_POOL_OVERFLOW);
+    } else {
+      // queue full: process these candidates right here
+      bool keep = false;
+      while (cm) {
+        int b = __ffs(cm) - 1;
+        cm &= cm - 1;
+        int cs = __shfl_sync(0xffffffffu, s, b);
+        unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
+        double cl = shfl_d(lb, b);
+        double ca[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) ca[q] = shfl_d(aux[q], b);
+        bool kk = warp_candidate<CL>(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
+        if (lane == b) keep = kk;
+      }
+      warp_append_survivors(a, keep, s, code, lb);
     }
   }
   __syncthreads();
@@ -1460,11 +1431,9 @@ __device__ void phase_candidates(const KArgs& a) {
 // phases.  While a tile is filtered and its survivors written, the copies of
 // the next two are under way, so the block never waits for a whole round trip
 // to memory per tile.
-constexpr int POOL_TEAMS = 2;              // independent warp teams per block
-constexpr int POOL_STAGES = 3;             // tiles in flight per team
-constexpr int POOL_STAGE_BYTES = TD * 16;  // LB slice, then key slice
-static_assert(POOL_TEAMS * POOL_STAGES * POOL_STAGE_BYTES <= SMEM_TAB_BYTES,
-              "pool stages exceed the dynamic shared memory");
+constexpr int POOL_STAGES = 3;
+constexpr int POOL_STAGE_BYTES = TD * 16;   // LB slice, then key slice
+static_assert(POOL_STAGES * POOL_STAGE_BYTES <= SMEM_TAB_BYTES, "pool stages exceed the dynamic shared memory");
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -1508,52 +1477,41 @@ struct PoolTile {
   int s, cur, compact, tile;
 };
 
-// the current instance's fields (stable during the pass), kept by a team's
-// leader: consecutive tiles of a block mostly belong to one instance
-struct PoolInst {
-  PoolTile m;
-  long long start, end, cnt;
-  const double* lb;
-  const unsigned long long* key;
-  int k;
-};
-
-__device__ __forceinline__ void team_sync(int team, int nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(nthreads) : "memory");
-}
-
-// The block's tiles alternate between two teams of warps (half the block each),
-// which run independently: each has its own ring of stages and meets only its
-// own members once per tile (a named barrier), so one team's waits (the atomic
-// that reserves its survivors' places, its stage's copy) overlap the other's
-// work.  Inside a team each warp filters its own contiguous part of the tile,
-// reserves its survivors' places with one atomicAdd and writes them in order.
+// Each warp filters its own contiguous quarter/eighth of a tile, reserves the
+// places of its survivors with one atomicAdd and writes them in order (its
+// stores are contiguous); the block meets once per tile, to combine the warps'
+// minima and to hand the stage to the next copy.
 __device__ __noinline__ void phase_pool(const KArgs& a) {
   extern __shared__ __align__(16) double s_tab[];
-  __shared__ __align__(8) unsigned long long s_bar[POOL_TEAMS][POOL_STAGES];
-  __shared__ PoolTile s_meta[POOL_TEAMS][POOL_STAGES];
-  __shared__ Best s_wbest[POOL_TEAMS][2][MAX_THREADS / 64];   // per warp, by tile parity
-  __shared__ PoolInst s_inst[POOL_TEAMS];
-  __shared__ int s_fail[POOL_TEAMS];
+  __shared__ __align__(8) unsigned long long s_bar[POOL_STAGES];
+  __shared__ PoolTile s_meta[POOL_STAGES];
+  __shared__ Best s_wbest[2][2][MAX_THREADS / 32];   // per warp and tile of a pair, by pair parity
+  __shared__ int s_fail;
   const long long tot = a.ctl->totD;
   const int nB = a.ctl->nBig;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int span = TD / nw;        // entries per warp and tile: 256 (8 warps) or 128 (16 warps)
+  const int rounds = span >> 5;    // 8 or 4
   const long long mine = (long long)blockIdx.x < tot ? (tot - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   if (mine == 0) return;   // the same for every thread of the block
-  const int tsize = blockDim.x / POOL_TEAMS;           // threads per team
-  const int team = threadIdx.x / tsize, tt = threadIdx.x - team * tsize;
-  const int lane = tt & 31, wid = tt >> 5, nw = tsize >> 5;
-  const int span = TD / nw;        // entries per warp and tile: 256 (4 warps) or 128 (8 warps)
-  const int rounds = span >> 5;    // 8 or 4
-  const long long mt = (mine - team + POOL_TEAMS - 1) / POOL_TEAMS;   // this team's tiles
-  char* smem = (char*)s_tab + (size_t)team * POOL_STAGES * POOL_STAGE_BYTES;
-  unsigned long long* bar = s_bar[team];
-  // the team leader: the team's tile q into stage q % POOL_STAGES.  Every member
-  // has finished with the stage's earlier contents (team barrier before the
-  // call); the proxy fence orders those reads before the copy's writes.
-  auto issue = [&](long long q) {
-    const int k = (int)(q % POOL_STAGES);
-    const long long t = blockIdx.x + (q * POOL_TEAMS + team) * gridDim.x;
-    PoolInst& c = s_inst[team];
+  char* smem = (char*)s_tab;
+  // the current instance's fields (stable during this phase), kept by thread 0
+  // in shared memory: consecutive tiles of a block mostly belong to one instance
+  struct InstCache {
+    PoolTile m;
+    long long start, end, cnt;
+    const double* lb;
+    const unsigned long long* key;
+    int k;
+  };
+  __shared__ InstCache s_inst;
+  // thread 0: tile j of this block into stage j % POOL_STAGES.  Every thread has
+  // finished with the stage's earlier contents (block barrier before the call);
+  // the proxy fence orders those reads before the copy's writes.
+  auto issue = [&](long long j) {
+    const int k = (int)(j % POOL_STAGES);
+    const long long t = blockIdx.x + j * gridDim.x;
+    InstCache& c = s_inst;
     if (t >= c.end) {
       c.k = find_seg(a.prefD, nB, t, c.k);
       c.start = a.prefD[c.k];
@@ -1575,124 +1533,148 @@ __device__ __noinline__ void phase_pool(const KArgs& a) {
     m.tile = (int)(t - c.start);
     m.lo = (long long)m.tile * TD;
     m.hi = min(c.cnt, m.lo + TD);
-    s_meta[team][k] = m;
+    s_meta[k] = m;
     // an even number of entries: 16-byte multiples from a 16 KB-aligned tile start
     const unsigned pair = (unsigned)((m.hi - m.lo) & ~1LL);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive_expect_tx(&bar[k], pair * 16u);
+    mbar_arrive_expect_tx(&s_bar[k], pair * 16u);
     if (pair) {
-      bulk_load(smem + k * POOL_STAGE_BYTES, c.lb + m.lo, pair * 8u, &bar[k]);
-      bulk_load(smem + k * POOL_STAGE_BYTES + TD * 8, c.key + m.lo, pair * 8u, &bar[k]);
+      bulk_load(smem + k * POOL_STAGE_BYTES, c.lb + m.lo, pair * 8u, &s_bar[k]);
+      bulk_load(smem + k * POOL_STAGE_BYTES + TD * 8, c.key + m.lo, pair * 8u, &s_bar[k]);
     }
   };
   if (threadIdx.x == 0) {
-    for (int g = 0; g < POOL_TEAMS; ++g) {
-      for (int k = 0; k < POOL_STAGES; ++k) mbar_init(&s_bar[g][k], 1);
-      s_inst[g].k = -1;
-      s_inst[g].end = -1;
-      s_fail[g] = 0;
-    }
+    s_inst.k = -1;
+    s_inst.end = -1;
+    for (int k = 0; k < POOL_STAGES; ++k) mbar_init(&s_bar[k], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+    for (long long j = 0; j < mine && j < POOL_STAGES; ++j) issue(j);
   }
   __syncthreads();
-  if (tt == 0)
-    for (long long q = 0; q < mt && q < POOL_STAGES; ++q) issue(q);
-  long long waited = 0;   // tiles whose copies the team has seen complete
-  for (long long q = 0; q < mt; ++q) {
-    const int k = (int)(q % POOL_STAGES);
-    const unsigned parity = (unsigned)((q / POOL_STAGES) & 1);
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[k], parity, a.timeout_ns));
+  // A warp takes its parts of two tiles at once: it counts the survivors of
+  // both and sends both atomics before it waits for either place, so the
+  // round trip of one atomic overlaps the other tile's work.
+  const long long w0 = (long long)wid * span;
+  auto count = [&](int k, const PoolTile& m, unsigned* bal, unsigned& tk, long long& removed_new) {
+    const Desc& D = a.desc[m.s];
+    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
+    const long long n = m.hi - m.lo, pair = n & ~1LL;
+    tk = 0;
+    removed_new = 0;
+#pragma unroll
+    for (int r = 0; r < TD / 256; ++r) {
+      bal[r] = 0;
+      if (r < rounds) {
+        const long long i = w0 + r * 32 + lane;
+        const bool in = i < n;
+        // the odd last entry of a list is not in the bulk copy
+        const bool keep = in && (!m.compact || !flt(m.ub, i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i)));
+        if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
+        bal[r] = __ballot_sync(0xffffffffu, keep);
+        tk += __popc(bal[r]);
+      }
+    }
+  };
+  auto write = [&](int k, const PoolTile& m, const unsigned* bal, unsigned long long base, long long removed_new) {
+    const Desc& D = a.desc[m.s];
+    State& st = a.st[m.s];
+    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
+    const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
+    const long long pair = (m.hi - m.lo) & ~1LL;
     Best b = best_none();
-    if (ok) {
-      const PoolTile m = s_meta[team][k];
-      const Desc& D = a.desc[m.s];
-      State& st = a.st[m.s];
-      const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
-      const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
-      const long long n = m.hi - m.lo, pair = n & ~1LL;
-      // entry i of the tile: from the stage, or (the odd last entry of a list, not
-      // in the bulk copy) from global memory
-      auto entry_lb = [&](long long i) { return i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i); };
-      auto entry_key = [&](long long i) { return i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i); };
-      const long long w0 = (long long)wid * span;
-      unsigned bal[TD / 128];   // survivors of each round of 32 (warp-uniform)
-      unsigned tk = 0;
-      long long removed_new = 0;
+    unsigned pre = 0;
 #pragma unroll
-      for (int r = 0; r < TD / 128; ++r) {
-        bal[r] = 0;
-        if (r < rounds) {
-          const long long i = w0 + r * 32 + lane;
-          const bool in = i < n;
-          const bool keep = in && (!m.compact || !flt(m.ub, entry_lb(i)));
-          if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
-          bal[r] = __ballot_sync(0xffffffffu, keep);
-          tk += __popc(bal[r]);
-        }
-      }
-      unsigned long long base = 0;
-      if (m.compact) {
-        if (lane == 0 && tk) base = atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk);
-        base = __shfl_sync(0xffffffffu, base, 0);
-      }
-      unsigned pre = 0;
-#pragma unroll
-      for (int r = 0; r < TD / 128; ++r) {
-        if (r < rounds) {
-          const long long i = w0 + r * 32 + lane;
-          if ((bal[r] >> lane) & 1u) {
-            const double lv = entry_lb(i);
-            const unsigned long long kv = entry_key(i);
-            unsigned long long pos = (unsigned long long)(m.lo + i);
-            if (m.compact) {
-              pos = base + pre + __popc(bal[r] & ((1u << lane) - 1u));
-              D.pool_lb[m.cur ^ 1][pos] = lv;
-              D.pool_key[m.cur ^ 1][pos] = kv;
-            }
-            Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
-            if (best_less(c, b)) b = c;
+    for (int r = 0; r < TD / 256; ++r) {
+      if (r < rounds) {
+        const long long i = w0 + r * 32 + lane;
+        if ((bal[r] >> lane) & 1u) {
+          const double lv = i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i);
+          const unsigned long long kv = i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i);
+          unsigned long long pos = (unsigned long long)(m.lo + i);
+          if (m.compact) {
+            pos = base + pre + __popc(bal[r] & ((1u << lane) - 1u));
+            D.pool_lb[m.cur ^ 1][pos] = lv;
+            D.pool_key[m.cur ^ 1][pos] = kv;
           }
-          pre += __popc(bal[r]);
+          Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
+          if (best_less(c, b)) b = c;
         }
+        pre += __popc(bal[r]);
       }
-      if (m.compact) {
-        for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
-        if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
+    }
+    if (m.compact) {
+      for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
+      if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
+    }
+    return warp_min(b);
+  };
+  auto reserve = [&](const PoolTile& m, unsigned tk) {   // lane 0's atomic; used later
+    unsigned long long base = 0;
+    if (m.compact && lane == 0 && tk) base = atomicAdd((unsigned long long*)&a.st[m.s].count_new, (unsigned long long)tk);
+    return base;
+  };
+  long long waited = 0;   // tiles whose copies this block has seen complete
+  for (long long j = 0; j < mine; j += 2) {
+    const bool two = j + 1 < mine;
+    const int k0 = (int)(j % POOL_STAGES), k1 = (int)((j + 1) % POOL_STAGES);
+    bool ok = mbar_wait(&s_bar[k0], (unsigned)((j / POOL_STAGES) & 1), a.timeout_ns);
+    if (two) ok = ok && mbar_wait(&s_bar[k1], (unsigned)(((j + 1) / POOL_STAGES) & 1), a.timeout_ns);
+    ok = __all_sync(0xffffffffu, ok);
+    Best b0 = best_none(), b1 = best_none();
+    if (ok) {
+      const PoolTile m0 = s_meta[k0];
+      PoolTile m1 = m0;
+      if (two) m1 = s_meta[k1];
+      unsigned bal0[TD / 256], bal1[TD / 256], tk0 = 0, tk1 = 0;
+      long long rm0 = 0, rm1 = 0;
+      count(k0, m0, bal0, tk0, rm0);
+      const unsigned long long base0 = reserve(m0, tk0);
+      unsigned long long base1 = 0;
+      if (two) {
+        count(k1, m1, bal1, tk1, rm1);
+        base1 = reserve(m1, tk1);
       }
+      b0 = write(k0, m0, bal0, __shfl_sync(0xffffffffu, base0, 0), rm0);
+      if (two) b1 = write(k1, m1, bal1, __shfl_sync(0xffffffffu, base1, 0), rm1);
     } else if (lane == 0) {
       atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT);
-      s_fail[team] = 1;
+      s_fail = 1;
     }
-    b = warp_min(b);
-    if (lane == 0) s_wbest[team][q & 1][wid] = b;
-    team_sync(team, tsize);   // every member is done with the stage and has posted its minimum
-    if (s_fail[team]) break;
-    waited = q + 1;
+    const int par = (int)((j >> 1) & 1);
+    if (lane == 0) { s_wbest[par][0][wid] = b0; s_wbest[par][1][wid] = b1; }
+    __syncthreads();   // every warp is done with both stages and has posted its minima
+    if (s_fail) break;
+    waited = two ? j + 2 : j + 1;
     if (wid == 0) {
-      Best c = lane < nw ? s_wbest[team][q & 1][lane] : best_none();
-      c = warp_min(c);
+      for (int h = 0; h < (two ? 2 : 1); ++h) {
+        Best c = lane < nw ? s_wbest[par][h][lane] : best_none();
+        c = warp_min(c);
+        if (lane == 0) {
+          const PoolTile& m = s_meta[h ? k1 : k0];
+          unsigned long long* tb = a.desc[m.s].tile_best + 3 * m.tile;
+          tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
+        }
+      }
       if (lane == 0) {
-        const PoolTile& m = s_meta[team][k];
-        unsigned long long* tb = a.desc[m.s].tile_best + 3 * m.tile;
-        tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
-        if (q + POOL_STAGES < mt) issue(q + POOL_STAGES);
+        if (j + POOL_STAGES < mine) issue(j + POOL_STAGES);
+        if (two && j + 1 + POOL_STAGES < mine) issue(j + 1 + POOL_STAGES);
       }
     }
   }
-  // after an expired wait: wait (bounded again) for the team's copies still in
-  // flight before the shared memory is used for anything else
-  if (s_fail[team] && tt == 0) {
+  // after an expired wait: wait (bounded again) for the copies still in flight
+  // before the shared memory is used for anything else
+  if (s_fail && threadIdx.x == 0) {
     // at least two seconds, however short the engine's budget: a bulk copy
     // normally lands within microseconds
     const unsigned long long budget = a.timeout_ns > 2000000000ULL ? a.timeout_ns : 2000000000ULL;
-    const long long issued = mt < waited + POOL_STAGES ? mt : waited + POOL_STAGES;
-    for (long long q = waited; q < issued; ++q)
-      mbar_wait(&bar[q % POOL_STAGES], (unsigned)((q / POOL_STAGES) & 1), budget);
+    const long long issued = mine < waited + POOL_STAGES ? mine : waited + POOL_STAGES;
+    for (long long j = waited; j < issued; ++j)
+      mbar_wait(&s_bar[j % POOL_STAGES], (unsigned)((j / POOL_STAGES) & 1), budget);
   }
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int g = 0; g < POOL_TEAMS; ++g)
-      for (int k = 0; k < POOL_STAGES; ++k) mbar_inval(&s_bar[g][k]);
+    for (int k = 0; k < POOL_STAGES; ++k) mbar_inval(&s_bar[k]);
   __syncthreads();
 }
 
@@ -2138,7 +2120,7 @@ struct gpugo_engine {
   unsigned long long* d_cands = nullptr;
   long long cand_cap = 0;
   long long chunk = 0;           // children per pass (<= cand_cap)
-  long long* d_pref = nullptr;   // prefA | prefB | prefD | prefA2
+  long long* d_pref = nullptr;   // prefA | prefB | prefD
   char* d_arena = nullptr;
   Arena arena;
   std::vector<HostSlot> slots;
@@ -2509,15 +2491,6 @@ void fill_desc(const gpugo_spec* s, const Layout& L, char* base, Desc* D) {
   D->max_iter = s->max_iter;
   D->pool_cap = L.pool_cap; D->parent_cap = L.parent_cap; D->out_cap = L.out_cap; D->trace_cap = L.trace_cap;
   D->tiles_cap = L.tiles_cap; D->ubc_cap = L.ubc_cap; D->a_items = L.a_items;
-  // the interval items the lower bounds read (build_item_t numbers the S sample
-  // passes first, then these, then the gradient items); a code list's are not
-  // one range, so all of its items come before the bound pass
-  {
-    const int64_t n = s->n, w = s->wid, S = s->samples;
-    const int64_t per = (s->family == GPUGO_CHAINED) ? (n - 1) * w * w : n * w;
-    D->lb_lo = (s->family == GPUGO_CODELIST) ? 0 : S * per;
-    D->lb_hi = (s->family == GPUGO_CODELIST) ? L.a_items : (S + 1) * per;
-  }
   D->tab_doubles = L.tab;
   for (int i = 0; i < T_NOFF; ++i) D->t_off[i] = L.t_off[i];
   for (int i = 0; i < 2 * CL_FLAG_TABLES; ++i) D->cl_toff[i] = L.cl_toff[i];
@@ -2846,7 +2819,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     E->cand_cap = std::min<long long>(1LL << 24, std::max<long long>(1LL << 20, 8192LL * E->max_slots));
     if ((rc = cuda_err(cudaMalloc(&E->d_cands, 8 * CAND_WORDS * (size_t)E->cand_cap)))) break;
     E->chunk = cfg->chunk_children > 0 ? std::min<long long>(cfg->chunk_children, E->cand_cap) : E->cand_cap;
-    if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 4 * (E->max_slots + 1))))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
     if (const char* sp = getenv("GPUGO_PHASE_STAMPS")) {
@@ -3229,7 +3202,6 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.prefA = E->d_pref;
   a.prefB = E->d_pref + (E->max_slots + 1);
   a.prefD = E->d_pref + 2 * (E->max_slots + 1);
-  a.prefA2 = E->d_pref + 3 * (E->max_slots + 1);
   a.queue = E->d_queue;
   a.cands = E->d_cands;
   a.cand_cap = E->cand_cap;

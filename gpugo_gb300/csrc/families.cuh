@@ -49,7 +49,6 @@ struct Desc {
   long long max_iter;
   long long pool_cap, parent_cap, out_cap, trace_cap, tiles_cap, ubc_cap;
   long long a_items;                 // table-build work items per iteration
-  long long lb_lo, lb_hi;            // the items [lb_lo, lb_hi) the lower-bound pass reads
   long long tab_doubles;             // table region size (doubles)
   long long t_off[T_NOFF];           // table offsets (doubles)
   const double* dom;                 // [2n]
@@ -242,8 +241,6 @@ __device__ void init_consts(const Desc& D) {
 // table build: one work item -> one table entry
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ long long table_items(const Desc& D) { return D.a_items; }
-// table items built before the lower-bound pass (the others are built during it)
-__device__ __forceinline__ long long lb_items(const Desc& D) { return D.lb_hi - D.lb_lo; }
 
 // chained family: gradient of coordinate j given its (up to) three child intervals
 __device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv Xp) {
