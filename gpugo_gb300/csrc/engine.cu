@@ -1481,11 +1481,11 @@ struct PoolTile {
 // places of its survivors with one atomicAdd and writes them in order (its
 // stores are contiguous); the block meets once per tile, to combine the warps'
 // minima and to hand the stage to the next copy.
-__device__ __noinline__ void phase_pool(const KArgs& a) {
+__device__ void phase_pool(const KArgs& a) {
   extern __shared__ __align__(16) double s_tab[];
   __shared__ __align__(8) unsigned long long s_bar[POOL_STAGES];
   __shared__ PoolTile s_meta[POOL_STAGES];
-  __shared__ Best s_wbest[2][2][MAX_THREADS / 32];   // per warp and tile of a pair, by pair parity
+  __shared__ Best s_wbest[2][MAX_THREADS / 32];   // per warp, double-buffered by tile parity
   __shared__ int s_fail;
   const long long tot = a.ctl->totD;
   const int nB = a.ctl->nBig;
@@ -1552,113 +1552,85 @@ __device__ __noinline__ void phase_pool(const KArgs& a) {
     for (long long j = 0; j < mine && j < POOL_STAGES; ++j) issue(j);
   }
   __syncthreads();
-  // A warp takes its parts of two tiles at once: it counts the survivors of
-  // both and sends both atomics before it waits for either place, so the
-  // round trip of one atomic overlaps the other tile's work.
-  const long long w0 = (long long)wid * span;
-  auto count = [&](int k, const PoolTile& m, unsigned* bal, unsigned& tk, long long& removed_new) {
-    const Desc& D = a.desc[m.s];
-    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
-    const long long n = m.hi - m.lo, pair = n & ~1LL;
-    tk = 0;
-    removed_new = 0;
-#pragma unroll
-    for (int r = 0; r < TD / 256; ++r) {
-      bal[r] = 0;
-      if (r < rounds) {
-        const long long i = w0 + r * 32 + lane;
-        const bool in = i < n;
-        // the odd last entry of a list is not in the bulk copy
-        const bool keep = in && (!m.compact || !flt(m.ub, i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i)));
-        if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
-        bal[r] = __ballot_sync(0xffffffffu, keep);
-        tk += __popc(bal[r]);
-      }
-    }
-  };
-  auto write = [&](int k, const PoolTile& m, const unsigned* bal, unsigned long long base, long long removed_new) {
-    const Desc& D = a.desc[m.s];
-    State& st = a.st[m.s];
-    const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
-    const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
-    const long long pair = (m.hi - m.lo) & ~1LL;
-    Best b = best_none();
-    unsigned pre = 0;
-#pragma unroll
-    for (int r = 0; r < TD / 256; ++r) {
-      if (r < rounds) {
-        const long long i = w0 + r * 32 + lane;
-        if ((bal[r] >> lane) & 1u) {
-          const double lv = i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i);
-          const unsigned long long kv = i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i);
-          unsigned long long pos = (unsigned long long)(m.lo + i);
-          if (m.compact) {
-            pos = base + pre + __popc(bal[r] & ((1u << lane) - 1u));
-            D.pool_lb[m.cur ^ 1][pos] = lv;
-            D.pool_key[m.cur ^ 1][pos] = kv;
-          }
-          Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
-          if (best_less(c, b)) b = c;
-        }
-        pre += __popc(bal[r]);
-      }
-    }
-    if (m.compact) {
-      for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
-      if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
-    }
-    return warp_min(b);
-  };
-  auto reserve = [&](const PoolTile& m, unsigned tk) {   // lane 0's atomic; used later
-    unsigned long long base = 0;
-    if (m.compact && lane == 0 && tk) base = atomicAdd((unsigned long long*)&a.st[m.s].count_new, (unsigned long long)tk);
-    return base;
-  };
   long long waited = 0;   // tiles whose copies this block has seen complete
-  for (long long j = 0; j < mine; j += 2) {
-    const bool two = j + 1 < mine;
-    const int k0 = (int)(j % POOL_STAGES), k1 = (int)((j + 1) % POOL_STAGES);
-    bool ok = mbar_wait(&s_bar[k0], (unsigned)((j / POOL_STAGES) & 1), a.timeout_ns);
-    if (two) ok = ok && mbar_wait(&s_bar[k1], (unsigned)(((j + 1) / POOL_STAGES) & 1), a.timeout_ns);
-    ok = __all_sync(0xffffffffu, ok);
-    Best b0 = best_none(), b1 = best_none();
+  for (long long j = 0; j < mine; ++j) {
+    const int k = (int)(j % POOL_STAGES);
+    const unsigned parity = (unsigned)((j / POOL_STAGES) & 1);
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&s_bar[k], parity, a.timeout_ns));
+    Best b = best_none();
     if (ok) {
-      const PoolTile m0 = s_meta[k0];
-      PoolTile m1 = m0;
-      if (two) m1 = s_meta[k1];
-      unsigned bal0[TD / 256], bal1[TD / 256], tk0 = 0, tk1 = 0;
-      long long rm0 = 0, rm1 = 0;
-      count(k0, m0, bal0, tk0, rm0);
-      const unsigned long long base0 = reserve(m0, tk0);
-      unsigned long long base1 = 0;
-      if (two) {
-        count(k1, m1, bal1, tk1, rm1);
-        base1 = reserve(m1, tk1);
+      const PoolTile m = s_meta[k];
+      const Desc& D = a.desc[m.s];
+      State& st = a.st[m.s];
+      const double* slb = (const double*)(smem + k * POOL_STAGE_BYTES);
+      const unsigned long long* skey = (const unsigned long long*)(smem + k * POOL_STAGE_BYTES + TD * 8);
+      const long long n = m.hi - m.lo, pair = n & ~1LL;
+      // entry i of the tile: from the stage, or (the odd last entry of a list, not
+      // in the bulk copy) from global memory
+      auto entry_lb = [&](long long i) { return i < pair ? slb[i] : __ldcg(D.pool_lb[m.cur] + m.lo + i); };
+      auto entry_key = [&](long long i) { return i < pair ? skey[i] : __ldcg(D.pool_key[m.cur] + m.lo + i); };
+      const long long w0 = (long long)wid * span;
+      unsigned bal[TD / 256];   // survivors of each round of 32 (warp-uniform)
+      unsigned tk = 0;
+      long long removed_new = 0;
+#pragma unroll
+      for (int r = 0; r < TD / 256; ++r) {
+        bal[r] = 0;
+        if (r < rounds) {
+          const long long i = w0 + r * 32 + lane;
+          const bool in = i < n;
+          const bool keep = in && (!m.compact || !flt(m.ub, entry_lb(i)));
+          if (m.compact && in && !keep && m.lo + i >= m.count_before) removed_new++;
+          bal[r] = __ballot_sync(0xffffffffu, keep);
+          tk += __popc(bal[r]);
+        }
       }
-      b0 = write(k0, m0, bal0, __shfl_sync(0xffffffffu, base0, 0), rm0);
-      if (two) b1 = write(k1, m1, bal1, __shfl_sync(0xffffffffu, base1, 0), rm1);
+      unsigned long long base = 0;
+      if (m.compact) {
+        if (lane == 0 && tk) base = atomicAdd((unsigned long long*)&st.count_new, (unsigned long long)tk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+      }
+      unsigned pre = 0;
+#pragma unroll
+      for (int r = 0; r < TD / 256; ++r) {
+        if (r < rounds) {
+          const long long i = w0 + r * 32 + lane;
+          if ((bal[r] >> lane) & 1u) {
+            const double lv = entry_lb(i);
+            const unsigned long long kv = entry_key(i);
+            unsigned long long pos = (unsigned long long)(m.lo + i);
+            if (m.compact) {
+              pos = base + pre + __popc(bal[r] & ((1u << lane) - 1u));
+              D.pool_lb[m.cur ^ 1][pos] = lv;
+              D.pool_key[m.cur ^ 1][pos] = kv;
+            }
+            Best c; c.lbk = ord_key(lv); c.key = kv; c.idx = pos;
+            if (best_less(c, b)) b = c;
+          }
+          pre += __popc(bal[r]);
+        }
+      }
+      if (m.compact) {
+        for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
+        if (lane == 0 && removed_new) atomicAdd((unsigned long long*)&st.removed_new, (unsigned long long)removed_new);
+      }
     } else if (lane == 0) {
       atomicCAS(&a.ctl->error, 0, GPUGO_ERR_TIMEOUT);
       s_fail = 1;
     }
-    const int par = (int)((j >> 1) & 1);
-    if (lane == 0) { s_wbest[par][0][wid] = b0; s_wbest[par][1][wid] = b1; }
-    __syncthreads();   // every warp is done with both stages and has posted its minima
+    b = warp_min(b);
+    if (lane == 0) s_wbest[j & 1][wid] = b;
+    __syncthreads();   // every warp is done with the stage and has posted its minimum
     if (s_fail) break;
-    waited = two ? j + 2 : j + 1;
+    waited = j + 1;
     if (wid == 0) {
-      for (int h = 0; h < (two ? 2 : 1); ++h) {
-        Best c = lane < nw ? s_wbest[par][h][lane] : best_none();
-        c = warp_min(c);
-        if (lane == 0) {
-          const PoolTile& m = s_meta[h ? k1 : k0];
-          unsigned long long* tb = a.desc[m.s].tile_best + 3 * m.tile;
-          tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
-        }
-      }
+      Best c = lane < nw ? s_wbest[j & 1][lane] : best_none();
+      c = warp_min(c);
       if (lane == 0) {
+        const PoolTile& m = s_meta[k];
+        unsigned long long* tb = a.desc[m.s].tile_best + 3 * m.tile;
+        tb[0] = c.lbk; tb[1] = c.key; tb[2] = c.idx;
         if (j + POOL_STAGES < mine) issue(j + POOL_STAGES);
-        if (two && j + 1 + POOL_STAGES < mine) issue(j + 1 + POOL_STAGES);
       }
     }
   }
