@@ -513,7 +513,7 @@ def run_list_pass(args):
     p = P.Problem(P.COSQUAD, n, np.tile([-5.5, 6.0], n), np.concatenate([np.ones(n), np.full(n, 10.0), np.ones(n)]),
                   wid=4, group=10, samples=10, stop_mode=P.STOP_WIDTH, width_tol=1e-4, ub_init=1e6,
                   max_iter=args.steps, pool_cap=1 << 26)
-    with G.Engine(max_slots=1, arena_bytes=8 << 30, threads=args.threads) as eng:
+    with G.Engine(max_slots=1, arena_bytes=8 << 30, threads=args.threads, blocks_per_sm=args.blocks_per_sm) as eng:
         eng.submit(p, box_cap=4, trace_cap=4096)
         eng.run(0)
         (_, r), = eng.poll()
@@ -532,7 +532,8 @@ def run_list_pass(args):
     best = max(big, key=lambda d: d["GBps"]) if big else None
     return {"metric": "list pass GB/s (algorithmic)", "value": best["GBps"] if best else None, "unit": "GB/s",
             "n_gpus": 1, "dtype": "f64/u64", "config": {"workload": "rastrigin50 reference loop, 4^10 children/iter",
-                                                      "iterations": int(st.shape[0]), "threads": args.threads},
+                                                      "iterations": int(st.shape[0]), "threads": args.threads,
+                                                      "blocks_per_sm": args.blocks_per_sm},
             "per_iteration": per}
 
 
@@ -645,6 +646,7 @@ def main():
     ap.add_argument("--arena-gb", type=int, default=80)
     ap.add_argument("--pool-gb", type=int, default=64, help="cfg3-full: list cap (two buffers)")
     ap.add_argument("--threads", type=int, default=256, help="listpass: threads per block (256 or 512)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="listpass: blocks per SM (0: the engine's choice)")
     ap.add_argument("--cpu-instances", type=int, default=64, help="batch instances the CPU baseline solves")
     ap.add_argument("--no-plain", dest="plain", action="store_false",
                     help="skip the plain one-instance-per-launch comparison")
