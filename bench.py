@@ -646,7 +646,9 @@ def main():
     ap.add_argument("--arena-gb", type=int, default=80)
     ap.add_argument("--pool-gb", type=int, default=64, help="cfg3-full: list cap (two buffers)")
     ap.add_argument("--threads", type=int, default=256, help="listpass: threads per block (256 or 512)")
-    ap.add_argument("--blocks-per-sm", type=int, default=0, help="listpass: blocks per SM (0: the engine's choice)")
+    ap.add_argument("--blocks-per-sm", type=int, default=2,
+                    help="listpass: blocks per SM (two of 256 threads: six 32 KB tiles in flight per SM; 0: the "
+                         "engine's choice for one instance, one block per SM)")
     ap.add_argument("--cpu-instances", type=int, default=64, help="batch instances the CPU baseline solves")
     ap.add_argument("--no-plain", dest="plain", action="store_false",
                     help="skip the plain one-instance-per-launch comparison")

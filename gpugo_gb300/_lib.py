@@ -31,7 +31,8 @@ class Spec(ctypes.Structure):
         ("family", ctypes.c_int32), ("n", ctypes.c_int32), ("wid", ctypes.c_int32),
         ("group", ctypes.c_int32), ("samples", ctypes.c_int32), ("stop_mode", ctypes.c_int32),
         ("width_tol", ctypes.c_double), ("gap_tol", ctypes.c_double), ("ub_init", ctypes.c_double),
-        ("domain", _dp), ("coef", _dp), ("ncoef", ctypes.c_int64), ("max_iter", ctypes.c_int64),
+        # const double* (addresses of float64 arrays; c_void_p takes them as integers)
+        ("domain", ctypes.c_void_p), ("coef", ctypes.c_void_p), ("ncoef", ctypes.c_int64), ("max_iter", ctypes.c_int64),
         ("pool_cap", ctypes.c_int64), ("parent_cap", ctypes.c_int64),
     ]
 
