@@ -277,10 +277,12 @@ def run_batch(args, dist):
         slots = min(len(stream), 2048)
         with G.Engine(max_slots=slots, arena_bytes=args.arena_gb << 30, threads=ecfg.threads,
                       blocks_per_sm=ecfg.blocks_per_sm, cand_mode=ecfg.cand_mode) as seng:
-            serving = serve_sharded(stream, dist, max_slots=slots, slice_iters=args.slice, engine=seng)
+            serving = serve_sharded(stream, dist, max_slots=slots, slice_iters=args.slice, engine=seng,
+                                    order=args.serve_order)
         if serving is not None:
             serving["workload"] = (f"cfg5-serve{args.serve_count}: Poisson {args.rate:g}/s, F1-F4, n log-uniform "
-                                   f"2..128, tol 1e-6 or 1e-4, arena {args.arena_gb} GiB, slice {args.slice}")
+                                   f"2..128, tol 1e-6 or 1e-4, arena {args.arena_gb} GiB, slice {args.slice}, "
+                                   f"admission by {args.serve_order}")
 
     # roofline: FP64 throughput of the persistent kernel against a DFMA peak measured now
     peak = ctypes.c_double()
@@ -642,7 +644,9 @@ def main():
     ap.add_argument("--count", type=int, default=1024, help="instances of the batch")
     ap.add_argument("--serve-count", type=int, default=4096, help="requests of the serving record (0: none)")
     ap.add_argument("--rate", type=float, default=20000.0)
-    ap.add_argument("--slice", type=int, default=16)
+    ap.add_argument("--slice", type=int, default=16, help="serving: iterations per run between admissions")
+    ap.add_argument("--serve-order", default="arrival", choices=["arrival", "shape"],
+                    help="serving: waiting requests take free slots in arrival order or grouped by (family, n)")
     ap.add_argument("--arena-gb", type=int, default=80)
     ap.add_argument("--pool-gb", type=int, default=64, help="cfg3-full: list cap (two buffers)")
     ap.add_argument("--threads", type=int, default=256, help="listpass: threads per block (256 or 512)")

@@ -63,9 +63,14 @@ class ServeReport:
 
 def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_bytes: int = 80 << 30,
           slice_iters: int = 16, box_cap: int = 4, engine: Engine | None = None,
-          clock=time.perf_counter) -> ServeReport:
+          clock=time.perf_counter, order: str = "arrival") -> ServeReport:
     """Run ``stream`` (pairs of arrival time in seconds and problem, sorted by
-    arrival) through one engine; returns per-request latencies and results."""
+    arrival) through one engine; returns per-request latencies and results.
+    ``order`` is how waiting requests take free slots: ``"arrival"`` first come
+    first served, ``"shape"`` grouped by (family, n) and then by arrival, so that
+    neighbouring slots (and so the kernel's work lists) hold solves of one shape."""
+    if order not in ("arrival", "shape"):
+        raise ValueError(f"order {order!r}")
     own = engine is None
     eng = engine or Engine(max_slots=max_slots, arena_bytes=arena_bytes)
     records = [RequestRecord(i, float(t)) for i, (t, _) in enumerate(stream)]
@@ -77,9 +82,13 @@ def serve(stream: list[tuple[float, Problem]], max_slots: int = 1024, arena_byte
     done = 0
     while done < len(records):
         now = clock() - t0
+        arrived = False
         while nxt < len(records) and stream[nxt][0] <= now:
             pending.append(nxt)
             nxt += 1
+            arrived = True
+        if arrived and order == "shape" and len(pending) > 1:
+            pending = deque(sorted(pending, key=lambda k: (stream[k][1].family, stream[k][1].n, k)))
         # admit in arrival order while slots and pool memory last; a request the
         # library refuses (a bad description) or that cannot fit even an empty
         # engine is answered with its error and the stream goes on

@@ -2,6 +2,8 @@
 ordering, admission only while slots are free, collection, latency accounting."""
 from types import SimpleNamespace
 
+import pytest
+
 from gpugo_gb300 import problems as P
 from gpugo_gb300.serve import serve
 
@@ -130,3 +132,18 @@ def test_device_failure_in_admission_is_not_swallowed():
     stream = [(0.0, P.instance(P.COSQUAD, 2, 1, tag="q0"))]
     with pytest.raises(G.GpugoError):
         serve(stream, engine=Broken(slots=2, iters=1), clock=FakeClock())
+
+
+def test_shape_order_groups_waiting_requests():
+    """order="shape": requests waiting together take the free slots grouped by
+    (family, n), then by arrival; every request is still served once."""
+    fams = [P.CHAINED, P.COSQUAD, P.CHAINED, P.COSQUAD, P.EXPSQRT, P.COSQUAD]
+    ns = [5, 3, 4, 3, 2, 2]
+    stream = [(0.0, P.instance(f, n, i, tag=f"q{i}")) for i, (f, n) in enumerate(zip(fams, ns))]
+    eng = FakeEngine(slots=2, iters=1)
+    rep = serve(stream, max_slots=2, slice_iters=1, engine=eng, clock=FakeClock(), order="shape")
+    assert sorted(eng.admit_order) == sorted(f"q{i}" for i in range(6))
+    assert eng.admit_order[:2] == ["q5", "q1"]          # cosquad n=2, then cosquad n=3 (earlier arrival)
+    assert rep.certified == 6
+    with pytest.raises(ValueError):
+        serve(stream, engine=FakeEngine(2, 1), order="random")
