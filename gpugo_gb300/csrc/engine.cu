@@ -93,6 +93,7 @@ struct State {
   long long cand_done;        // candidates processed this iteration
   int has_who;
   int pad;
+  unsigned long long lb_max;  // ord_key at or above every list entry's LB (0: no entry yet)
 };
 
 struct Ctl {
@@ -653,6 +654,20 @@ __device__ void finish_iteration(const Desc& D, State& st, Best b, long long cnt
   __syncwarp();
 }
 
+// ord_key of a UB with both zeros taken as +0 (list entries store -0 as +0)
+__device__ __forceinline__ unsigned long long zkey(unsigned long long k) {
+  return (k == ord_key(-0.0)) ? ord_key(0.0) : k;
+}
+
+// Whether the list update has entries to rule out: the UB moved this iteration
+// and some entry's LB may lie above it (lb_max bounds them all from above).
+// When no entry can be ruled out the list is left as it is: the compaction
+// would keep every entry, and selection does not depend on their order.
+__device__ __forceinline__ bool must_compact(unsigned long long ubk, unsigned long long ub_start,
+                                             unsigned long long lb_max) {
+  return ubk != ub_start && lb_max > zkey(ubk);
+}
+
 // Block-level list update of one instance whose children are all done:
 // in-place compaction when the UB moved (list rule-out, ackley50.py:1154-1166),
 // argmin (ackley50.py:1273), then the selection.
@@ -664,11 +679,12 @@ __device__ void block_instance(const KArgs& a, int s) {
   long long cnt = count < D.pool_cap ? count : D.pool_cap;
   if (vload(st.outcome) < 0) cnt = 0;
   const unsigned long long ubk = vload(st.ub);
-  const bool compact = ubk != vload(st.ub_start);
+  const bool moved = ubk != vload(st.ub_start);
+  const bool compact = must_compact(ubk, vload(st.ub_start), vload(st.lb_max));
   const double ub = ord_val(ubk);
   const long long before = vload(st.count_before);
   const int c = vload(st.cur);
-  if (expanded && compact && threadIdx.x < 32) locate_who(D, st);
+  if (expanded && moved && threadIdx.x < 32) locate_who(D, st);
   Best b = best_none();
   long long kept = 0, removed_new = 0;
   for (long long base = 0; base < cnt; base += blockDim.x) {
@@ -698,6 +714,7 @@ __device__ void block_instance(const KArgs& a, int s) {
   long long rn;
   block_exclusive_scan(removed_new, &rn);
   b = block_min(b);
+  if (compact && threadIdx.x == 0) st.lb_max = zkey(ubk);   // every kept LB is at most the UB
   if (threadIdx.x < 32) {
     long long n_surv = (cnt - before) - rn;
     finish_iteration(D, st, b, kept, n_surv, expanded);
@@ -720,11 +737,12 @@ __device__ void warp_instance(const KArgs& a, int s) {
   long long cnt = count < D.pool_cap ? count : D.pool_cap;
   if (vload(st.outcome) < 0) cnt = 0;
   const unsigned long long ubk = vload(st.ub);
-  const bool compact = ubk != vload(st.ub_start);
+  const bool moved = ubk != vload(st.ub_start);
+  const bool compact = must_compact(ubk, vload(st.ub_start), vload(st.lb_max));
   const double ub = ord_val(ubk);
   const long long before = vload(st.count_before);
   const int c = vload(st.cur);
-  if (expanded && compact) locate_who(D, st);
+  if (expanded && moved) locate_who(D, st);
   Best b = best_none();
   long long kept = 0, removed_new = 0;
   for (long long base = 0; base < cnt; base += 32) {
@@ -753,6 +771,7 @@ __device__ void warp_instance(const KArgs& a, int s) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) removed_new += __shfl_xor_sync(0xffffffffu, removed_new, o);
   b = warp_min(b);
+  if (compact && lane == 0) st.lb_max = zkey(ubk);   // every kept LB is at most the UB
   finish_iteration(D, st, b, kept, (cnt - before) - removed_new, expanded);
 }
 
@@ -1024,8 +1043,18 @@ __device__ __noinline__ void warp_append_survivors(const KArgs& a, bool keep, in
     const int leader = __ffs(act) - 1;
     const int ls = __shfl_sync(0xffffffffu, s, leader);
     const unsigned int m = __ballot_sync(0xffffffffu, keep && s == ls);
+    // the group's largest LB raises the instance's bound on its list's LBs
+    unsigned long long mk = (keep && s == ls) ? ord_key(feq(lb, 0.0) ? 0.0 : lb) : 0ULL;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, mk, o);
+      mk = y > mk ? y : mk;
+    }
     unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd((unsigned long long*)&a.st[ls].count, (unsigned long long)__popc(m));
+    if (lane == leader) {
+      base = atomicAdd((unsigned long long*)&a.st[ls].count, (unsigned long long)__popc(m));
+      atomicMax(&a.st[ls].lb_max, mk);
+    }
     base = __shfl_sync(0xffffffffu, base, leader);
     if (keep && s == ls) {
       const Desc& D = a.desc[ls];
@@ -1531,7 +1560,7 @@ __device__ void phase_pool(const KArgs& a) {
       c.cnt = count < D.pool_cap ? count : D.pool_cap;
       const unsigned long long ubk = vload(st.ub);
       c.m.cur = vload(st.cur);
-      c.m.compact = ubk != vload(st.ub_start);
+      c.m.compact = must_compact(ubk, vload(st.ub_start), vload(st.lb_max));
       c.m.ub = ord_val(ubk);
       c.m.count_before = vload(st.count_before);
       c.lb = D.pool_lb[c.m.cur];
@@ -1668,9 +1697,10 @@ __device__ void phase_select_big(const KArgs& a) {
     const Desc& D = a.desc[s];
     State& st = a.st[s];
     const bool expanded = (st.status == ST_EXPAND);
-    const bool compact = st.ub != st.ub_start;
+    const bool moved = st.ub != st.ub_start;
+    const bool compact = must_compact(st.ub, st.ub_start, st.lb_max);
     long long cnt = st.count < D.pool_cap ? st.count : D.pool_cap;
-    if (expanded && compact) locate_who(D, st);
+    if (expanded && moved) locate_who(D, st);
     long long n_surv = (cnt - st.count_before) - (compact ? st.removed_new : 0);
     Best b = best_none();
     const long long tiles = pool_tiles(D, st);
@@ -1683,7 +1713,7 @@ __device__ void phase_select_big(const KArgs& a) {
     if (compact) {
       cnt = st.count_new;
       __syncwarp();
-      if (lane == 0) { st.cur ^= 1; st.count_new = 0; }
+      if (lane == 0) { st.cur ^= 1; st.count_new = 0; st.lb_max = zkey(st.ub); }
       __syncwarp();
     }
     finish_iteration(D, st, b, cnt, n_surv, expanded);
@@ -2950,14 +2980,14 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
 }  // extern "C"
 namespace {
 struct CkptHeader {
-  char magic[8];                      // "GPUGOCK1"
+  char magic[8];                      // "GPUGOCK2"
   int32_t family, n, wid, group, samples, stop_mode;
   double width_tol, gap_tol, ub_init;
   int64_t ncoef, max_iter, pool_cap, parent_cap;
   State st;
   int64_t rows, cnt, nout, ntrace;
 };
-const char CKPT_MAGIC[8] = {'G', 'P', 'U', 'G', 'O', 'C', 'K', '1'};
+const char CKPT_MAGIC[8] = {'G', 'P', 'U', 'G', 'O', 'C', 'K', '2'};
 size_t pad8(size_t b) { return (b + 7) & ~size_t(7); }
 
 // The kernels trust a restored solve as they trust one they built: every index
@@ -3138,6 +3168,7 @@ int gpugo_restore(gpugo_engine* E, const void* buf, int64_t bytes, double* boxes
   st.cur = 0;               // the list was packed into buffer 0
   st.count = hd.cnt;
   st.count_new = 0;
+  st.lb_max = ~0ULL;        // no bound taken from the buffer: the next UB move compacts
   return admit(E, &sp, boxes_out, box_lb_out, cap, xhat_out, trace, &st, pcs, ticket_out);
 }
 

@@ -27,7 +27,7 @@ class State(ctypes.Structure):
                 ("out_lb_min", ctypes.c_double), ("bounded", ctypes.c_int64), ("samples", ctypes.c_int64),
                 ("ubc_count", ctypes.c_int64), ("m_children", ctypes.c_int64), ("b_done", ctypes.c_int64),
                 ("seed_key", ctypes.c_uint64), ("cand_total", ctypes.c_int64), ("cand_done", ctypes.c_int64),
-                ("has_who", ctypes.c_int), ("pad", ctypes.c_int)]
+                ("has_who", ctypes.c_int), ("pad", ctypes.c_int), ("lb_max", ctypes.c_uint64)]
 
 
 class Header(ctypes.Structure):
@@ -55,7 +55,7 @@ def _checkpoint(p, rows=2, keys=None, out_keys=(), pcyc=None, **state):
     """A checkpoint of ``p`` after ``rows - 1`` expansions, in the library's layout."""
     n = p.n
     h = Header()
-    h.magic = b"GPUGOCK1"
+    h.magic = b"GPUGOCK2"
     h.family, h.n, h.wid, h.group, h.samples, h.stop_mode = p.family, n, p.wid, p.group, p.samples, p.stop_mode
     h.width_tol, h.gap_tol, h.ub_init = p.width_tol, p.gap_tol, 1e6
     h.ncoef = p.coef.size
@@ -87,7 +87,7 @@ def _ok(lib, data):
 
 
 def test_layout_matches_the_library():
-    assert ctypes.sizeof(State) == 168
+    assert ctypes.sizeof(State) == 176
 
 
 @pytest.mark.parametrize("make", [lambda: P.config1(), lambda: P.config2(),
