@@ -7,9 +7,10 @@
 //   A  term tables for each instance's selected parent        (families.cuh)
 //   B  children: lower bound, sample upper bounds -> atomicMin(UB), KKT test,
 //      survivors appended to the instance's box pool          (sampling + ruleOutGPU,
-//                                                              ackley50.py:602-766)
-//   D  pool: drop entries with LB > UB when UB moved, argmin   (ackley50.py:1154-1166,
-//      per 2048-entry tile                                      :768-810, :1273)
+//      in passes of at most the candidate queue's capacity     ackley50.py:602-766)
+//   D  pool: drop entries with LB > UB when UB moved and an    (ackley50.py:1154-1166,
+//      entry may lie above it, argmin; large lists per 2048-   :768-810, :1273)
+//      entry tile streamed through shared memory by bulk copies
 //   E  one warp per instance: pop the best entry, width/gap rule, decode the
 //      next parent into the parent table                       (ackley50.py:1269-1370)
 //
