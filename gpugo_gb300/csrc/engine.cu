@@ -1147,7 +1147,8 @@ __device__ void phase_bound(const KArgs& a) {
         act &= ~m;
       }
     } else {
-      // queue full: process these candidates right here
+      // queue full: process these candidates right here (not reached while a
+      // children pass has at most cand_cap children; kept as the safe path)
       bool keep = false;
       while (cm) {
         int b = __ffs(cm) - 1;
