@@ -229,9 +229,9 @@ class Engine:
         s, keep = _spec(p)
         boxes, lbs, xhat, tr, arrs = _alloc_out(p, box_cap, trace_cap)
         t = ctypes.c_int64()
-        rc = self._L.gpugo_submit(self._h, ctypes.byref(s), boxes.ctypes.data_as(_dp), lbs.ctypes.data_as(_dp),
-                                  box_cap, xhat.ctypes.data_as(_dp), ctypes.byref(tr) if tr is not None else None,
-                                  ctypes.byref(t))
+        rc = self._L.gpugo_submit(self._h, ctypes.byref(s), boxes.__array_interface__["data"][0],
+                                  lbs.__array_interface__["data"][0], box_cap, xhat.__array_interface__["data"][0],
+                                  ctypes.byref(tr) if tr is not None else None, ctypes.byref(t))
         if rc == _lib.ERR_BUSY:
             return None
         _lib.check(rc, "gpugo_submit")

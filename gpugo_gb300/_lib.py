@@ -113,7 +113,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     L.gpugo_eval_children_static.argtypes = L.gpugo_eval_children.argtypes
     L.gpugo_engine_create.argtypes = [ctypes.POINTER(EngineCfg), ctypes.POINTER(vp)]
     L.gpugo_engine_destroy.argtypes = [vp]
-    L.gpugo_submit.argtypes = [vp, ctypes.POINTER(Spec), _dp, _dp, ctypes.c_int64, _dp, ctypes.POINTER(Trace), _i64p]
+    # output buffers by address (double* in the header): an engine admits thousands of problems
+    L.gpugo_submit.argtypes = [vp, ctypes.POINTER(Spec), vp, vp, ctypes.c_int64, vp, ctypes.POINTER(Trace), _i64p]
     L.gpugo_run.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
     L.gpugo_poll.argtypes = [vp, ctypes.POINTER(Done), ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     L.gpugo_engine_free_bytes.argtypes = [vp, _i64p]
