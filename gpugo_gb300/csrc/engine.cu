@@ -1176,6 +1176,9 @@ __device__ void phase_bound(const KArgs& a) {
 // GB300 with the 1024-instance mixed batch: 151 ms to certified at 64 per warp,
 // 139 at 8, 132 at 12, 128 at 16 and at 24, 130 at 32.
 constexpr long long LANE_FROM = 24;
+// Candidates left per warp below which a lane-per-candidate pass hands its last
+// candidates out one per warp.
+constexpr unsigned long long TAIL_FROM = 4;
 
 // instances without queued candidates are ready for their list update at once
 __device__ void prefill_ready(const KArgs& a) {
@@ -1310,18 +1313,30 @@ __device__ void phase_candidates(const KArgs& a) {
   // different SMs, which do not share an FP64 unit.  Later claims, and every
   // claim of a long queue, come from the shared counter.
   const unsigned long long g = (unsigned long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   bool first = K < 32;
   for (;;) {
-    unsigned long long h = g * K;
+    unsigned long long h = g * K, Kc = K;
     if (!first) {
-      if (lane == 0) h = atomicAdd(&a.ctl->cand_head, K);
+      if (lane == 0) {
+        // The tail of a long queue goes a warp per candidate: a lane-per-candidate
+        // claim runs each lane's sample passes one after the other, so the last
+        // such claims would keep a few warps busy while all others wait.
+        if (K >= 32) {
+          const unsigned long long hd = vload(a.ctl->cand_head);
+          const unsigned long long rem = hd < tot ? tot - hd : 0ULL;
+          if (rem < TAIL_FROM * nwarps) Kc = 1;
+        }
+        h = atomicAdd(&a.ctl->cand_head, Kc);
+      }
       h = __shfl_sync(0xffffffffu, h, 0);
+      Kc = __shfl_sync(0xffffffffu, Kc, 0);
     }
     first = false;
     if (h >= tot) break;   // a static range past the end: the shared counter starts later still
-    const unsigned long long e = min(tot, h + K);
+    const unsigned long long e = min(tot, h + Kc);
     if (a.bstamps && lane == 0) atomicAdd(&s_claimed, e - h);
-    if (K >= 32) {
+    if (Kc >= 32) {
       // One candidate per lane.  The claim is filtered first (LB against the
       // current UB) and the survivors are packed densely, so that no lane idles
       // through another lane's sample chains.
