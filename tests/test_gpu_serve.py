@@ -11,8 +11,9 @@ from gpugo_gb300.serve import serve
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("with_codelists", [False, True], ids=["builtin", "mixed"])
-def test_served_results_match_solo(with_codelists):
+@pytest.mark.parametrize("with_codelists,order", [(False, "arrival"), (True, "arrival"), (False, "shape")],
+                         ids=["builtin", "mixed", "builtin-shape-order"])
+def test_served_results_match_solo(with_codelists, order):
     probs = P.config4(count=18, seed=91, nmax=16) + [P.config1(), P.config2()]
     if with_codelists:
         from gpugo_gb300 import objectives as O
@@ -24,7 +25,7 @@ def test_served_results_match_solo(with_codelists):
     stream = [(0.0002 * i, p) for i, p in enumerate(probs)]
     solo = [G.solve(p, box_cap=4) for p in probs]
     with G.Engine(max_slots=5, arena_bytes=1 << 30) as eng:
-        rep = serve(stream, engine=eng, slice_iters=3, box_cap=4)
+        rep = serve(stream, engine=eng, slice_iters=3, box_cap=4, order=order)
     assert rep.launches > len(probs) // 5          # solves were interleaved across several runs
     for p, a, rec in zip(probs, solo, rep.records):
         b = rec.result
