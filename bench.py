@@ -332,7 +332,7 @@ def run_batch(args, dist):
                    "serving": serving},
         "e2e": {"value": boxes_all / w_max, "unit": "boxes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * w_max / args.steps,
-                "api": "Engine.solve_all (gpugo_submit / gpugo_run / gpugo_poll), host buffers"},
+                "api": "Engine.solve_all (gpugo_submit_batch / gpugo_run / gpugo_poll), host buffers"},
         "gpu_launches": int(launches),
         "roofline": roof,
         "clocks": clk,

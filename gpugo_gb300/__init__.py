@@ -28,6 +28,8 @@ __all__ = ["solve", "eval_children", "Engine", "SolveResult", "Problem", "GpugoE
            "checkpoint_ok"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
+_SPEC = np.dtype(_lib.Spec)      # gpugo_spec as a NumPy record (a batch of them is one array)
+_DONE = np.dtype(_lib.Done)      # gpugo_done as a NumPy record
 
 
 def _f64(a) -> np.ndarray:
@@ -238,6 +240,58 @@ class Engine:
         self._pending[t.value] = (p, boxes, lbs, xhat, arrs, tr, keep)
         return t.value
 
+    def submit_many(self, problems: list[Problem], box_cap: int = 16) -> list[int]:
+        """Admit ``problems`` in order with one ``gpugo_submit_batch`` call, as many
+        as fit: returns the tickets of the admitted prefix (shorter than
+        ``problems`` when the engine filled up).  Their results come from ``poll``
+        as for ``submit``; the descriptions are gathered column by column and the
+        output buffers are three arrays shared by the batch.  A description the
+        library refuses raises ``GpugoError`` whose ``admitted`` lists the tickets
+        of the problems before it (admitted all the same); a domain of the wrong
+        size raises ``ValueError`` before anything is admitted."""
+        m = len(problems)
+        if m == 0:
+            return []
+        ns = np.fromiter((p.n for p in problems), np.int64, m)
+        doms = [_f64(p.domain) for p in problems]
+        coefs = [_f64(p.coef) for p in problems]
+        dsz = np.fromiter((d.size for d in doms), np.int64, m)
+        bad = np.flatnonzero(dsz != 2 * ns)
+        if bad.size:       # the library reads 2n bounds through a plain pointer
+            i = int(bad[0])
+            raise ValueError(f"problem {i}: domain holds {dsz[i]} bounds, the problem needs 2n = {2 * ns[i]}")
+        csz = np.fromiter((c.size for c in coefs), np.int64, m)
+        dom = np.concatenate(doms)
+        coef = np.concatenate(coefs) if csz.sum() else np.zeros(1)
+        specs = np.zeros(m, _SPEC)
+        for name in ("family", "wid", "group", "samples", "stop_mode", "width_tol", "gap_tol", "ub_init"):
+            specs[name] = [getattr(p, name) for p in problems]
+        for name in ("max_iter", "pool_cap", "parent_cap"):
+            specs[name] = [getattr(p, name) or 0 for p in problems]
+        specs["n"] = ns
+        specs["ncoef"] = csz
+        specs["domain"] = dom.ctypes.data + 8 * (np.cumsum(dsz) - dsz)
+        specs["coef"] = coef.ctypes.data + 8 * (np.cumsum(csz) - csz)
+        at = np.cumsum(ns) - ns                      # N_i: coordinates before problem i
+        cap = int(box_cap)
+        boxes = np.zeros(2 * cap * int(ns.sum()))
+        lbs = np.zeros(cap * m)
+        xhat = np.zeros(int(ns.sum()))
+        tickets = np.zeros(m, np.int64)
+        done = ctypes.c_int64()
+        rc = self._L.gpugo_submit_batch(self._h, specs.ctypes.data, m, boxes.ctypes.data, lbs.ctypes.data, cap,
+                                        xhat.ctypes.data, tickets.ctypes.data, ctypes.byref(done))
+        k = done.value
+        for i in range(k):     # admitted problems are registered before an error is raised
+            a, n = int(at[i]), int(ns[i])
+            self._pending[int(tickets[i])] = (problems[i], boxes[2 * cap * a:2 * cap * (a + n)].reshape(cap, 2 * n),
+                                              lbs[cap * i:cap * (i + 1)], xhat[a:a + n], None, None, None)
+        if rc < 0 and rc != _lib.ERR_BUSY:
+            err = GpugoError(rc, f"gpugo_submit_batch (problem {k})")
+            err.admitted = tickets[:k].tolist()
+            raise err
+        return tickets[:k].tolist()
+
     def checkpoint(self, ticket: int) -> bytes:
         """Serialise a resident solve (between runs): problem, state, parent table,
         list, emitted boxes and trace."""
@@ -273,10 +327,24 @@ class Engine:
         nd = ctypes.c_int32()
         _lib.check(self._L.gpugo_poll(self._h, arr, max_done, ctypes.byref(nd)), "gpugo_poll")
         out = []
-        for i in range(nd.value):
-            t = int(arr[i].ticket)
+        m = nd.value
+        if m == 0:
+            return out
+        # the records read column by column (a batch returns a thousand at once);
+        # boxes, LBs and points are views of the buffers allocated at admission
+        rec = np.frombuffer(arr, _DONE, m)
+        res = rec["result"]
+        cols = [res[f].tolist() for f in ("lb", "ub", "status", "iterations", "boxes_bounded",
+                                          "samples_evaluated", "pool_size", "n_boxes", "n_out", "has_xhat",
+                                          "device_ms")]
+        rows = zip(rec["ticket"].tolist(), *cols)
+        for i, (t, lb, ub, status, iters, bb, se, ps, nb, k, hx, dms) in enumerate(rows):
             p, boxes, lbs, xhat, arrs, tr, keep = self._pending.pop(t)
-            out.append((t, _result(p, arr[i].result, boxes, lbs, xhat, arrs)))
+            if arrs is not None:
+                out.append((t, _result(p, arr[i].result, boxes, lbs, xhat, arrs)))
+                continue
+            out.append((t, SolveResult(lb, ub, status, iters, bb, se, ps, nb, boxes[:k].reshape(k, p.n, 2),
+                                       lbs[:k], xhat if hx else None, dms)))
         return out
 
     def stats(self) -> dict:
@@ -304,12 +372,10 @@ class Engine:
             order.sort(key=lambda k: (problems[k].family, problems[k].n))
         nxt = 0
         while nxt < len(problems) or tickets:
-            while nxt < len(problems):
-                t = self.submit(problems[order[nxt]], box_cap=box_cap)
-                if t is None:
-                    break
-                tickets[t] = order[nxt]
-                nxt += 1
+            if nxt < len(problems):
+                for t in self.submit_many([problems[k] for k in order[nxt:]], box_cap=box_cap):
+                    tickets[t] = order[nxt]
+                    nxt += 1
             if not tickets:
                 raise GpugoError(-7, f"problem {order[nxt]} does not fit an empty engine")
             self.run(iters_per_run)

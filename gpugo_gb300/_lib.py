@@ -74,7 +74,7 @@ EXPORTS = [
     "gpugo_solve", "gpugo_eval_children", "gpugo_engine_create", "gpugo_engine_destroy", "gpugo_submit",
     "gpugo_run", "gpugo_poll", "gpugo_engine_free_bytes", "gpugo_instance_bytes", "gpugo_strerror",
     "gpugo_device_info", "gpugo_engine_stats", "gpugo_fp64_peak", "gpugo_eval_children_static",
-    "gpugo_combine", "gpugo_checkpoint", "gpugo_restore", "gpugo_checkpoint_check",
+    "gpugo_combine", "gpugo_checkpoint", "gpugo_restore", "gpugo_checkpoint_check", "gpugo_submit_batch",
 ]
 
 _lib = None
@@ -115,6 +115,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     L.gpugo_engine_destroy.argtypes = [vp]
     # output buffers by address (double* in the header): an engine admits thousands of problems
     L.gpugo_submit.argtypes = [vp, ctypes.POINTER(Spec), vp, vp, ctypes.c_int64, vp, ctypes.POINTER(Trace), _i64p]
+    L.gpugo_submit_batch.argtypes = [vp, vp, ctypes.c_int64, vp, vp, ctypes.c_int64, vp, vp, _i64p]
     L.gpugo_run.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
     L.gpugo_poll.argtypes = [vp, ctypes.POINTER(Done), ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     L.gpugo_engine_free_bytes.argtypes = [vp, _i64p]

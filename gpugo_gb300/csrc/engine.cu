@@ -2991,6 +2991,28 @@ int gpugo_submit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, dou
   return admit(E, spec, boxes_out, box_lb_out, cap, xhat_out, trace, nullptr, {}, ticket_out);
 }
 
+int gpugo_submit_batch(gpugo_engine* E, const gpugo_spec* specs, int64_t count, double* boxes_out,
+                       double* box_lb_out, int64_t cap, double* xhat_out, int64_t* tickets_out,
+                       int64_t* admitted_out) {
+  NvtxRange nvtx_range("gpugo_submit_batch");
+  if (!E || !admitted_out || count < 0 || (count > 0 && (!specs || !tickets_out))) return GPUGO_ERR_INVALID;
+  *admitted_out = 0;
+  if (cap < 0 || cap > (1LL << 40)) return GPUGO_ERR_INVALID;
+  int64_t coords = 0;   // n_0 + ... + n_{i-1}
+  for (int64_t i = 0; i < count; ++i) {
+    // the byte offset of problem i's boxes, 16 * cap * coords, must be representable
+    if (cap > 0 && coords > (INT64_MAX / 16) / cap) return GPUGO_ERR_INVALID;
+    double* bx = boxes_out ? boxes_out + 2 * cap * coords : nullptr;
+    double* bl = box_lb_out ? box_lb_out + cap * i : nullptr;
+    double* xh = xhat_out ? xhat_out + coords : nullptr;
+    const int rc = admit(E, &specs[i], bx, bl, cap, xh, nullptr, nullptr, {}, &tickets_out[i]);
+    if (rc) return rc;
+    coords += specs[i].n;   // validated by admit: 1..16384
+    *admitted_out = i + 1;
+  }
+  return GPUGO_OK;
+}
+
 // ---------------------------------------------------------------------------
 // checkpoint / resume of one instance (between runs)
 // ---------------------------------------------------------------------------

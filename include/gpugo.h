@@ -212,6 +212,21 @@ int gpugo_engine_destroy(gpugo_engine* eng);
 int gpugo_submit(gpugo_engine* eng, const gpugo_spec* spec, double* boxes_out, double* box_lb_out,
                  int64_t cap, double* xhat_out, gpugo_trace* trace, int64_t* ticket_out);
 
+/* Admit specs[0..count) in order, as that many gpugo_submit calls without a
+ * trace would, in one call (a batch of a thousand problems crosses the boundary
+ * once).  The output buffers are packed: with N_i = n_0 + ... + n_{i-1},
+ * problem i's boxes start at boxes_out + 2 * cap * N_i, its box LBs at
+ * box_lb_out + cap * i and its sample point at xhat_out + N_i (buffers of
+ * 2 * cap * N_count, cap * count and N_count doubles).  Stops at the first
+ * problem that is not admitted: *admitted_out = the number admitted, their
+ * tickets in tickets_out[0 .. *admitted_out).  Returns GPUGO_OK when all were
+ * admitted, GPUGO_ERR_BUSY when problem *admitted_out found no free slot or
+ * memory, and that problem's error when its spec is invalid; the problems
+ * before it stay admitted in every case. */
+int gpugo_submit_batch(gpugo_engine* eng, const gpugo_spec* specs, int64_t count, double* boxes_out,
+                       double* box_lb_out, int64_t cap, double* xhat_out, int64_t* tickets_out,
+                       int64_t* admitted_out);
+
 /* Run the persistent kernel for at most max_iters iterations (0: until every
  * admitted instance has finished).  Returns the number of instances still active
  * through *active_out. */

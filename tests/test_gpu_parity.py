@@ -194,6 +194,60 @@ def test_engine_batch_matches_single(oracle_lib):
         assert _same(a.boxes, b.boxes)
 
 
+def _results_equal(a, b):
+    """Equal results.  The count of evaluated samples is not compared: candidates
+    are filtered against the running UB, which depends on the order in which the
+    batch's warps reach them (the results do not)."""
+    assert (a.lb, a.ub, a.iterations, a.status, a.pool_size, a.n_boxes, a.boxes_bounded) == \
+        (b.lb, b.ub, b.iterations, b.status, b.pool_size, b.n_boxes, b.boxes_bounded)
+    assert _same(a.boxes, b.boxes) and _same(a.box_lbs, b.box_lbs)
+    assert (a.xhat is None) == (b.xhat is None)
+    if a.xhat is not None:
+        assert _same(a.xhat, b.xhat)
+
+
+@pytest.mark.parametrize("cap", [0, 1, 4])
+def test_batch_admission_matches_single_submits(cap):
+    """gpugo_submit_batch: one call admits what as many gpugo_submit calls would,
+    each problem's outputs land in its part of the packed buffers, and a full
+    engine admits a prefix (the rest follow once slots are free)."""
+    probs = [make() for _, make in CFGS] + P.config4(count=10, seed=5, nmax=12)
+    for p in probs:
+        p.max_iter = 2000
+    with G.Engine(max_slots=len(probs), arena_bytes=2 << 30) as eng:
+        ts = [eng.submit(p, box_cap=cap) for p in probs]
+        eng.run(0)
+        one = dict(eng.poll())
+    with G.Engine(max_slots=5, arena_bytes=2 << 30) as eng:
+        many, nxt = {}, 0
+        while nxt < len(probs):
+            got = eng.submit_many(probs[nxt:], box_cap=cap)
+            assert len(got) == min(5, len(probs) - nxt)
+            for t in got:
+                many[t] = nxt
+                nxt += 1
+            eng.run(0)
+            done = dict(eng.poll())
+            assert sorted(done) == sorted(got)
+            for t, r in done.items():
+                _results_equal(one[ts[many[t]]], r)
+
+
+def test_batch_admission_stops_at_an_invalid_spec():
+    """An invalid description ends the batch with its error; those before it are
+    admitted and solve."""
+    good = [make() for _, make in CFGS]
+    bad = P.instance(P.COSQUAD, 6, 3, 1e-6)
+    bad.wid = 1                                    # the library refuses wid < 2
+    with G.Engine(max_slots=8, arena_bytes=1 << 30) as eng:
+        with pytest.raises(G.GpugoError) as e:
+            eng.submit_many(good[:2] + [bad] + good[2:], box_cap=2)
+        assert e.value.code == G._lib.ERR_INVALID and len(e.value.admitted) == 2
+        eng.run(0)
+        done = eng.poll()
+    assert sorted(t for t, _ in done) == sorted(e.value.admitted) and all(r.certified for _, r in done)
+
+
 WIDE = [
     ("cosquad40", lambda: P.instance(P.COSQUAD, 40, 21, 1e-6)),
     ("chained30", lambda: P.instance(P.CHAINED, 30, 22, 1e-6)),

@@ -29,6 +29,16 @@ class FakeEngine:
         self.max_resident = max(self.max_resident, len(self.resident))
         return t
 
+    def submit_many(self, probs, box_cap=4):
+        """gpugo_submit_batch's contract: the admitted prefix's tickets."""
+        out = []
+        for p in probs:
+            t = self.submit(p, box_cap)
+            if t is None:
+                break
+            out.append(t)
+        return out
+
     def run(self, k):
         self.runs += 1
         for v in self.resident.values():
