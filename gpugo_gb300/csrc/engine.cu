@@ -271,7 +271,7 @@ __device__ void build_lists_warp(const KArgs& a) {
   const bool have = s < a.max_slots;
   const int stt = have ? a.st[s].status : ST_DONE;
   const bool ex = stt == ST_EXPAND, rp = stt == ST_REPOP;
-  const long long items = ex ? a.desc[s].a_items : 0, kids = ex ? a.st[s].m_children : 0;
+  const long long items = ex ? table_items(a.desc[s], a.st[s].cyc) : 0, kids = ex ? a.st[s].m_children : 0;
   const unsigned mA = __ballot_sync(0xffffffffu, ex), mR = __ballot_sync(0xffffffffu, rp);
   const unsigned mE = __ballot_sync(0xffffffffu, ex || rp);
   const unsigned below = (1u << lane) - 1u;
@@ -334,7 +334,7 @@ __device__ void build_lists(const KArgs& a) {
     long long cA = 0, sA = 0, sB = 0;
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
-        cA++; sA += a.desc[s].a_items; sB += a.st[s].m_children;
+        cA++; sA += table_items(a.desc[s], a.st[s].cyc); sB += a.st[s].m_children;
       }
     }
     long long tA, tSA, tSB;
@@ -347,7 +347,7 @@ __device__ void build_lists(const KArgs& a) {
         a.prefA[oA] = oSA;
         a.prefB[oA] = oSB;
         oA++;
-        oSA += a.desc[s].a_items;
+        oSA += table_items(a.desc[s], a.st[s].cyc);
         oSB += a.st[s].m_children;
       }
     }
@@ -1983,7 +1983,8 @@ __global__ void eval_init_kernel(Desc* desc) {
 
 __global__ void eval_tables_kernel(Desc* desc, int cyc) {
   const Desc& D = desc[0];
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < D.a_items; t += (long long)gridDim.x * blockDim.x)
+  const long long items = table_items(D, cyc);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (long long)gridDim.x * blockDim.x)
     build_item(D, D.parents, D.pwid, cyc, t);
 }
 

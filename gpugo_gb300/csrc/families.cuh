@@ -48,7 +48,7 @@ struct Desc {
   double width_tol, gap_tol;
   long long max_iter;
   long long pool_cap, parent_cap, out_cap, trace_cap, tiles_cap, ubc_cap;
-  long long a_items;                 // table-build work items per iteration
+  long long a_items;                 // table-build items with every coordinate split (table_items: per iteration)
   long long tab_doubles;             // table region size (doubles)
   long long t_off[T_NOFF];           // table offsets (doubles)
   const double* dom;                 // [2n]
@@ -240,7 +240,59 @@ __device__ void init_consts(const Desc& D) {
 // ---------------------------------------------------------------------------
 // table build: one work item -> one table entry
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ long long table_items(const Desc& D) { return D.a_items; }
+// Table entries of one iteration.  Coordinate i has ndig(i) digit values: wid in
+// the split group [c0, c0 + gsz), one outside it, so a pass over the coordinates
+// holds n + gsz (wid - 1) entries (a chained pair or gradient triple touching the
+// group runs all wid^2 or wid^3 digit combinations, the invalid ones returning at
+// once).  Items are numbered densely over these entries: the lanes of a warp do
+// not idle on digit values a coordinate does not have this iteration.  a_items
+// is the count with every coordinate split (the largest over the cycle).
+struct ChainZones {
+  int pl, pr;   // pair positions [0, pl) and [pr, n - 1): one item each; [pl, pr): wid^2 each
+  int gl, gr;   // gradient positions [0, gl) and [gr, n): one item each; [gl, gr): wid^3 each
+};
+__device__ __forceinline__ ChainZones chain_zones(int n, int c0, int gsz) {
+  ChainZones z;
+  z.pl = c0 > 0 ? c0 - 1 : 0;
+  z.pr = c0 + gsz < n - 1 ? c0 + gsz : n - 1;
+  z.gl = z.pl;
+  z.gr = c0 + gsz + 1 < n ? c0 + gsz + 1 : n;
+  return z;
+}
+
+__device__ __forceinline__ long long table_items(const Desc& D, int cyc) {
+  if (D.family == FAM_CODELIST) return D.a_items;
+  const long long n = D.n, w = D.wid, S = D.S;
+  const int c0 = cyc - 1, gsz = group_size(D.n, D.group, cyc);
+  if (D.family == FAM_CHAINED) {
+    const ChainZones z = chain_zones(D.n, c0, gsz);
+    const long long pairs = z.pl + (long long)(z.pr - z.pl) * w * w + (n - 1 - z.pr);
+    const long long grads = z.gl + (long long)(z.gr - z.gl) * w * w * w + (n - z.gr);
+    return pairs * (S + 1) + grads;
+  }
+  return (n + (long long)gsz * (w - 1)) * (S + 2);
+}
+
+// dense entry q of a pass -> (coordinate, digit)
+template <typename U>
+__device__ __forceinline__ void dense_entry(U q, int c0, int gsz, U w, int* i, int* d) {
+  if (q < (U)c0) { *i = (int)q; *d = 0; return; }
+  const U r = q - (U)c0, gw = (U)gsz * w;
+  if (r < gw) { *i = c0 + (int)(r / w); *d = (int)(r % w); return; }
+  *i = c0 + gsz + (int)(r - gw);
+  *d = 0;
+}
+
+// dense position q of a chained zone list (one item per position outside [lo, hi),
+// per items per position inside) -> (position, combination number within it)
+template <typename U>
+__device__ __forceinline__ void zone_entry(U q, int lo, int hi, U per, int* i, U* e) {
+  if (q < (U)lo) { *i = (int)q; *e = 0; return; }
+  const U r = q - (U)lo, span = (U)(hi - lo) * per;
+  if (r < span) { *i = lo + (int)(r / per); *e = r % per; return; }
+  *i = hi + (int)(r - span);
+  *e = 0;
+}
 
 // chained family: gradient of coordinate j given its (up to) three child intervals
 __device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv Xp) {
@@ -275,14 +327,14 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
   const double* k = D.cst;
   double* T = D.tab;
   const long long* off = D.t_off;
-  const U NW = (U)n * w;
+  const U NE = (U)n + (U)gsz * (w - 1);   // entries of one pass (dense_entry)
   switch (D.family) {
     case FAM_COSQUAD: {
-      // [S sample passes x n*w][LB terms: n*w][gradient tests: n*w]
-      const int j = (int)(t / NW);
-      const U e = t - (U)j * NW;
-      const int d = (int)(e % w), i = (int)(e / w);
-      if (d >= ndig(D, c0, gsz, i)) return;
+      // [S sample passes][LB terms][gradient tests], each over the NE entries
+      const int j = (int)(t / NE);
+      int i, d;
+      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[i], a = k[2 * n + i], b = k[3 * n + i];
       if (j == S) {
@@ -301,16 +353,16 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
     }
     case FAM_CHAINED: {
       const U w2 = w * w;
-      const U P1 = (U)(n - 1) * w2;
+      const ChainZones z = chain_zones(n, c0, gsz);
+      const U P1 = (U)z.pl + (U)(z.pr - z.pl) * w2 + (U)(n - 1 - z.pr);   // pairs of one pass
       const U part1 = P1 * (U)(S + 1);
       if (t < part1) {
-        // [S + 1 passes (samples, then LB) x (n-1)*w*w]
+        // [S + 1 passes (samples, then LB) x the pairs (i, i + 1)]
         const int j = (int)(t / P1);
-        const U r = t - (U)j * P1;
-        const int d1 = (int)(r % w);
-        const U r2 = r / w;
-        const int d0 = (int)(r2 % w);
-        const int i = (int)(r2 / w);
+        int i;
+        U r;
+        zone_entry<U>(t - (U)j * P1, z.pl, z.pr, w2, &i, &r);
+        const int d1 = (int)(r % w), d0 = (int)(r / w);
         if (d0 >= ndig(D, c0, gsz, i) || d1 >= ndig(D, c0, gsz, i + 1)) return;
         const double kq = k[n + i], kp = k[i];   // loaded with the parent box, not after the chain
         iv X = child_iv(D, pbox, pw, c0, gsz, i, d0);
@@ -326,10 +378,10 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
         if (j == S) T[off[T_LO] + e] = term.lo;
         else T[off[T_SHI] + e * S + j] = term.hi;
       } else {
-        const U r = t - part1;
         const U w3 = w2 * w;
-        const int j = (int)(r / w3);
-        const U e = r - (U)j * w3;
+        int j;
+        U e;
+        zone_entry<U>(t - part1, z.gl, z.gr, w3, &j, &e);
         const int dm = (int)(e / w2), d = (int)((e / w) % w), dp = (int)(e % w);
         int nm = (j > 0) ? ndig(D, c0, gsz, j - 1) : 1;
         int np = (j + 1 < n) ? ndig(D, c0, gsz, j + 1) : 1;
@@ -344,11 +396,11 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       return;
     }
     case FAM_EXPSQRT: {
-      // [S sample passes x n*w][interval items: n*w][sine items: n*w]
-      const int j = (int)(t / NW);
-      const U e = t - (U)j * NW;
-      const int d = (int)(e % w), i = (int)(e / w);
-      if (d >= ndig(D, c0, gsz, i)) return;
+      // [S sample passes][interval items][sine items], each over the NE entries
+      const int j = (int)(t / NE);
+      int i, d;
+      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[8 + i];
       if (j == S) {
@@ -368,11 +420,11 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       return;
     }
     case FAM_PRODCOS: {
-      // [S sample passes x n*w][interval items: n*w][sine items: n*w]
-      const int j = (int)(t / NW);
-      const U e = t - (U)j * NW;
-      const int d = (int)(e % w), i = (int)(e / w);
-      if (d >= ndig(D, c0, gsz, i)) return;
+      // [S sample passes][interval items][sine items], each over the NE entries
+      const int j = (int)(t / NE);
+      int i, d;
+      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
       if (j == S) {
