@@ -918,6 +918,85 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
   return !__any_sync(0xffffffffu, pruned);
 }
 
+// Lanes per candidate in group_candidate for instance D (0: a warp per candidate).
+__device__ __forceinline__ int group_lanes(const Desc& D) {
+  return (D.S <= 16 && D.family != FAM_EXPSQRT) ? D.S : 0;
+}
+
+// Candidates of instances with S <= 16 samples (exp-sqrt excepted: it spreads
+// its sums over 2S + 4 lanes) taken 32 / G at a time, G = S: group g (lanes
+// g G .. g G + G - 1) processes candidate g, lane j of the group computing
+// sample j, and its lanes then split the KKT coordinates.  An FP64 instruction
+// costs the same for 10 active lanes as for 30, so three candidates of S = 10
+// share what a warp per candidate pays for one.  has: the group holds a
+// candidate (the other lanes only take part in the warp's shuffles).  Returns,
+// on every lane of a group, whether its candidate survives.
+template <bool CL>
+__device__ __noinline__ bool group_candidate(const KArgs& a, int G, bool has, int s, const double* T,
+                                             unsigned long long code, double lb, const double* aux, const double* pfx) {
+  const int lane = threadIdx.x & 31;
+  const int base = (lane / G) * G, lig = lane - base;
+  const Desc& D = a.desc[has ? s : 0];
+  State& st = a.st[has ? s : 0];
+  ChildCtx C;
+  C.c0 = has ? st.cyc - 1 : 0;
+  C.gsz = has ? group_size(D.n, D.group, st.cyc) : 1;
+  double ub = has ? atomic_ub_read(&st.ub) : 0.0;
+  ub = __shfl_sync(0xffffffffu, ub, base);   // one view of the UB per group
+  bool live = has && !flt(ub, lb);
+  const unsigned long long pc = live ? pack_code(D, C.gsz, code) : 0ULL;
+  double bv = 0.0;
+  int bj = J_NONE;
+  if (live && lig < D.S) {
+    bv = samp_one<CL>(D, T, C, pc, lig, ub, pfx);
+    bj = lig;
+  }
+  // minimum over the group's samples (segments of G lanes, G <= 16)
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const double ov = __shfl_down_sync(0xffffffffu, bv, o);
+    const int oj = __shfl_down_sync(0xffffffffu, bj, o);
+    if (lig + o < G && samp_less(ov, oj, bv, bj)) { bv = ov; bj = oj; }
+  }
+  if (live && lig == 0) {
+    double sm = bv;
+    if (feq(sm, 0.0)) sm = 0.0;  // -0 -> +0
+    atomicAdd((unsigned long long*)&st.samples, 1ULL);
+    if (flt(sm, ub)) {
+      long long slot = atomicAdd((unsigned long long*)&st.ubc_count, 1ULL);
+      if (slot < D.ubc_cap) {
+        D.ubc_val[slot] = sm;
+        D.ubc_id[slot] = (code << 8) | (unsigned long long)bj;
+      }
+      atomicMin(&st.ub, ord_key(sm));
+    }
+  }
+  __syncwarp();
+  // the leader's view of the UB decides for the whole group
+  ub = live ? atomic_ub_read(&st.ub) : 0.0;
+  ub = __shfl_sync(0xffffffffu, ub, base);
+  live = live && !flt(ub, lb);
+  DerivPre P;
+  P.g = mk(0.0, 0.0);
+  P.u = P.g;
+  if (live && D.family == FAM_PRODCOS) deriv_pre_aux(aux, &P);
+  int pruned = 0;
+  if (live) {
+    bool done = false;
+    if constexpr (CL) {
+      if (D.family == FAM_CODELIST) {
+        pruned = cl_deriv(D, T, C, pc, lig, G);
+        done = true;
+      }
+    }
+    if (!done)
+      for (int j = lig; j < D.n && !pruned; j += G) pruned = deriv_coord(D, T, C, pc, j, P);
+  }
+  const unsigned int pm = __ballot_sync(0xffffffffu, pruned != 0);
+  const unsigned int gm = ((1u << G) - 1u) << base;
+  return live && (pm & gm) == 0;
+}
+
 // thread_candidate for a code-list instance (one interpreter run per sample)
 __device__ __noinline__ int thread_candidate_cl(const KArgs& a, int s, const double* T, unsigned long long code,
                                                 double lb) {
@@ -1436,8 +1515,42 @@ __device__ void phase_candidates(const KArgs& a) {
       }
       unsigned int lm = __ballot_sync(0xffffffffu, live);
       bool kept = false;   // this lane's own entry survived
+      // entries whose instance takes groups of S lanes (group_candidate)
+      const int my_g = live ? group_lanes(a.desc[s]) : 0;
       while (lm) {
         const int b = __ffs(lm) - 1;
+        const int G = __shfl_sync(0xffffffffu, my_g, b);
+        if (G > 0) {
+          // the next 32 / G live entries of the same group size, one per group
+          unsigned int same = __ballot_sync(0xffffffffu, ((lm >> lane) & 1u) && my_g == G);
+          unsigned int take = 0;
+          for (int k = 32 / G; k > 0 && same; --k) {
+            take |= same & (~same + 1u);
+            same &= same - 1u;
+          }
+          lm &= ~take;
+          // group g takes the g-th entry of `take`
+          const int g = lane / G;
+          unsigned int t = take;
+          for (int k = 0; k < g && t; ++k) t &= t - 1u;
+          const bool has = g < 32 / G && t != 0;
+          const int src = has ? __ffs(t) - 1 : 0;
+          const int gs = __shfl_sync(0xffffffffu, s, src);
+          const unsigned long long gc = __shfl_sync(0xffffffffu, code, src);
+          const double gl = shfl_d(lb, src);
+          double ga[2];
+          ga[0] = shfl_d(aux[0], src);
+          ga[1] = shfl_d(aux[1], src);
+          const double* T = !has ? nullptr : (gs == si) ? s_tab : a.desc[gs].tab;
+          const bool keep = group_candidate<CL>(a, G, has, gs, T, gc, gl, ga,
+                                                (has && pfx_on) ? T + a.desc[gs].t_off[T_PFX] : nullptr);
+          // each entry of `take` reads its group's result from the group's first lane
+          const bool mine = (take >> lane) & 1u;
+          const int from = mine ? __popc(take & ((1u << lane) - 1u)) * G : 0;
+          const bool k2 = __shfl_sync(0xffffffffu, keep, from);
+          if (mine) kept = k2;
+          continue;
+        }
         lm &= lm - 1;
         const int cs = __shfl_sync(0xffffffffu, s, b);
         const unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
