@@ -1249,15 +1249,19 @@ __device__ void phase_bound(const KArgs& a) {
 }
 
 // Candidates per warp from which each lane takes its own candidate instead of a
-// whole warp taking one.  A warp per candidate spreads the S sample passes over
-// S lanes (short latency, the other lanes idle); a lane per candidate keeps all
-// 32 lanes busy but runs the S passes one after the other.  Measured on the
-// GB300 with the 1024-instance mixed batch: 151 ms to certified at 64 per warp,
-// 139 at 8, 132 at 12, 128 at 16 and at 24, 130 at 32.
-constexpr long long LANE_FROM = 24;
+// group of S lanes (or a whole warp) taking one.  A group spreads the S sample
+// passes over S lanes (short latency); a lane per candidate keeps all 32 lanes
+// busy but runs the S passes one after the other, in claims of 32 or 64 that
+// leave warps idle when the queue is short.  Measured on the GB300 with the
+// 1024-instance mixed batch (S = 10): 108.4 ms to certified at 24 per warp, 107.8
+// at 32, 110.4 at 48, 124.2 at 96 and with no lane per candidate at all.
+constexpr long long LANE_FROM = 32;
 // Candidates left per warp below which a lane-per-candidate pass hands its last
-// candidates out one per warp.
-constexpr unsigned long long TAIL_FROM = 4;
+// candidates out TAIL_CLAIM at a time (three groups of ten lanes for S = 10).
+// Measured with LANE_FROM 32: 105.0 ms; tails from 4 per warp 105.6, claims of 1
+// 107.8 (at LANE_FROM 24: claims of 2, 3, 6 gave 106.9, 106.1, 106.2 ms).
+constexpr unsigned long long TAIL_FROM = 8;
+constexpr unsigned long long TAIL_CLAIM = 3;
 
 // instances without queued candidates are ready for their list update at once
 __device__ void prefill_ready(const KArgs& a) {
@@ -1275,8 +1279,8 @@ __device__ void prefill_ready(const KArgs& a) {
     if (tot > a.cand_cap) tot = a.cand_cap;
     long long W = ((long long)gridDim.x * blockDim.x) >> 5;
     long long c = tot / (2 * W);
-    // a warp per candidate while there are fewer than LANE_FROM candidates per
-    // warp; beyond that each lane takes its own candidate, 32 or 64 per claim
+    // lane groups (or a warp) per candidate while there are fewer than LANE_FROM
+    // candidates per warp; beyond that each lane takes its own, 32 or 64 per claim
     long long k = (tot >= LANE_FROM * W) ? (c >= 64 ? 64 : 32) : (c < 1 ? 1 : (c > 31 ? 31 : c));
     if (a.cand_mode == GPUGO_CAND_WARP && k >= 32) k = 31;
     if (a.cand_mode == GPUGO_CAND_LANE && k < 32) k = 32;
@@ -1398,13 +1402,14 @@ __device__ void phase_candidates(const KArgs& a) {
     unsigned long long h = g * K, Kc = K;
     if (!first) {
       if (lane == 0) {
-        // The tail of a long queue goes a warp per candidate: a lane-per-candidate
-        // claim runs each lane's sample passes one after the other, so the last
-        // such claims would keep a few warps busy while all others wait.
+        // The tail of a long queue goes to lane groups, a few candidates per
+        // claim: a lane-per-candidate claim runs each lane's sample passes one
+        // after the other, so the last such claims would keep a few warps busy
+        // while all others wait.
         if (K >= 32) {
           const unsigned long long hd = vload(a.ctl->cand_head);
           const unsigned long long rem = hd < tot ? tot - hd : 0ULL;
-          if (rem < TAIL_FROM * nwarps) Kc = 1;
+          if (rem < TAIL_FROM * nwarps) Kc = TAIL_CLAIM;
         }
         h = atomicAdd(&a.ctl->cand_head, Kc);
       }
