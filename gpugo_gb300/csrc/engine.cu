@@ -111,7 +111,7 @@ struct Ctl {
   int n_big_q;                // big list length (appended during the children phase)
   unsigned int epoch;         // iteration tag of the ready-queue entries
   unsigned long long chunk_next;  // children phase: next chunk to hand out
-  unsigned long long cand_tail;   // candidate queue: entries written in pass 1
+  unsigned long long cand_tail;   // candidates of the pass (numbered across the instances' runs)
   unsigned long long cand_head;   // candidate queue: entries claimed in pass 2
   long long cand_claim;           // entries claimed per atomic in pass 2
   int seed_on;                    // run the seed pass this iteration
@@ -130,6 +130,8 @@ struct KArgs {
   long long* prefD;           // [max_slots + 1] pool tiles prefix of big instances
   unsigned long long* queue;  // [max_slots] ready queue entries: epoch << 32 | slot
   unsigned long long* cands;  // [cand_cap][CAND_WORDS] candidate queue: slot << 32 | code, lb bits, aux
+  long long* prefC;           // [max_slots + 1] candidates of the pass before each work-list position
+  unsigned long long* cpass;  // [max_slots] candidates of the pass per work-list position (zero between passes)
   long long cand_cap;
   long long chunk;            // children bounded per pass (at most cand_cap)
   int cand_mode;              // GPUGO_CAND_AUTO / _WARP / _LANE
@@ -1204,44 +1206,34 @@ __device__ void phase_bound(const KArgs& a) {
         act &= ~__ballot_sync(0xffffffffu, cand && s == ls);
       }
     }
-    unsigned long long qb = 0;
-    if (lane == 0) qb = atomicAdd(&a.ctl->cand_tail, (unsigned long long)__popc(cm));
-    qb = __shfl_sync(0xffffffffu, qb, 0);
-    if (qb + __popc(cm) <= (unsigned long long)a.cand_cap) {
-      if (cand) {
-        unsigned long long pos = qb + __popc(cm & ((1u << lane) - 1u));
-        unsigned long long* e = a.cands + CAND_WORDS * pos;
-        e[0] = ((unsigned long long)s << 32) | code;
-        e[1] = (unsigned long long)__double_as_longlong(lb);
+    // Candidates are stored in runs, one per instance: instance k's run starts
+    // where its children of this pass start in the pass's flat range (so it
+    // cannot overflow into the next run, and the pass has at most cand_cap
+    // children).  Pass 2 then takes claims of one instance's candidates.
+    unsigned long long pos = 0;
+    unsigned int act = cm;
+    while (act) {
+      const int leader = __ffs(act) - 1;
+      const int lk = __shfl_sync(0xffffffffu, k, leader);
+      const unsigned int m = __ballot_sync(0xffffffffu, cand && k == lk);
+      unsigned long long base = 0;
+      if (lane == leader) {
+        base = atomicAdd(&a.cpass[lk], (unsigned long long)__popc(m));
+        atomicAdd((unsigned long long*)&a.st[s].cand_total, (unsigned long long)__popc(m));
+      }
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (cand && k == lk) {
+        const long long start = (a.prefB[k] > lo ? a.prefB[k] : lo) - lo;
+        pos = (unsigned long long)start + base + __popc(m & ((1u << lane) - 1u));
+      }
+      act &= ~m;
+    }
+    if (cand) {
+      unsigned long long* e = a.cands + CAND_WORDS * pos;
+      e[0] = ((unsigned long long)s << 32) | code;
+      e[1] = (unsigned long long)__double_as_longlong(lb);
 #pragma unroll
-        for (int q = 0; q < 2; ++q) e[2 + q] = (unsigned long long)__double_as_longlong(aux[q]);
-      }
-      // per-instance queued counts
-      unsigned int act = cm;
-      while (act) {
-        int leader = __ffs(act) - 1;
-        int ls = __shfl_sync(0xffffffffu, s, leader);
-        unsigned int m = __ballot_sync(0xffffffffu, cand && s == ls);
-        if (lane == leader) atomicAdd((unsigned long long*)&a.st[ls].cand_total, (unsigned long long)__popc(m));
-        act &= ~m;
-      }
-    } else {
-      // queue full: process these candidates right here (not reached while a
-      // children pass has at most cand_cap children; kept as the safe path)
-      bool keep = false;
-      while (cm) {
-        int b = __ffs(cm) - 1;
-        cm &= cm - 1;
-        int cs = __shfl_sync(0xffffffffu, s, b);
-        unsigned long long cc = __shfl_sync(0xffffffffu, code, b);
-        double cl = shfl_d(lb, b);
-        double ca[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) ca[q] = shfl_d(aux[q], b);
-        bool kk = warp_candidate<CL>(a, cs, (cs == si) ? s_tab : a.desc[cs].tab, cc, cl, ca, nullptr);
-        if (lane == b) keep = kk;
-      }
-      warp_append_survivors(a, keep, s, code, lb);
+      for (int q = 0; q < 2; ++q) e[2 + q] = (unsigned long long)__double_as_longlong(aux[q]);
     }
   }
   __syncthreads();
@@ -1273,6 +1265,26 @@ __device__ void prefill_ready(const KArgs& a) {
       int s = a.idsA[k];
       if (vload(a.st[s].cand_total) == vload(a.st[s].cand_done)) queue_push(a, s);
     }
+  }
+  {
+    // number the pass's candidates across the per-instance runs (prefC) and
+    // clear the run counters for the next pass
+    const int per = (nA + blockDim.x - 1) / blockDim.x;
+    const int lo = threadIdx.x * per, hi = min(nA, lo + per);
+    long long c = 0;
+    for (int k = lo; k < hi; ++k) c += (long long)__ldcg(a.cpass + k);
+    long long total;
+    long long o = block_exclusive_scan(c, &total);
+    for (int k = lo; k < hi; ++k) {
+      a.prefC[k] = o;
+      o += (long long)__ldcg(a.cpass + k);
+      a.cpass[k] = 0ULL;
+    }
+    if (threadIdx.x == 0) {
+      a.prefC[nA] = total;
+      a.ctl->cand_tail = (unsigned long long)total;
+    }
+    __syncthreads();
   }
   if (threadIdx.x == 0) {
     long long tot = (long long)vload(a.ctl->cand_tail);
@@ -1375,6 +1387,17 @@ __device__ __forceinline__ void instance_ready(const KArgs& a, int s) {
   __syncwarp();
 }
 
+// Queue position of candidate number q of the pass: instance k's candidates
+// (numbers prefC[k] .. prefC[k + 1] - 1) lie in its run, which starts where its
+// children of the pass start.  hint: the lane's last instance.
+__device__ __forceinline__ unsigned long long cand_pos(const KArgs& a, unsigned long long q, long long b_lo, int nA,
+                                                       int& hint) {
+  const int k = find_seg(a.prefC, nA, (long long)q, hint);
+  hint = k;
+  const long long pb = a.prefB[k];
+  return (unsigned long long)((pb > b_lo ? pb : b_lo) - b_lo + ((long long)q - a.prefC[k]));
+}
+
 template <bool CL>
 __device__ void phase_candidates(const KArgs& a) {
   extern __shared__ __align__(16) double s_tab[];
@@ -1391,6 +1414,9 @@ __device__ void phase_candidates(const KArgs& a) {
   const bool pfx_on = vload(a.ctl->seed_on) != 0;   // the seed pass stored the shared sample prefixes
   // instances are updated only after the iteration's last children pass
   const bool last = vload(a.ctl->b_last) != 0;
+  const long long b_lo = vload(a.ctl->b_lo);
+  const int nA = a.ctl->nA;
+  int chint = -1;
   // With a short queue (a warp per candidate) the first claim of warp g (numbered
   // across the blocks first) is the range g*K: the candidates land on warps of
   // different SMs, which do not share an FP64 unit.  Later claims, and every
@@ -1431,14 +1457,17 @@ __device__ void phase_candidates(const KArgs& a) {
         bool valid = q < e;
         bool live = false;
         int s = -1;
+        unsigned long long p = 0;
         if (valid) {
-          const unsigned long long* en = a.cands + CAND_WORDS * q;
+          p = cand_pos(a, q, b_lo, nA, chint);
+          const unsigned long long* en = a.cands + CAND_WORDS * p;
           s = (int)(en[0] >> 32);
           double lb = __longlong_as_double((long long)en[1]);
           live = !flt(atomic_ub_read(&a.st[s].ub), lb);
         }
         unsigned int lm = __ballot_sync(0xffffffffu, live);
-        if (live) surv[nsurv + __popc(lm & ((1u << lane) - 1u))] = (unsigned int)(q - h);
+        // queue positions of the survivors (below cand_cap <= 2^24)
+        if (live) surv[nsurv + __popc(lm & ((1u << lane) - 1u))] = (unsigned int)p;
         nsurv += __popc(lm);
         // candidates ruled out here are done
         unsigned int act = __ballot_sync(0xffffffffu, valid && !live);
@@ -1461,7 +1490,7 @@ __device__ void phase_candidates(const KArgs& a) {
         int s = -1;
         bool keep = false, sampled = false;
         if (valid) {
-          const unsigned long long q = h + surv[idx];
+          const unsigned long long q = surv[idx];
           const unsigned long long* en = a.cands + CAND_WORDS * q;
           s = (int)(en[0] >> 32);
           unsigned long long code = en[0] & 0xffffffffULL;
@@ -1475,7 +1504,7 @@ __device__ void phase_candidates(const KArgs& a) {
           sampled = rr & 2;
         }
         {
-          const unsigned long long q = valid ? h + surv[idx] : 0ULL;
+          const unsigned long long q = valid ? surv[idx] : 0ULL;
           const unsigned long long code = valid ? (a.cands[CAND_WORDS * q] & 0xffffffffULL) : 0ULL;
           const double lb = valid ? __longlong_as_double((long long)a.cands[CAND_WORDS * q + 1]) : 0.0;
           warp_append_survivors(a, keep, s, code, lb);
@@ -1509,7 +1538,7 @@ __device__ void phase_candidates(const KArgs& a) {
       double lb = 0.0, aux[2] = {0.0, 0.0};
       bool live = false;
       if (valid) {
-        const unsigned long long* en = a.cands + CAND_WORDS * q;
+        const unsigned long long* en = a.cands + CAND_WORDS * cand_pos(a, q, b_lo, nA, chint);
         const unsigned long long w0 = en[0];
         s = (int)(w0 >> 32);
         code = w0 & 0xffffffffULL;
@@ -1906,7 +1935,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) solve_kernel(KArgs a) {
   TailPrefill tp{&a};
   TailNextPass tn{&a};
   // queue entries of earlier launches carry stale epochs
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_slots; i += gridDim.x * blockDim.x) a.queue[i] = 0ULL;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_slots; i += gridDim.x * blockDim.x) {
+    a.queue[i] = 0ULL;
+    a.cpass[i] = 0ULL;
+  }
   if (!grid_barrier(a, tl)) return;
   long long it = 0;
   while (a.ctl->nE > 0 && (a.max_iters <= 0 || it < a.max_iters)) {
@@ -2266,7 +2298,7 @@ struct gpugo_engine {
   unsigned long long* d_cands = nullptr;
   long long cand_cap = 0;
   long long chunk = 0;           // children per pass (<= cand_cap)
-  long long* d_pref = nullptr;   // prefA | prefB | prefD
+  long long* d_pref = nullptr;   // prefA | prefB | prefD | prefC | cpass
   char* d_arena = nullptr;
   Arena arena;
   std::vector<HostSlot> slots;
@@ -2965,7 +2997,7 @@ int gpugo_engine_create(const gpugo_engine_cfg* cfg, gpugo_engine** out) {
     E->cand_cap = std::min<long long>(1LL << 24, std::max<long long>(1LL << 20, 8192LL * E->max_slots));
     if ((rc = cuda_err(cudaMalloc(&E->d_cands, 8 * CAND_WORDS * (size_t)E->cand_cap)))) break;
     E->chunk = cfg->chunk_children > 0 ? std::min<long long>(cfg->chunk_children, E->cand_cap) : E->cand_cap;
-    if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 3 * (E->max_slots + 1))))) break;
+    if ((rc = cuda_err(cudaMalloc(&E->d_pref, sizeof(long long) * 5 * (E->max_slots + 1))))) break;
     if (cudaMalloc(&E->d_arena, (size_t)cfg->arena_bytes) != cudaSuccess) { cudaGetLastError(); rc = GPUGO_ERR_NOMEM; break; }
     E->arena.init(E->d_arena, (size_t)cfg->arena_bytes);
     if (const char* sp = getenv("GPUGO_PHASE_STAMPS")) {
@@ -3371,6 +3403,8 @@ int gpugo_run(gpugo_engine* E, int64_t max_iters, int32_t* active_out) {
   a.prefA = E->d_pref;
   a.prefB = E->d_pref + (E->max_slots + 1);
   a.prefD = E->d_pref + 2 * (E->max_slots + 1);
+  a.prefC = E->d_pref + 3 * (E->max_slots + 1);
+  a.cpass = (unsigned long long*)(E->d_pref + 4 * (E->max_slots + 1));
   a.queue = E->d_queue;
   a.cands = E->d_cands;
   a.cand_cap = E->cand_cap;
