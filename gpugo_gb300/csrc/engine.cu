@@ -273,7 +273,7 @@ __device__ void build_lists_warp(const KArgs& a) {
   const bool have = s < a.max_slots;
   const int stt = have ? a.st[s].status : ST_DONE;
   const bool ex = stt == ST_EXPAND, rp = stt == ST_REPOP;
-  const long long items = ex ? table_items(a.desc[s], a.st[s].cyc) : 0, kids = ex ? a.st[s].m_children : 0;
+  const long long items = ex ? table_items(a.desc[s], a.st[s].cyc, false) : 0, kids = ex ? a.st[s].m_children : 0;
   const unsigned mA = __ballot_sync(0xffffffffu, ex), mR = __ballot_sync(0xffffffffu, rp);
   const unsigned mE = __ballot_sync(0xffffffffu, ex || rp);
   const unsigned below = (1u << lane) - 1u;
@@ -336,7 +336,7 @@ __device__ void build_lists(const KArgs& a) {
     long long cA = 0, sA = 0, sB = 0;
     for (int s = lo; s < hi; ++s) {
       if (a.st[s].status == ST_EXPAND && (f == 0 || a.desc[s].family == f)) {
-        cA++; sA += table_items(a.desc[s], a.st[s].cyc); sB += a.st[s].m_children;
+        cA++; sA += table_items(a.desc[s], a.st[s].cyc, false); sB += a.st[s].m_children;
       }
     }
     long long tA, tSA, tSB;
@@ -349,7 +349,7 @@ __device__ void build_lists(const KArgs& a) {
         a.prefA[oA] = oSA;
         a.prefB[oA] = oSB;
         oA++;
-        oSA += table_items(a.desc[s], a.st[s].cyc);
+        oSA += table_items(a.desc[s], a.st[s].cyc, false);
         oSB += a.st[s].m_children;
       }
     }
@@ -484,7 +484,8 @@ __device__ void phase_tables(const KArgs& a) {
     int s = a.idsA[k];
     const Desc& D = a.desc[s];
     const State& st = a.st[s];
-    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k]);
+    build_item<CL>(D, D.parents + 2LL * D.n * st.iter, D.pwid + (long long)D.n * st.iter, st.cyc, it - a.prefA[k],
+                   false);
   }
   __syncthreads();
   bstamp(a, 1);
@@ -915,8 +916,12 @@ __device__ bool warp_candidate(const KArgs& a, int s, const double* T, unsigned 
       done = true;
     }
   }
-  if (!done && !skip)
-    for (int j = lane; j < D.n && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
+  {
+    int klo, khi;
+    kkt_span(D, C, &klo, &khi);
+    if (!done && !skip)
+      for (int j = klo + lane; j < khi && !pruned; j += 32) pruned = deriv_coord(D, T, C, pc, j, P);
+  }
   return !__any_sync(0xffffffffu, pruned);
 }
 
@@ -991,8 +996,11 @@ __device__ __noinline__ bool group_candidate(const KArgs& a, int G, bool has, in
         done = true;
       }
     }
-    if (!done)
-      for (int j = lig; j < D.n && !pruned; j += G) pruned = deriv_coord(D, T, C, pc, j, P);
+    if (!done) {
+      int klo, khi;
+      kkt_span(D, C, &klo, &khi);
+      for (int j = klo + lig; j < khi && !pruned; j += G) pruned = deriv_coord(D, T, C, pc, j, P);
+    }
   }
   const unsigned int pm = __ballot_sync(0xffffffffu, pruned != 0);
   const unsigned int gm = ((1u << G) - 1u) << base;
@@ -1089,7 +1097,9 @@ __device__ int thread_candidate(const KArgs& a, int s, const double* T, unsigned
   } else if (D.family == FAM_PRODCOS) {
     deriv_pre_aux(aux, &P);
   }
-  for (int jj = 0; jj < D.n; ++jj)
+  int klo, khi;
+  kkt_span(D, C, &klo, &khi);
+  for (int jj = klo; jj < khi; ++jj)
     if (deriv_coord(D, T, C, pc, jj, P)) return 2;
   return 3;
 }
@@ -2133,9 +2143,9 @@ __global__ void eval_init_kernel(Desc* desc) {
 
 __global__ void eval_tables_kernel(Desc* desc, int cyc) {
   const Desc& D = desc[0];
-  const long long items = table_items(D, cyc);
+  const long long items = table_items(D, cyc, true);   // any parent box: every KKT flag
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (long long)gridDim.x * blockDim.x)
-    build_item(D, D.parents, D.pwid, cyc, t);
+    build_item(D, D.parents, D.pwid, cyc, t, true);
 }
 
 __global__ void eval_children_kernel(Desc* desc, int cyc, const unsigned long long* codes, long long m, double ub,

@@ -260,17 +260,42 @@ __device__ __forceinline__ ChainZones chain_zones(int n, int c0, int gsz) {
   return z;
 }
 
-__device__ __forceinline__ long long table_items(const Desc& D, int cyc) {
+// all_kkt: KKT flags for every coordinate (per-child evaluation of any parent);
+// inside a solve only the coordinates kkt_span names are built.
+__device__ __forceinline__ long long table_items(const Desc& D, int cyc, bool all_kkt) {
   if (D.family == FAM_CODELIST) return D.a_items;
   const long long n = D.n, w = D.wid, S = D.S;
   const int c0 = cyc - 1, gsz = group_size(D.n, D.group, cyc);
   if (D.family == FAM_CHAINED) {
     const ChainZones z = chain_zones(D.n, c0, gsz);
     const long long pairs = z.pl + (long long)(z.pr - z.pl) * w * w + (n - 1 - z.pr);
-    const long long grads = z.gl + (long long)(z.gr - z.gl) * w * w * w + (n - z.gr);
+    const long long grads = (long long)(z.gr - z.gl) * w * w * w + (all_kkt ? z.gl + (n - z.gr) : 0);
     return pairs * (S + 1) + grads;
   }
-  return (n + (long long)gsz * (w - 1)) * (S + 2);
+  const long long ne = n + (long long)gsz * (w - 1);
+  if (D.family == FAM_COSQUAD && !all_kkt) return ne * (S + 1) + (long long)gsz * w;
+  return ne * (S + 2);
+}
+
+// Coordinates whose KKT flag a child of a solve's parent can have set.  For the
+// two separable one-sum families the flag of coordinate j depends on its own
+// interval (cos-quadratic) or on those of j - 1 .. j + 1 (chained gradient).
+// Outside the split group a child keeps its parent's intervals, and the parent
+// -- a child kept by the same test, or the whole domain, where no flag is set
+// (every interval touches both domain bounds) -- has those flags clear.  The
+// other families test every coordinate: their derivative scalars change with
+// any coordinate.
+__device__ __forceinline__ void kkt_span(const Desc& D, ChildCtx C, int* lo, int* hi) {
+  if (D.family == FAM_COSQUAD) {
+    *lo = C.c0;
+    *hi = C.c0 + C.gsz;
+  } else if (D.family == FAM_CHAINED) {
+    *lo = C.c0 > 0 ? C.c0 - 1 : 0;
+    *hi = C.c0 + C.gsz + 1 < D.n ? C.c0 + C.gsz + 1 : D.n;
+  } else {
+    *lo = 0;
+    *hi = D.n;
+  }
 }
 
 // dense entry q of a pass -> (coordinate, digit)
@@ -320,7 +345,8 @@ __device__ __forceinline__ iv chained_grad(const Desc& D, int j, iv Xm, iv X, iv
 // run the same code path; index arithmetic is 32-bit (U = unsigned) unless an
 // instance has 2^31 items or more.
 template <typename U>
-__device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, const double* pw, int cyc, U t) {
+__device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, const double* pw, int cyc, U t,
+                                             bool all_kkt) {
   const int n = D.n, S = D.S;
   const U w = (U)D.wid;
   const int c0 = cyc - 1, gsz = group_size(n, D.group, cyc);
@@ -330,10 +356,18 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
   const U NE = (U)n + (U)gsz * (w - 1);   // entries of one pass (dense_entry)
   switch (D.family) {
     case FAM_COSQUAD: {
-      // [S sample passes][LB terms][gradient tests], each over the NE entries
-      const int j = (int)(t / NE);
+      // [S sample passes][LB terms] over the NE entries, then the gradient tests:
+      // over the NE entries (all_kkt) or over the split group's entries only
+      int j = (int)(t / NE);
       int i, d;
-      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      if (j > S && !all_kkt) {
+        const U r = t - (U)(S + 1) * NE;
+        i = c0 + (int)(r / w);
+        d = (int)(r % w);
+        j = S + 1;
+      } else {
+        dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      }
       const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[i], a = k[2 * n + i], b = k[3 * n + i];
@@ -378,10 +412,17 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
         if (j == S) T[off[T_LO] + e] = term.lo;
         else T[off[T_SHI] + e * S + j] = term.hi;
       } else {
+        // the gradient triples: positions [gl, gr) only, unless all_kkt
         const U w3 = w2 * w;
         int j;
         U e;
-        zone_entry<U>(t - part1, z.gl, z.gr, w3, &j, &e);
+        if (all_kkt) {
+          zone_entry<U>(t - part1, z.gl, z.gr, w3, &j, &e);
+        } else {
+          const U r = t - part1;
+          j = z.gl + (int)(r / w3);
+          e = r % w3;
+        }
         const int dm = (int)(e / w2), d = (int)((e / w) % w), dp = (int)(e % w);
         int nm = (j > 0) ? ndig(D, c0, gsz, j - 1) : 1;
         int np = (j + 1 < n) ? ndig(D, c0, gsz, j + 1) : 1;
@@ -449,12 +490,13 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
 }
 
 template <bool CL = true>
-__device__ __forceinline__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t) {
+__device__ __forceinline__ void build_item(const Desc& D, const double* pbox, const double* pw, int cyc, long long t,
+                                           bool all_kkt) {
   if constexpr (CL) {
     if (D.family == FAM_CODELIST) { cl_build_item(D, pbox, pw, cyc, t); return; }
   }
-  if (D.a_items < (1LL << 31)) build_item_t<unsigned>(D, pbox, pw, cyc, (unsigned)t);
-  else build_item_t<unsigned long long>(D, pbox, pw, cyc, (unsigned long long)t);
+  if (D.a_items < (1LL << 31)) build_item_t<unsigned>(D, pbox, pw, cyc, (unsigned)t, all_kkt);
+  else build_item_t<unsigned long long>(D, pbox, pw, cyc, (unsigned long long)t, all_kkt);
 }
 
 // ---------------------------------------------------------------------------
