@@ -2579,11 +2579,11 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
   switch (s->family) {
     case GPUGO_COSQUAD:
       put(T_LO, n * w); put(T_SHI, n * w * S); put(T_PRB, (n * w + 7) / 8);
-      L->a_items = n * w * (S + 2);
+      L->a_items = n * w * (S + 2) + 64;   // + the padding that aligns item kinds to warps
       break;
     case GPUGO_CHAINED:
       put(T_LO, (n - 1) * w * w); put(T_SHI, (n - 1) * w * w * S); put(T_PRB, (n * w * w * w + 7) / 8);
-      L->a_items = (n - 1) * w * w * (S + 1) + n * w * w * w;
+      L->a_items = (n - 1) * w * w * (S + 1) + n * w * w * w + 32;
       break;
     case GPUGO_CODELIST: {
       put(T_LO, 2 * n * w); put(T_SHI, n * w * S);
@@ -2617,12 +2617,12 @@ void layout(const gpugo_spec* s, int64_t out_cap, int64_t trace_cap, Layout* L) 
     case GPUGO_EXPSQRT:
       put(T_SQ, 2 * n * w); put(T_CS, 2 * n * w); put(T_XI, 2 * n * w); put(T_SN, 2 * n * w);
       put(T_ZB, (n * w + 7) / 8); put(T_SQS, 2 * n * w * S); put(T_CSS, 2 * n * w * S);
-      L->a_items = n * w * (S + 2);
+      L->a_items = n * w * (S + 2) + 64;
       break;
     default:
       put(T_CR, 2 * n * w); put(T_SQ4, 2 * n * w); put(T_SNA, 2 * n * w); put(T_XD2, 2 * n * w);
       put(T_XI4, 2 * n * w); put(T_CRS, 2 * n * w * S); put(T_SQS4, 2 * n * w * S); put(T_RCP4, 2 * n * w);
-      L->a_items = n * w * (S + 2);
+      L->a_items = n * w * (S + 2) + 64;
       break;
   }
   put(T_PFX, 3 * S);

@@ -260,6 +260,12 @@ __device__ __forceinline__ ChainZones chain_zones(int n, int c0, int gsz) {
   return z;
 }
 
+// Each kind of item (sample points, intervals, sines or gradient tests) starts
+// on a multiple of 32, so that no warp runs two kinds' code one after the other:
+// the numbers in between are padding (the item returns at once).
+template <typename U>
+__device__ __forceinline__ U pad32(U x) { return (x + 31) & ~(U)31; }
+
 // all_kkt: KKT flags for every coordinate (per-child evaluation of any parent);
 // inside a solve only the coordinates kkt_span names are built.
 __device__ __forceinline__ long long table_items(const Desc& D, int cyc, bool all_kkt) {
@@ -270,11 +276,11 @@ __device__ __forceinline__ long long table_items(const Desc& D, int cyc, bool al
     const ChainZones z = chain_zones(D.n, c0, gsz);
     const long long pairs = z.pl + (long long)(z.pr - z.pl) * w * w + (n - 1 - z.pr);
     const long long grads = (long long)(z.gr - z.gl) * w * w * w + (all_kkt ? z.gl + (n - z.gr) : 0);
-    return pairs * (S + 1) + grads;
+    return pad32(pairs * (S + 1)) + grads;
   }
   const long long ne = n + (long long)gsz * (w - 1);
-  if (D.family == FAM_COSQUAD && !all_kkt) return ne * (S + 1) + (long long)gsz * w;
-  return ne * (S + 2);
+  const long long last = (D.family == FAM_COSQUAD && !all_kkt) ? (long long)gsz * w : ne;
+  return pad32(ne * S) + pad32(ne) + last;
 }
 
 // Coordinates whose KKT flag a child of a solve's parent can have set.  For the
@@ -354,19 +360,32 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
   double* T = D.tab;
   const long long* off = D.t_off;
   const U NE = (U)n + (U)gsz * (w - 1);   // entries of one pass (dense_entry)
+  // per-coordinate families: S sample passes, then two kinds of NE items, each
+  // kind from a multiple of 32 (pad32)
+  const U SNE = (U)S * NE, K1 = pad32(SNE), K2 = K1 + pad32(NE);
   switch (D.family) {
     case FAM_COSQUAD: {
       // [S sample passes][LB terms] over the NE entries, then the gradient tests:
       // over the NE entries (all_kkt) or over the split group's entries only
-      int j = (int)(t / NE);
-      int i, d;
-      if (j > S && !all_kkt) {
-        const U r = t - (U)(S + 1) * NE;
+      int j, i, d;
+      if (t < SNE) {
+        j = (int)(t / NE);
+        dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      } else if (t < K1) {
+        return;
+      } else if (t < K1 + NE) {
+        j = S;
+        dense_entry<U>(t - K1, c0, gsz, w, &i, &d);
+      } else if (t < K2) {
+        return;
+      } else if (all_kkt) {
+        j = S + 1;
+        dense_entry<U>(t - K2, c0, gsz, w, &i, &d);
+      } else {
+        const U r = t - K2;
+        j = S + 1;
         i = c0 + (int)(r / w);
         d = (int)(r % w);
-        j = S + 1;
-      } else {
-        dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
       }
       const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
@@ -390,6 +409,7 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
       const ChainZones z = chain_zones(n, c0, gsz);
       const U P1 = (U)z.pl + (U)(z.pr - z.pl) * w2 + (U)(n - 1 - z.pr);   // pairs of one pass
       const U part1 = P1 * (U)(S + 1);
+      if (t >= part1 && t < pad32(part1)) return;
       if (t < part1) {
         // [S + 1 passes (samples, then LB) x the pairs (i, i + 1)]
         const int j = (int)(t / P1);
@@ -417,9 +437,9 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
         int j;
         U e;
         if (all_kkt) {
-          zone_entry<U>(t - part1, z.gl, z.gr, w3, &j, &e);
+          zone_entry<U>(t - pad32(part1), z.gl, z.gr, w3, &j, &e);
         } else {
-          const U r = t - part1;
+          const U r = t - pad32(part1);
           j = z.gl + (int)(r / w3);
           e = r % w3;
         }
@@ -438,9 +458,16 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
     }
     case FAM_EXPSQRT: {
       // [S sample passes][interval items][sine items], each over the NE entries
-      const int j = (int)(t / NE);
-      int i, d;
-      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      int j, i, d;
+      if (t < SNE) {
+        j = (int)(t / NE);
+        dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      } else if (t < K1 || (t >= K1 + NE && t < K2)) {
+        return;
+      } else {
+        j = (t < K2) ? S : S + 1;
+        dense_entry<U>(t - ((t < K2) ? K1 : K2), c0, gsz, w, &i, &d);
+      }
       const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       double K = k[8 + i];
@@ -462,9 +489,16 @@ __device__ __forceinline__ void build_item_t(const Desc& D, const double* pbox, 
     }
     case FAM_PRODCOS: {
       // [S sample passes][interval items][sine items], each over the NE entries
-      const int j = (int)(t / NE);
-      int i, d;
-      dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      int j, i, d;
+      if (t < SNE) {
+        j = (int)(t / NE);
+        dense_entry<U>(t - (U)j * NE, c0, gsz, w, &i, &d);
+      } else if (t < K1 || (t >= K1 + NE && t < K2)) {
+        return;
+      } else {
+        j = (t < K2) ? S : S + 1;
+        dense_entry<U>(t - ((t < K2) ? K1 : K2), c0, gsz, w, &i, &d);
+      }
       const U e = (U)i * w + (U)d;
       iv X = child_iv(D, pbox, pw, c0, gsz, i, d);
       iv RSQ = mk(k[4 + 2 * i], k[4 + 2 * i + 1]);
