@@ -1260,9 +1260,10 @@ __device__ void phase_bound(const KArgs& a) {
 constexpr long long LANE_FROM = 32;
 // Candidates left per warp below which a lane-per-candidate pass hands its last
 // candidates out TAIL_CLAIM at a time (three groups of ten lanes for S = 10).
-// Measured with LANE_FROM 32: 105.0 ms; tails from 4 per warp 105.6, claims of 1
-// 107.8 (at LANE_FROM 24: claims of 2, 3, 6 gave 106.9, 106.1, 106.2 ms).
-constexpr unsigned long long TAIL_FROM = 8;
+// Measured with LANE_FROM 32: tails from 4, 8, 16, 32 per warp 105.6, 105.0,
+// 102.1 (on the later per-instance queue runs; 102.9 at 8 there), 107.7 ms;
+// claims of 1 107.8, of 6 102.6 (at 16 per warp).
+constexpr unsigned long long TAIL_FROM = 16;
 constexpr unsigned long long TAIL_CLAIM = 3;
 
 // instances without queued candidates are ready for their list update at once
