@@ -1309,7 +1309,11 @@ __device__ void prefill_ready(const KArgs& a) {
     if (a.cand_mode == GPUGO_CAND_LANE && k < 32) k = 32;
     a.ctl->cand_claim = k;
     a.ctl->cand_head = (k < 32) ? (unsigned long long)(W * k) : 0ULL;   // short queues: static first claims
-    a.ctl->seed_on = (tot > 4 * W) ? 1 : 0;
+    // the seed pass costs a sample chain per instance; it pays from 4 candidates
+    // per warp with a single instance, from 16 in batches (measured: config 3
+    // 3.86 ms seeding from 1 per warp, 3.88 from 4, 4.06 from 16; the 1024
+    // batch 102.5, 102.2, 101.2 ms)
+    a.ctl->seed_on = (tot > (nA <= 4 ? 4 : 16) * W) ? 1 : 0;
     a.ctl->cand_tail = (unsigned long long)tot;
   }
 }
