@@ -282,10 +282,12 @@ class Engine:
         rc = self._L.gpugo_submit_batch(self._h, specs.ctypes.data, m, boxes.ctypes.data, lbs.ctypes.data, cap,
                                         xhat.ctypes.data, tickets.ctypes.data, ctypes.byref(done))
         k = done.value
-        for i in range(k):     # admitted problems are registered before an error is raised
-            a, n = int(at[i]), int(ns[i])
-            self._pending[int(tickets[i])] = (problems[i], boxes[2 * cap * a:2 * cap * (a + n)].reshape(cap, 2 * n),
-                                              lbs[cap * i:cap * (i + 1)], xhat[a:a + n], None, None, None)
+        # admitted problems are registered before an error is raised; their parts
+        # of the shared buffers are cut out when their results come (poll)
+        out = (boxes, lbs, xhat, cap)
+        self._pending.update(zip(tickets[:k].tolist(),
+                                 ((q, None, None, None, None, None, (out, i, a))
+                                  for i, (q, a) in enumerate(zip(problems[:k], at[:k].tolist())))))
         if rc < 0 and rc != _lib.ERR_BUSY:
             err = GpugoError(rc, f"gpugo_submit_batch (problem {k})")
             err.admitted = tickets[:k].tolist()
@@ -340,10 +342,18 @@ class Engine:
         rows = zip(rec["ticket"].tolist(), *cols)
         for i, (t, lb, ub, status, iters, bb, se, ps, nb, k, hx, dms) in enumerate(rows):
             p, boxes, lbs, xhat, arrs, tr, keep = self._pending.pop(t)
+            n = p.n
+            if boxes is None:
+                # a batch admission (submit_many): problem j's parts of the shared buffers
+                (bx, bl, bh, cap), j, at = keep
+                out.append((t, SolveResult(lb, ub, status, iters, bb, se, ps, nb,
+                                           bx[2 * cap * at:2 * cap * at + 2 * n * k].reshape(k, n, 2),
+                                           bl[cap * j:cap * j + k], bh[at:at + n] if hx else None, dms)))
+                continue
             if arrs is not None:
                 out.append((t, _result(p, arr[i].result, boxes, lbs, xhat, arrs)))
                 continue
-            out.append((t, SolveResult(lb, ub, status, iters, bb, se, ps, nb, boxes[:k].reshape(k, p.n, 2),
+            out.append((t, SolveResult(lb, ub, status, iters, bb, se, ps, nb, boxes[:k].reshape(k, n, 2),
                                        lbs[:k], xhat if hx else None, dms)))
         return out
 

@@ -2317,6 +2317,7 @@ struct gpugo_engine {
   char* d_arena = nullptr;
   Arena arena;
   std::vector<HostSlot> slots;
+  int free_from = 0;             // every slot below this index is in use
   std::vector<int> pending_init;
   // admissions since the last run, packed as records (admit_kernel's layout)
   std::vector<unsigned long long> stage;
@@ -3087,7 +3088,7 @@ int admit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* bo
   if (trace && trace->cap > 0 && (!trace->ub || !trace->n_surv || !trace->pool || !trace->sel))
     return GPUGO_ERR_INVALID;
   int slot = -1;
-  for (int s = 0; s < E->max_slots; ++s) if (!E->slots[s].used) { slot = s; break; }
+  for (int s = E->free_from; s < E->max_slots; ++s) if (!E->slots[s].used) { slot = s; break; }
   if (slot < 0) return GPUGO_ERR_BUSY;
   Layout L;
   layout(spec, cap, trace ? trace->cap : 0, &L);
@@ -3096,6 +3097,7 @@ int admit(gpugo_engine* E, const gpugo_spec* spec, double* boxes_out, double* bo
   HostSlot& h = E->slots[slot];
   h = HostSlot();
   h.used = true;
+  E->free_from = slot + 1;
   h.ticket = E->next_ticket++;
   h.spec = *spec;
   h.dom.assign(spec->domain, spec->domain + 2 * spec->n);
@@ -3580,6 +3582,7 @@ int gpugo_poll(gpugo_engine* E, gpugo_done* done, int32_t max_done, int32_t* n_d
     memset(&z, 0, sizeof(z));
     E->h_state[s] = z;
     h = HostSlot();
+    if (s < E->free_from) E->free_from = s;
   }
   if (n_done_out) *n_done_out = k;
   return GPUGO_OK;
