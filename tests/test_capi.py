@@ -140,6 +140,11 @@ def test_null_arguments_are_rejected_before_the_device(lib):
     assert lib.gpugo_solve(ctypes.byref(s), ctypes.byref(res), None, None, (1 << 40) + 1, None, None) == INVALID
     tr = G._lib.Trace(16, None, None, None, None)          # rows promised, no arrays
     assert lib.gpugo_solve(ctypes.byref(s), ctypes.byref(res), None, None, 4, None, ctypes.byref(tr)) == INVALID
+    adm = ctypes.c_int64(-5)
+    tk = np.zeros(2, dtype=np.int64)
+    assert lib.gpugo_submit_batch(None, ctypes.byref(s), 1, None, None, 0, None, tk.ctypes.data,
+                                  ctypes.byref(adm)) == INVALID
+    assert lib.gpugo_submit_batch(None, None, 0, None, None, 0, None, None, None) == INVALID
     nr = ctypes.c_int64()
     assert lib.gpugo_combine(None, 3, 2, 1e-3, None, 0, ctypes.byref(nr)) == INVALID
     assert lib.gpugo_combine(out.ctypes.data_as(dp), 1, 2, -1.0, None, 0, ctypes.byref(nr)) == INVALID
@@ -147,13 +152,23 @@ def test_null_arguments_are_rejected_before_the_device(lib):
 
 def test_python_side_checks_array_sizes(lib):
     """The C ABI reads 2n bounds through plain pointers: the Python mirror
-    refuses a domain or a parent box of the wrong size before the call."""
+    refuses a domain or a parent box of the wrong size before the call (for a
+    batch admission, before anything is admitted)."""
     import numpy as np
     import gpugo_gb300 as G
     p = G.config2()
     p.domain = p.domain[:-2]                  # changed after construction
     with pytest.raises(ValueError):
         G._spec(p)
+
+    class NoEngine:                           # a call would fail: there is none
+        def __getattr__(self, name):
+            raise AssertionError(f"{name} called")
+    e = object.__new__(G.Engine)
+    e._L, e._h, e._pending = NoEngine(), None, {}
+    with pytest.raises(ValueError, match="problem 1"):
+        e.submit_many([G.config2(), p, G.config2()], box_cap=2)
+    assert e._pending == {}
     q = G.config2()
     with pytest.raises(ValueError):
         G.eval_children(q, q.domain[:6], 1, np.zeros(2, dtype=np.uint64), 1e300)
