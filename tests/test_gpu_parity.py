@@ -334,6 +334,12 @@ EDGE = [
     ("expsqrt9_s14", lambda: P.instance(P.EXPSQRT, 9, 34, 1e-5, samples=14)),
     ("prodcos5_s40", lambda: P.instance(P.PRODCOS, 5, 35, 1e-6, samples=40)),
     ("cosquad3_w9", lambda: P.instance(P.COSQUAD, 3, 36, 1e-6, split=(9, 3), samples=3)),
+    # lane groups of S lanes for short candidate queues: 4, 2 and 2 groups a warp
+    # with idle lanes above them, then the first S that takes a warp per candidate
+    ("chained6_s7", lambda: P.instance(P.CHAINED, 6, 37, 1e-6, samples=7)),
+    ("prodcos6_s12", lambda: P.instance(P.PRODCOS, 6, 38, 1e-6, samples=12)),
+    ("cosquad5_s16", lambda: P.instance(P.COSQUAD, 5, 39, 1e-6, samples=16)),
+    ("chained4_s17", lambda: P.instance(P.CHAINED, 4, 40, 1e-6, samples=17)),
 ]
 
 
@@ -345,6 +351,28 @@ def test_solve_trace_parity_edge_shapes(oracle_lib, name, make):
     p.max_iter = 3000
     rg, ro = _compare_solves(p, oracle_lib, box_cap=16)
     assert rg.status == G.CERTIFIED
+
+
+def test_lane_groups_of_mixed_sizes_in_one_batch(oracle_lib):
+    """Short queues with candidates of instances of different S side by side:
+    each round takes entries of one group size, the others wait for their own
+    rounds; every solve matches the oracle trace for trace."""
+    probs = [P.instance(fam, n, 60 + k, 1e-6, samples=S)
+             for k, (fam, n, S) in enumerate([(P.CHAINED, 5, 7), (P.CHAINED, 5, 10), (P.COSQUAD, 4, 12),
+                                               (P.PRODCOS, 4, 16), (P.CHAINED, 3, 17), (P.COSQUAD, 6, 1),
+                                               (P.EXPSQRT, 4, 10)])]
+    for p in probs:
+        p.max_iter = 3000
+    ros = [oracle_lib.solve(p, box_cap=8, trace_cap=100000) for p in probs]
+    with G.Engine(max_slots=len(probs), arena_bytes=2 << 30, cand_mode=G._lib.CAND_WARP) as eng:
+        tickets = [eng.submit(p, box_cap=8, trace_cap=100000) for p in probs]
+        eng.run(0)
+        done = dict(eng.poll())
+    for t, p, ro in zip(tickets, probs, ros):
+        rg = done[t]
+        assert (rg.iterations, rg.lb, rg.ub, rg.pool_size) == (ro.iterations, ro.lb, ro.ub, ro.pool_size), p.tag
+        for k in ("ub", "n_surv", "pool", "sel"):
+            assert _same(rg.trace[k], ro.trace[k]), (p.tag, k)
 
 
 def test_finalized_results_match_collected():
