@@ -1256,8 +1256,10 @@ __device__ void phase_bound(const KArgs& a) {
 // busy but runs the S passes one after the other, in claims of 32 or 64 that
 // leave warps idle when the queue is short.  Measured on the GB300 with the
 // 1024-instance mixed batch (S = 10): 108.4 ms to certified at 24 per warp, 107.8
-// at 32, 110.4 at 48, 124.2 at 96 and with no lane per candidate at all.
-constexpr long long LANE_FROM = 32;
+// at 32, 110.4 at 48, 124.2 at 96 and with no lane per candidate at all; with the
+// later tail hand-out and seed threshold 102.3 at 16, 99.5 at 20, 99.6 at 24, 101.4
+// at 32, 102.9 at 40.
+constexpr long long LANE_FROM = 24;
 // Candidates left per warp below which a lane-per-candidate pass hands its last
 // candidates out TAIL_CLAIM at a time (three groups of ten lanes for S = 10).
 // Measured with LANE_FROM 32: tails from 4, 8, 16, 32 per warp 105.6, 105.0,
