@@ -644,7 +644,7 @@ def main():
     ap.add_argument("--count", type=int, default=1024, help="instances of the batch")
     ap.add_argument("--serve-count", type=int, default=4096, help="requests of the serving record (0: none)")
     ap.add_argument("--rate", type=float, default=20000.0)
-    ap.add_argument("--slice", type=int, default=8, help="serving: iterations per run between admissions")
+    ap.add_argument("--slice", type=int, default=6, help="serving: iterations per run between admissions")
     ap.add_argument("--serve-order", default="shape", choices=["arrival", "shape"],
                     help="serving: waiting requests take free slots in arrival order or grouped by (family, n)")
     ap.add_argument("--arena-gb", type=int, default=80)
