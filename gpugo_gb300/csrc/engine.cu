@@ -1380,8 +1380,8 @@ __device__ void phase_seed(const KArgs& a) {
 
 // Pass 2: candidates claimed dynamically by warps; the warp finishing an
 // instance's last candidate queues it for its list update.  Short queues give a
-// whole warp to each candidate (samples and KKT coordinates across the lanes);
-// long queues give each lane its own candidate.
+// group of S lanes (or a whole warp) to each candidate (samples and KKT
+// coordinates across the lanes); long queues give each lane its own candidate.
 // Called by one lane; returns true when these were the instance's last candidates.
 __device__ __forceinline__ bool count_done(const KArgs& a, int s, long long n) {
   __threadfence();
@@ -1434,10 +1434,10 @@ __device__ void phase_candidates(const KArgs& a) {
   const long long b_lo = vload(a.ctl->b_lo);
   const int nA = a.ctl->nA;
   int chint = -1;
-  // With a short queue (a warp per candidate) the first claim of warp g (numbered
-  // across the blocks first) is the range g*K: the candidates land on warps of
-  // different SMs, which do not share an FP64 unit.  Later claims, and every
-  // claim of a long queue, come from the shared counter.
+  // With a short queue (lane groups or a warp per candidate) the first claim of
+  // warp g (numbered across the blocks first) is the range g*K: the candidates
+  // land on warps of different SMs, which do not share an FP64 unit.  Later
+  // claims, and every claim of a long queue, come from the shared counter.
   const unsigned long long g = (unsigned long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   bool first = K < 32;
@@ -1544,9 +1544,10 @@ __device__ void phase_candidates(const KArgs& a) {
       __syncwarp();
       continue;
     }
-    // A warp per candidate.  The claim (at most 32 entries) is loaded by the
-    // lanes at once and filtered against the current UB; the survivors of the
-    // filter are then processed one after the other by the whole warp.
+    // Lane groups or a warp per candidate.  The claim (at most 32 entries) is
+    // loaded by the lanes at once and filtered against the current UB; the
+    // survivors of the filter are then processed a group size at a time
+    // (group_candidate) or one after the other by the whole warp.
     {
       const unsigned long long q = h + lane;
       const bool valid = q < e;
