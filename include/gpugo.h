@@ -175,7 +175,10 @@ int gpugo_eval_children_static(const gpugo_spec* spec, const double* parent_box,
                                double* lb_out, double* samp_out, int32_t* flag_out);
 
 /* ---------------------------------------------------------------------------
- * Engines: many solves share one persistent kernel (batching and serving).
+ * Engines: many solves share one persistent kernel (batching and serving).  The
+ * reference runs one solve per script (GPUGO_1.1/1-Ackley/ackley50.py:950-1396);
+ * these calls have no counterpart there: each admitted problem is that script's
+ * solve, with the same inputs (gpugo_spec) and results (gpugo_result).
  * ------------------------------------------------------------------------- */
 typedef struct gpugo_engine gpugo_engine;
 
@@ -193,8 +196,10 @@ typedef struct gpugo_engine_cfg {
 } gpugo_engine_cfg;
 
 /* Candidate children (LB not above the UB) are sampled and KKT-tested either by
-   a whole warp each (sample points and coordinates across the lanes: short
-   queues) or by one lane each (long queues).  AUTO picks by queue length. */
+   a group of lanes each (S lanes for S <= 16 sample points, else a whole warp:
+   sample points and coordinates across the lanes; short queues, GPUGO_CAND_WARP)
+   or by one lane each (long queues, GPUGO_CAND_LANE).  AUTO picks by queue
+   length. */
 #define GPUGO_CAND_AUTO 0
 #define GPUGO_CAND_WARP 1
 #define GPUGO_CAND_LANE 2
